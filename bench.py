@@ -1,0 +1,436 @@
+"""Benchmark of the fused FP64 finite-volume step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload kh4096|ot1024|sod256] [--no-cpu-baseline]
+
+One step = one pass of the fused step (reconstruction + fluxes + update + CFL dt + the
+funk_time rotation) over the whole grid.  Metric: FP64 cell-updates/s, whole job.
+
+* value     K steps timed with CUDA events on the launching stream, state resident in HBM.
+* e2e       the same metric through the C ABI with HOST buffers: every step imports the
+            state from pinned host memory (gd_import), advances one step and exports it
+            back (gd_export); copies inside the timed region.
+* roofline  HBM roofline of the step kernel: algorithmic bytes per launch (each state field
+            read once and written once, 8 B each) / average launch time, against the
+            measured HBM bandwidth.  The step is FP64-issue bound on GB300; the "fp64"
+            object reports that fraction against the FP64 FMA rate measured in this run.
+* cpu_baseline  the oracle (the project's C restatement of the reference step, OpenMP over
+            all host cores) timed on a bounded sample of the same workload.
+
+--impl reference times the reference path on the host cores (the oracle port: the
+reference's own CUDA sources are compiled for the host only where they are present, and
+they are not on the GPU host) for the same workload, metric and unit.
+
+Multi-GPU (torchrun): replicas only -- every rank advances its own copy of the workload
+(the grid is not decomposed); value = all ranks' cell-updates / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (description, problem factory, bytes per cell-update)
+    "kh4096": "Kelvin-Helmholtz 4096x4096 periodic, Euler, HLLC + minmod, CFL 0.4, FP64",
+    "ot1024": "Orszag-Tang 1024x1024 periodic, ideal MHD, HLLD + minmod, CFL 0.4, FP64",
+    "sod256": "Sod 256x256 transmissive, Euler, HLLC + minmod, CFL 0.4, FP64",
+}
+L2_BYTES = 129 * 2 ** 20
+
+
+def make_problem(name, mode=0):
+    from golikov_2d_gb300 import problems
+    if name == "kh4096":
+        return problems.kelvin_helmholtz(4096, 4096, mode=mode)
+    if name == "ot1024":
+        return problems.orszag_tang(1024, 1024, mode=mode)
+    if name == "sod256":
+        return problems.sod(256, 256, mode=mode)
+    raise ValueError(name)
+
+
+def bytes_per_cell(cfg) -> int:
+    return 8 * 2 * cfg.nfields
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == workload:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def ncu_fp64_per_cell(workload):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == workload:
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.bus_id = bus_id
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        if self.bus_id:
+            cmd[1:1] = ["-i", self.bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
+    """The oracle on all host cores, `nsteps` full steps of the workload."""
+    import oracle
+    oracle.build(ref=False)
+    o = oracle.Oracle()
+    threads = threads or os.cpu_count() or 1
+    o.set_threads(threads)
+    grid = oracle.Grid(cfg.N, cfg.M, cfg.dx, cfg.dy, cfg.x0, cfg.y0, cfg.gamma, cfg.krit,
+                       physics=cfg.physics, geometry=cfg.geometry, order=cfg.order,
+                       method=cfg.method, bc=tuple(cfg.bc), frozen_radius=cfg.frozen_radius)
+    T_do = o.dt_only(grid, s, u, b)
+    t0 = time.perf_counter()
+    o.run(grid, s, u, b, nsteps, T_do)
+    dt = time.perf_counter() - t0
+    return {"value": cfg.N * cfg.M * nsteps / dt, "unit": "cell-updates/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{nsteps} full steps of {workload} ({cfg.N}x{cfg.M}) on {threads} host "
+                      f"threads, oracle/gd_oracle.c -O2 OpenMP, {dt:.2f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    cfg, s, u, b = make_problem(args.workload)
+    import oracle
+    oracle.build(ref=False)
+    o = oracle.Oracle()
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    grid = oracle.Grid(cfg.N, cfg.M, cfg.dx, cfg.dy, cfg.x0, cfg.y0, cfg.gamma, cfg.krit,
+                       physics=cfg.physics, geometry=cfg.geometry, order=cfg.order,
+                       method=cfg.method, bc=tuple(cfg.bc), frozen_radius=cfg.frozen_radius)
+    T_do = o.dt_only(grid, s, u, b)
+    # Each step is one full step of the workload; bounded so the run ends in minutes.
+    s, u, b, T_do, _ = o.run(grid, s, u, b, args.warmup, T_do)
+    t0 = time.perf_counter()
+    o.run(grid, s, u, b, args.steps, T_do)
+    dt = time.perf_counter() - t0
+    K = cfg.N * cfg.M
+    value = K * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "FP64 cell-updates/s", "value": value,
+        "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "cells": K, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{args.steps} full steps of {args.workload} after "
+                                   f"{args.warmup} warm-up steps, oracle/gd_oracle.c "
+                                   f"(restatement of the reference step) on {threads} threads"},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def time_workload(name, steps, warmup, torch, g, flush_l2):
+    """Device-resident timing of `steps` steps; returns (ms per step, launches)."""
+    cfg, s, u, b = make_problem(name)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.advance(warmup)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda") if flush_l2 else None
+    l0 = sol.launch_count()
+    if flush_l2:
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for a, z in evs:
+            flush.fill_(1.0)
+            a.record(stream)
+            sol.advance(1)
+            z.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(z) for a, z in evs) / steps
+    else:
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sol.advance(steps)
+        z.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(z) / steps
+    launches = sol.launch_count() - l0
+    st = sol.stats(allow_nonfinite=True)
+    sol.close()
+    return cfg, ms, launches, st
+
+
+def run_gb300(args):
+    import torch
+    import golikov_2d_gb300 as g
+    from golikov_2d_gb300 import _build
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    _build.build()
+    g.load()
+
+    cfg, s, u, b = make_problem(args.workload)
+    K = cfg.N * cfg.M
+    state_bytes = K * cfg.nfields * 8
+    flush_l2 = 2 * state_bytes <= 2 * L2_BYTES  # both ping-pong buffers could sit in L2
+
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.advance(args.warmup)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    bus = None
+    try:
+        props = torch.cuda.get_device_properties(local)
+        bus = f"{props.pci_domain_id:08X}:{props.pci_bus_id:02X}:{props.pci_device_id:02X}.0"
+    except Exception:
+        bus = None
+
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = sol.launch_count()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda") if flush_l2 else None
+    with ClockSampler(bus) as clk:
+        if flush_l2:
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+            for a, z in evs:
+                flush.fill_(1.0)
+                a.record(stream)
+                sol.advance(1)
+                z.record(stream)
+            torch.cuda.synchronize()
+            ms_total = sum(a.elapsed_time(z) for a, z in evs)
+        else:
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sol.advance(args.steps)
+            z.record(stream)
+            torch.cuda.synchronize()
+            ms_total = a.elapsed_time(z)
+    launches = sol.launch_count() - l0
+    if ws > 1:
+        t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    stats = sol.stats(allow_nonfinite=True)
+    ms_step = ms_total / args.steps
+    value = ws * K * args.steps / (ms_total * 1e-3)
+
+    # ---- e2e: host buffers through the C ABI, copies inside the timed region ---------------
+    hs = torch.from_numpy(s).pin_memory()
+    hu = torch.from_numpy(u).pin_memory()
+    hb = torch.from_numpy(b).pin_memory() if b is not None else None
+    hs2, hu2 = torch.empty_like(hs).pin_memory(), torch.empty_like(hu).pin_memory()
+    hb2 = torch.empty_like(hb).pin_memory() if hb is not None else None
+    e2e_steps = max(1, min(args.steps, 10))
+    sol.import_state(hs, hu, hb)
+    sol.advance(1)
+    sol.export_state(hs2, hu2, hb2)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sol.import_state(hs, hu, hb)
+        sol.advance(1)
+        sol.export_state(hs2, hu2, hb2)  # synchronises the stream
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    io_bytes = K * (4 + (3 if b is not None else 0)) * 8
+    e2e = {"value": ws * K * e2e_steps / e2e_s, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+           "path": "gd_import(host, pinned) + gd_advance(1) + gd_export(host) per step"}
+    sol.close()
+
+    if rank != 0:
+        return 0
+
+    peak_gbs, peak_kind = measured_peaks()
+    alg_bytes = K * bytes_per_cell(cfg)
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic = ncu_traffic(args.workload)
+    fp64_peak = g.probe_fp64_peak()
+    dp_per_cell = ncu_fp64_per_cell(args.workload)
+    fp64 = {"peak_flops": fp64_peak, "peak_kind": "measured in this run (DFMA loop, FMA = 2)"}
+    if dp_per_cell is not None:
+        fl = dp_per_cell * K / (ms_step * 1e-3)
+        fp64.update({"flops_per_cell": dp_per_cell, "achieved_flops": fl,
+                     "frac": fl / fp64_peak if fp64_peak else None,
+                     "source": "ncu FP64 instruction counts, profiles/ncu_traffic.txt"})
+    line = {
+        "metric": "FP64 cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "cells": K, "fields": cfg.nfields,
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "flushed before every timed step" if flush_l2 else
+                         f"state {2 * state_bytes / 2**20:.0f} MiB > L2 (129 MiB), no flush",
+                   "steps_per_launch": 1, "dt": "lagged reference protocol, dt-only pre-pass"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved / peak_gbs,
+                     "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "note": "FP64-issue bound on GB300; see fp64"},
+        "fp64": fp64,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "sim": {"t": stats.t, "dt": stats.dt, "steps": stats.steps,
+                "rho_floor_hits": stats.rho_floor_hits, "p_floor_hits": stats.p_floor_hits,
+                "nonfinite": stats.nonfinite},
+    }
+    if args.secondary and args.workload != "ot1024":
+        try:
+            c2, ms2, l2, st2 = time_workload("ot1024", args.steps, args.warmup, torch, g, True)
+            K2 = c2.N * c2.M
+            ach2 = K2 * bytes_per_cell(c2) / (ms2 * 1e-3) / 1e9
+            line["secondary"] = {"workload": WORKLOADS["ot1024"], "value": K2 / (ms2 * 1e-3),
+                                 "unit": "cell-updates/s", "ms_per_step": ms2,
+                                 "roofline": {"bound": "hbm", "achieved": ach2, "peak": peak_gbs,
+                                              "unit": "GB/s", "frac": ach2 / peak_gbs,
+                                              "traffic": ncu_traffic("ot1024")},
+                                 "gpu_launches": l2}
+        except Exception as e:  # the MHD fast path may be unavailable in this build
+            line["secondary"] = {"workload": WORKLOADS["ot1024"], "unavailable": str(e)}
+    if not args.no_cpu_baseline and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(args.workload, cfg, s, u, b)
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="kh4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--secondary", type=int, default=1)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

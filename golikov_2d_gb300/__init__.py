@@ -1,0 +1,251 @@
+"""golikov_2d_gb300 -- GB300-native finite-volume step for 2-D Euler and ideal MHD.
+
+Python mirror of the C ABI in ``include/gd2d.h`` (ctypes over ``libgd2d.so``).  The
+reference's interface for this path is its kernel launch protocol (kernel.cu main()):
+
+    Kernel_TVD<<<K/256, 256>>>(s, u, b, s2, u2, b2, T, T_do, i, method)   # one step
+    funk_time<<<1, 1>>>(T, T_do, TT, i)                                   # dt rotation
+
+``kernel_step`` and ``funk_time`` below keep those names' argument roles and take CUDA
+tensors (device pointers) in the reference's AoS layout.  ``Solver`` wraps the resident
+state (import / advance / export) used by the benchmark.
+
+The CUDA library is required: importing works without a GPU, but every compute call
+raises if ``libgd2d.so`` is missing or no CUDA device is present.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgd2d.so")
+
+EULER, MHD = 0, 1
+CARTESIAN, AXISYM = 0, 1
+METHOD_HLLC, METHOD_HLLC_MHD, METHOD_HLLD = 1, 2, 3
+(BC_PERIODIC, BC_TRANSMISSIVE, BC_MIRROR_X, BC_AXIS, BC_AMBIENT, BC_OUTFLOW,
+ BC_AMBIENT_KEEPB) = range(7)
+MODE_FAST, MODE_PARITY = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "non-finite state",
+          4: "device wait timed out", 5: "unsupported combination"}
+
+# Every symbol include/gd2d.h declares (checked by the tests against the built library).
+EXPORTS = (
+    "gd_create", "gd_destroy", "gd_get_config", "gd_status_string", "gd_last_cuda_error",
+    "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
+    "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
+    "gd_probe_fp64_peak",
+)
+
+
+class GdError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {STATUS.get(status, status)} (status {status})")
+        self.status = status
+
+
+class gd_config(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int), ("M", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+        ("x0", ctypes.c_double), ("y0", ctypes.c_double),
+        ("gamma", ctypes.c_double), ("krit", ctypes.c_double),
+        ("physics", ctypes.c_int), ("geometry", ctypes.c_int),
+        ("order", ctypes.c_int), ("method", ctypes.c_int),
+        ("bc", ctypes.c_int * 4),
+        ("frozen_radius", ctypes.c_double),
+        ("mode", ctypes.c_int),
+    ]
+
+
+class gd_stats(ctypes.Structure):
+    _fields_ = [
+        ("t", ctypes.c_double), ("dt", ctypes.c_double), ("dt_next", ctypes.c_double),
+        ("steps", ctypes.c_longlong), ("rho_floor_hits", ctypes.c_longlong),
+        ("p_floor_hits", ctypes.c_longlong), ("nonfinite", ctypes.c_longlong),
+    ]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libgd2d.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with golikov_2d_gb300._build.build() "
+                           "(there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    cfgp = ctypes.POINTER(gd_config)
+    L.gd_create.argtypes = [cfgp, ctypes.POINTER(vp)]
+    L.gd_destroy.argtypes = [vp]
+    L.gd_get_config.argtypes = [vp, cfgp]
+    L.gd_status_string.restype = ctypes.c_char_p
+    L.gd_status_string.argtypes = [i]
+    L.gd_step_ref.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i, vp]
+    L.gd_funk_time.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.gd_import.argtypes = [vp, vp, vp, vp, i, vp]
+    L.gd_export.argtypes = [vp, vp, vp, vp, i, vp]
+    L.gd_set_time.argtypes = [vp, d, d, vp]
+    L.gd_init_dt.argtypes = [vp, vp]
+    L.gd_advance.argtypes = [vp, i, i, vp]
+    L.gd_get_stats.argtypes = [vp, ctypes.POINTER(gd_stats), vp]
+    L.gd_field_ptr.argtypes = [vp, i, ctypes.POINTER(vp)]
+    L.gd_launch_count.restype = ll
+    L.gd_launch_count.argtypes = [vp]
+    L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
+    for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
+                 "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
+                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak"):
+        getattr(L, name).restype = i
+    _lib = L
+    return L
+
+
+def _check(status: int, what: str) -> None:
+    if status != 0:
+        raise GdError(status, what)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream or None
+    return getattr(stream, "cuda_stream", stream) or None
+
+
+@dataclass
+class Config:
+    """Grid, physics and boundaries (gd_config)."""
+    N: int
+    M: int
+    dx: float
+    dy: float
+    x0: float
+    y0: float
+    gamma: float
+    krit: float
+    physics: int = EULER
+    geometry: int = CARTESIAN
+    order: int = 2
+    method: int = METHOD_HLLC
+    bc: tuple = (BC_TRANSMISSIVE,) * 4
+    frozen_radius: float = 0.0
+    mode: int = MODE_FAST
+
+    def cstruct(self) -> gd_config:
+        c = gd_config()
+        for name, _ in gd_config._fields_:
+            if name == "bc":
+                for k in range(4):
+                    c.bc[k] = int(self.bc[k])
+            else:
+                setattr(c, name, getattr(self, name))
+        return c
+
+    @property
+    def nfields(self) -> int:
+        return 7 if self.physics == MHD else 4
+
+
+class Solver:
+    """A context: resident state, dt scalars and the step kernels for one grid."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        self.lib = load()
+        self._c = cfg.cstruct()
+        h = ctypes.c_void_p()
+        _check(self.lib.gd_create(ctypes.byref(self._c), ctypes.byref(h)), "gd_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.gd_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the reference's launch protocol (device pointers, AoS layout) ------------------------
+    def kernel_step(self, s, u, b, s2, u2, b2, T, T_do, i=0, method=0, stream=None) -> None:
+        """gd_step_ref: Kernel_TVD / add2 / Ker_Dekard on CUDA tensors."""
+        p = lambda t: None if t is None else t.data_ptr()
+        _check(self.lib.gd_step_ref(self.handle, p(s), p(u), p(b), p(s2), p(u2), p(b2), p(T),
+                                    p(T_do), int(i), int(method), _stream_handle(stream)),
+               "gd_step_ref")
+
+    def funk_time(self, T, T_do, TT, i, stream=None) -> None:
+        _check(self.lib.gd_funk_time(self.handle, T.data_ptr(), T_do.data_ptr(), TT.data_ptr(),
+                                     i.data_ptr(), _stream_handle(stream)), "gd_funk_time")
+
+    # -- resident state ------------------------------------------------------------------------
+    def import_state(self, s, u, b=None, stream=None) -> None:
+        """Load AoS state from torch tensors (CPU or CUDA) or numpy arrays (host)."""
+        host, ptrs = self._ptrs(s, u, b)
+        _check(self.lib.gd_import(self.handle, *ptrs, 1 if host else 0, _stream_handle(stream)),
+               "gd_import")
+
+    def export_state(self, s, u, b=None, stream=None) -> None:
+        host, ptrs = self._ptrs(s, u, b)
+        _check(self.lib.gd_export(self.handle, *ptrs, 1 if host else 0, _stream_handle(stream)),
+               "gd_export")
+
+    @staticmethod
+    def _ptrs(s, u, b):
+        import numpy as np
+        if isinstance(s, np.ndarray):
+            arrs = [s, u, b]
+            for a in arrs:
+                if a is not None:
+                    assert a.dtype == np.float64 and a.flags.c_contiguous
+            return True, [None if a is None else a.ctypes.data for a in arrs]
+        host = not s.is_cuda
+        return host, [None if t is None else t.data_ptr() for t in (s, u, b)]
+
+    def set_time(self, T_do: float, TT: float = 0.0, stream=None) -> None:
+        _check(self.lib.gd_set_time(self.handle, float(T_do), float(TT), _stream_handle(stream)),
+               "gd_set_time")
+
+    def init_dt(self, stream=None) -> None:
+        _check(self.lib.gd_init_dt(self.handle, _stream_handle(stream)), "gd_init_dt")
+
+    def advance(self, nsteps: int, use_graph: bool = False, stream=None) -> None:
+        _check(self.lib.gd_advance(self.handle, int(nsteps), 1 if use_graph else 0,
+                                   _stream_handle(stream)), "gd_advance")
+
+    def stats(self, stream=None, allow_nonfinite: bool = False) -> gd_stats:
+        st = gd_stats()
+        r = self.lib.gd_get_stats(self.handle, ctypes.byref(st), _stream_handle(stream))
+        if not (r == 3 and allow_nonfinite):
+            _check(r, "gd_get_stats")
+        return st
+
+    def field_ptr(self, f: int) -> int:
+        p = ctypes.c_void_p()
+        _check(self.lib.gd_field_ptr(self.handle, int(f), ctypes.byref(p)), "gd_field_ptr")
+        return p.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.gd_launch_count(self.handle))
+
+
+def probe_fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the current device in FLOP/s."""
+    L = load()
+    v = ctypes.c_double()
+    _check(L.gd_probe_fp64_peak(ctypes.byref(v)), "gd_probe_fp64_peak")
+    return v.value

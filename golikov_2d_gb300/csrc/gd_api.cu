@@ -1,0 +1,400 @@
+// gd_api.cu -- host side of the C ABI declared in include/gd2d.h.
+//
+// Replaces the host part of the reference's main() (kernel.cu:3810-4470): allocation,
+// host<->device transfer, the ping-pong step loop with funk_time, and error checks.  The
+// reference checks every launch with cudaGetLastError + cudaDeviceSynchronize and calls
+// exit(-1) (kernel.cu:4044-4084); here every entry point returns a status, never exits,
+// and never synchronises unless it says so.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+#include <utility>
+
+#include "../../include/gd2d.h"
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+
+using gd::CPlanes;
+using gd::Params;
+using gd::Planes;
+using gd::Scalars;
+
+namespace {
+std::atomic<int> g_last_cuda_error{0};
+
+gd_status cuda_fail(cudaError_t e) {
+    g_last_cuda_error.store((int)e);
+    return GD_ERR_CUDA;
+}
+}  // namespace
+
+#define GD_CUDA(call)                                 \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_);  \
+    } while (0)
+
+struct gd_ctx {
+    gd_config cfg;
+    Params P;
+    int nf = 4;
+    long long K = 0;
+    int device = 0;
+    double* state[2] = {nullptr, nullptr};  // nf planes of K doubles each
+    int cur = 0;
+    Scalars* sc = nullptr;                  // device scalars of the resident state
+    double* ref_planes = nullptr;           // 2 * nf * K: SoA in/out for gd_step_ref
+    double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
+    long long launches = 0;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
+
+    Planes planes(int which) const {
+        Planes p{};
+        for (int f = 0; f < gd::kMaxFields; ++f)
+            p.f[f] = f < nf ? state[which] + (size_t)f * K : nullptr;
+        return p;
+    }
+    static CPlanes cplanes(const Planes& p) {
+        CPlanes c{};
+        for (int f = 0; f < gd::kMaxFields; ++f) c.f[f] = p.f[f];
+        return c;
+    }
+    Planes ref_plane_set(int which) const {
+        Planes p{};
+        for (int f = 0; f < gd::kMaxFields; ++f)
+            p.f[f] = f < nf ? ref_planes + ((size_t)which * nf + f) * K : nullptr;
+        return p;
+    }
+};
+
+namespace {
+
+bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
+
+gd_status validate(const gd_config* c) {
+    if (!c) return GD_ERR_INVALID_ARG;
+    if (c->N < 3 || c->M < 3 || c->N > (1 << 28) || c->M > (1 << 28)) return GD_ERR_INVALID_ARG;
+    if ((long long)c->N * c->M > (1LL << 40)) return GD_ERR_INVALID_ARG;
+    if (!finite_pos(c->dx) || !finite_pos(c->dy)) return GD_ERR_INVALID_ARG;
+    if (!std::isfinite(c->x0) || !std::isfinite(c->y0)) return GD_ERR_INVALID_ARG;
+    if (!(std::isfinite(c->gamma) && c->gamma > 1.0)) return GD_ERR_INVALID_ARG;
+    if (!finite_pos(c->krit)) return GD_ERR_INVALID_ARG;
+    if (c->physics != GD_EULER && c->physics != GD_MHD) return GD_ERR_INVALID_ARG;
+    if (c->geometry != GD_CARTESIAN && c->geometry != GD_AXISYM) return GD_ERR_INVALID_ARG;
+    if (c->order != 1 && c->order != 2) return GD_ERR_INVALID_ARG;
+    if (c->mode != GD_MODE_FAST && c->mode != GD_MODE_PARITY) return GD_ERR_INVALID_ARG;
+    if (c->physics == GD_EULER && c->method != GD_METHOD_HLLC) return GD_ERR_INVALID_ARG;
+    if (c->physics == GD_MHD && c->method != GD_METHOD_HLLC_MHD && c->method != GD_METHOD_HLLD)
+        return GD_ERR_INVALID_ARG;
+    for (int s = 0; s < 4; ++s)
+        if (c->bc[s] < GD_BC_PERIODIC || c->bc[s] > GD_BC_AMBIENT_KEEPB) return GD_ERR_INVALID_ARG;
+    if ((c->bc[0] == GD_BC_PERIODIC) != (c->bc[1] == GD_BC_PERIODIC)) return GD_ERR_INVALID_ARG;
+    if ((c->bc[2] == GD_BC_PERIODIC) != (c->bc[3] == GD_BC_PERIODIC)) return GD_ERR_INVALID_ARG;
+    // the axisymmetric sources divide by the radius y of every cell centre
+    if (c->geometry == GD_AXISYM && !(c->y0 > 0.0)) return GD_ERR_INVALID_ARG;
+    if (!(std::isfinite(c->frozen_radius) && c->frozen_radius >= 0.0)) return GD_ERR_INVALID_ARG;
+    return GD_OK;
+}
+
+Params make_params(const gd_config& c) {
+    Params P{};
+    P.N = c.N;
+    P.M = c.M;
+    P.physics = c.physics;
+    P.geometry = c.geometry;
+    P.order = c.order;
+    P.method = c.method;
+    for (int s = 0; s < 4; ++s) P.bc[s] = c.bc[s];
+    P.dx = c.dx;
+    P.dy = c.dy;
+    P.x0 = c.x0;
+    P.y0 = c.y0;
+    P.gamma = c.gamma;
+    P.krit = c.krit;
+    P.frozen_radius = c.frozen_radius;
+    P.gm1 = c.gamma - 1.0;
+    P.inv_gm1 = 1.0 / (c.gamma - 1.0);
+    P.ambient_p = 1.0 / c.gamma;
+    // rad passed to the flux: dy on x-faces in the Euler kernels (kernel.cu:1811, 3562),
+    // dx on x-faces in the MHD kernels (kernel.cu:2560)
+    if (c.physics == GD_EULER) {
+        P.krad_x = c.krit * c.dy;
+        P.krad_y = c.krit * c.dx;
+    } else {
+        P.krad_x = c.krit * c.dx;
+        P.krad_y = c.krit * c.dy;
+    }
+    return P;
+}
+
+cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const Planes& out,
+                        const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                        Scalars* ctr, int dt_only, cudaStream_t st) {
+    ctx->launches += 1;
+    if (ctx->cfg.mode == GD_MODE_PARITY)
+        return gd::launch_parity(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+    if (P.physics == GD_EULER)
+        return gd::launch_euler_fast(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+    return gd::launch_mhd_fast(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gd_abi_version(void) { return GD_ABI_VERSION; }
+
+int gd_last_cuda_error(void) { return g_last_cuda_error.load(); }
+
+const char* gd_status_string(gd_status s) {
+    switch (s) {
+        case GD_OK: return "ok";
+        case GD_ERR_INVALID_ARG: return "invalid argument";
+        case GD_ERR_CUDA: return "CUDA error";
+        case GD_ERR_NONPHYSICAL: return "non-finite state";
+        case GD_ERR_TIMEOUT: return "device wait timed out";
+        case GD_ERR_UNSUPPORTED: return "unsupported combination";
+    }
+    return "unknown status";
+}
+
+gd_status gd_create(const gd_config* cfg, gd_ctx** out) {
+    if (!out) return GD_ERR_INVALID_ARG;
+    *out = nullptr;
+    gd_status v = validate(cfg);
+    if (v != GD_OK) return v;
+    gd_ctx* ctx = new (std::nothrow) gd_ctx();
+    if (!ctx) return GD_ERR_INVALID_ARG;
+    ctx->cfg = *cfg;
+    ctx->P = make_params(*cfg);
+    ctx->nf = cfg->physics == GD_MHD ? 7 : 4;
+    ctx->K = (long long)cfg->N * cfg->M;
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    const size_t plane_bytes = sizeof(double) * (size_t)ctx->K * ctx->nf;
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->state[0], plane_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->state[1], plane_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->sc, sizeof(Scalars));
+    if (e == cudaSuccess) e = cudaMemset(ctx->sc, 0, sizeof(Scalars));
+    if (e == cudaSuccess) {
+        Scalars h{};
+        h.T_do = 1e-8;  // main(): *host_T_do = 0.00000001 (kernel.cu:3861)
+        double reset = gd::kTReset;
+        std::memcpy(&h.T_bits, &reset, sizeof(double));
+        e = cudaMemcpy(ctx->sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && cfg->mode == GD_MODE_FAST)
+        e = cfg->physics == GD_EULER ? gd::prepare_euler_fast() : gd::prepare_mhd_fast();
+    if (e == cudaSuccess) e = cudaMemset(ctx->state[0], 0, plane_bytes);
+    if (e == cudaSuccess) e = cudaMemset(ctx->state[1], 0, plane_bytes);
+    if (e != cudaSuccess) {
+        gd_destroy(ctx);
+        return cuda_fail(e);
+    }
+    *out = ctx;
+    return GD_OK;
+}
+
+gd_status gd_destroy(gd_ctx* ctx) {
+    if (!ctx) return GD_ERR_INVALID_ARG;
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(ctx->state[0]);
+    cudaFree(ctx->state[1]);
+    cudaFree(ctx->sc);
+    cudaFree(ctx->ref_planes);
+    cudaFree(ctx->aos);
+    delete ctx;
+    return GD_OK;
+}
+
+gd_status gd_get_config(const gd_ctx* ctx, gd_config* out) {
+    if (!ctx || !out) return GD_ERR_INVALID_ARG;
+    *out = ctx->cfg;
+    return GD_OK;
+}
+
+gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                      double* s2, double* u2, double* b2, double* T, const double* T_do, int i,
+                      int method, gd_stream stream) {
+    (void)i;
+    if (!ctx || !s || !u || !s2 || !u2 || !T || !T_do) return GD_ERR_INVALID_ARG;
+    if (ctx->nf == 7 && (!b || !b2)) return GD_ERR_INVALID_ARG;
+    Params P = ctx->P;
+    if (method > 0) {
+        if (ctx->cfg.physics == GD_EULER && method != GD_METHOD_HLLC) return GD_ERR_INVALID_ARG;
+        if (ctx->cfg.physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
+            return GD_ERR_INVALID_ARG;
+        P.method = method;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!ctx->ref_planes)
+        GD_CUDA(cudaMalloc(&ctx->ref_planes, sizeof(double) * 2 * (size_t)ctx->nf * ctx->K));
+    const Planes pin = ctx->ref_plane_set(0), pout = ctx->ref_plane_set(1);
+    GD_CUDA(gd::launch_aos_to_soa(s, u, b, pin, ctx->K, ctx->nf, st));
+    ctx->launches += 1;
+    GD_CUDA(launch_step(ctx, P, gd_ctx::cplanes(pin), pout, T_do, (unsigned long long*)T, nullptr,
+                        ctx->sc, 0, st));
+    GD_CUDA(gd::launch_soa_to_aos(gd_ctx::cplanes(pout), s2, u2, b2, ctx->K, ctx->nf, st));
+    ctx->launches += 1;
+    return GD_OK;
+}
+
+gd_status gd_funk_time(gd_ctx* ctx, double* T, double* T_do, double* TT, int* i,
+                       gd_stream stream) {
+    if (!ctx || !T || !T_do || !TT || !i) return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::launch_funk_time(T, T_do, TT, i, (cudaStream_t)stream));
+    ctx->launches += 1;
+    return GD_OK;
+}
+
+gd_status gd_import(gd_ctx* ctx, const double* s, const double* u, const double* b, int is_host,
+                    gd_stream stream) {
+    if (!ctx || !s || !u || (ctx->nf == 7 && !b)) return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const double *ds = s, *du = u, *db = b;
+    if (is_host) {
+        if (!ctx->aos) GD_CUDA(cudaMalloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
+        double* hs = ctx->aos;
+        double* hu = hs + 2 * ctx->K;
+        double* hb = hu + 2 * ctx->K;
+        GD_CUDA(cudaMemcpyAsync(hs, s, sizeof(double) * 2 * ctx->K, cudaMemcpyHostToDevice, st));
+        GD_CUDA(cudaMemcpyAsync(hu, u, sizeof(double) * 2 * ctx->K, cudaMemcpyHostToDevice, st));
+        if (ctx->nf == 7)
+            GD_CUDA(cudaMemcpyAsync(hb, b, sizeof(double) * 3 * ctx->K, cudaMemcpyHostToDevice, st));
+        ds = hs;
+        du = hu;
+        db = hb;
+    }
+    GD_CUDA(gd::launch_aos_to_soa(ds, du, db, ctx->planes(ctx->cur), ctx->K, ctx->nf, st));
+    ctx->launches += 1;
+    return GD_OK;
+}
+
+gd_status gd_export(gd_ctx* ctx, double* s, double* u, double* b, int is_host, gd_stream stream) {
+    if (!ctx || !s || !u || (ctx->nf == 7 && !b)) return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    double *ds = s, *du = u, *db = b;
+    if (is_host) {
+        if (!ctx->aos) GD_CUDA(cudaMalloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
+        ds = ctx->aos;
+        du = ds + 2 * ctx->K;
+        db = du + 2 * ctx->K;
+    }
+    GD_CUDA(gd::launch_soa_to_aos(gd_ctx::cplanes(ctx->planes(ctx->cur)), ds, du, db, ctx->K,
+                                  ctx->nf, st));
+    ctx->launches += 1;
+    if (is_host) {
+        GD_CUDA(cudaMemcpyAsync(s, ds, sizeof(double) * 2 * ctx->K, cudaMemcpyDeviceToHost, st));
+        GD_CUDA(cudaMemcpyAsync(u, du, sizeof(double) * 2 * ctx->K, cudaMemcpyDeviceToHost, st));
+        if (ctx->nf == 7)
+            GD_CUDA(cudaMemcpyAsync(b, db, sizeof(double) * 3 * ctx->K, cudaMemcpyDeviceToHost, st));
+        GD_CUDA(cudaStreamSynchronize(st));
+    }
+    return GD_OK;
+}
+
+gd_status gd_set_time(gd_ctx* ctx, double T_do, double TT, gd_stream stream) {
+    if (!ctx || !(std::isfinite(T_do) && T_do >= 0.0) || !std::isfinite(TT))
+        return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::launch_set_time(ctx->sc, T_do, TT, (cudaStream_t)stream));
+    ctx->launches += 1;
+    return GD_OK;
+}
+
+gd_status gd_init_dt(gd_ctx* ctx, gd_stream stream) {
+    if (!ctx) return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    GD_CUDA(gd::launch_reset_T(ctx->sc, st));
+    ctx->launches += 1;
+    const Planes cur = ctx->planes(ctx->cur);
+    GD_CUDA(launch_step(ctx, ctx->P, gd_ctx::cplanes(cur), ctx->planes(1 - ctx->cur),
+                        &ctx->sc->T_do, &ctx->sc->T_bits, nullptr, nullptr, 1, st));
+    GD_CUDA(gd::launch_dt_commit(ctx->sc, st));
+    ctx->launches += 1;
+    return GD_OK;
+}
+
+static gd_status advance_plain(gd_ctx* ctx, int nsteps, cudaStream_t st) {
+    for (int s = 0; s < nsteps; ++s) {
+        const Planes in = ctx->planes(ctx->cur), out = ctx->planes(1 - ctx->cur);
+        GD_CUDA(launch_step(ctx, ctx->P, gd_ctx::cplanes(in), out, &ctx->sc->T_do,
+                            &ctx->sc->T_bits, ctx->sc, ctx->sc, 0, st));
+        ctx->cur ^= 1;
+    }
+    return GD_OK;
+}
+
+gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream) {
+    if (!ctx || nsteps < 0) return GD_ERR_INVALID_ARG;
+    if (nsteps == 0) return GD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!use_graph) return advance_plain(ctx, nsteps, st);
+    const auto key = std::make_pair(nsteps, ctx->cur);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+        cudaStream_t cap = st;
+        bool own = false;
+        if (cap == nullptr) {  // the legacy default stream cannot be captured
+            GD_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            own = true;
+        }
+        const int cur0 = ctx->cur;
+        const long long l0 = ctx->launches;
+        cudaGraph_t g = nullptr;
+        GD_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        gd_status s = advance_plain(ctx, nsteps, cap);
+        cudaError_t ce = cudaStreamEndCapture(cap, &g);
+        ctx->cur = cur0;  // capture did not execute anything
+        ctx->launches = l0;
+        if (own) cudaStreamDestroy(cap);
+        if (s != GD_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce);
+        cudaGraphExec_t ge = nullptr;
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ce);
+        it = ctx->graphs.emplace(key, ge).first;
+    }
+    GD_CUDA(cudaGraphLaunch(it->second, st));
+    ctx->launches += nsteps;
+    if (nsteps & 1) ctx->cur ^= 1;
+    return GD_OK;
+}
+
+gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream) {
+    if (!ctx || !out) return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scalars h{};
+    GD_CUDA(cudaMemcpyAsync(&h, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    GD_CUDA(cudaStreamSynchronize(st));
+    double T;
+    std::memcpy(&T, &h.T_bits, sizeof(double));
+    out->t = h.TT;
+    out->dt = h.T_do;
+    out->dt_next = T;
+    out->steps = h.step;
+    out->rho_floor_hits = (long long)h.rho_floor;
+    out->p_floor_hits = (long long)h.p_floor;
+    out->nonfinite = (long long)h.nonfinite;
+    return h.nonfinite ? GD_ERR_NONPHYSICAL : GD_OK;
+}
+
+gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out) {
+    if (!ctx || !out || f < 0 || f >= ctx->nf) return GD_ERR_INVALID_ARG;
+    *out = ctx->state[ctx->cur] + (size_t)f * ctx->K;
+    return GD_OK;
+}
+
+long long gd_launch_count(const gd_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+gd_status gd_probe_fp64_peak(double* flops_out) {
+    if (!flops_out) return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::probe_fp64_peak(flops_out));
+    return GD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,310 @@
+// gd_fast_euler.cu -- fused minmod-TVD + HLLC + update step for 2-D Euler, face-once tiles.
+//
+// One CTA owns a TX x TY tile.  Phases, separated by __syncthreads():
+//   L  load the tile plus a 2-cell cross-shaped halo (boundary ghosts applied) into smem;
+//   S  per-cell minmod slopes along x and y (integer-pipe minmod, one FP64 sub per edge);
+//   F  every face of the tile once: left/right face states from the slopes, the HLLC flux
+//      in the face's local (normal, tangent) frame, and the face's wave-speed maximum;
+//   U  conservative update of each cell from its four face fluxes, positivity floors,
+//      primitive recovery; store; block dt minimum and the fused funk_time rotation.
+// The reference computes every face twice, once from each neighbour (kernel.cu:3560-3586);
+// here each face is computed once and used with opposite signs by its two cells.
+//
+// Reference semantics kept: primitive reconstruction of (rho, p, vx, vy) with the rho/p
+// face fallback to the cell value (kernel.cu:3436-3544), Davis wave speeds and the HLLC
+// star states of HLLC_Aleksashov (kernel.cu:853-1165), the Ker_Dekard update and floors
+// rho <= 0 -> 1e-4, p <= 0 -> 1e-6 (kernel.cu:1849-1874), dt = min over faces of
+// krit*rad/max(|SL|,|SR|) with rad = dy on x-faces (kernel.cu:1811).
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+
+namespace gd {
+namespace {
+
+constexpr int TX = 32;
+constexpr int TY = 16;
+constexpr int NT = 256;
+constexpr int NF = 4;
+
+struct FluxE {
+    double m, mn, mt, e;
+};
+
+// HLLC flux in a local frame: un = normal velocity, ut = in-plane tangential velocity.
+// Returns the flux (mass, normal momentum, tangential momentum, energy) and, in UU,
+// max(|SL|, |SR|).
+__device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, double utL,
+                                            double rR, double pR, double unR, double utR,
+                                            const Params& P, double& UU) {
+    const double g = P.gamma;
+    const double gpL = g * pL, gpR = g * pR;
+    const double cL = gpL * rsqrt_fast(gpL * rL);  // sqrt(g p / rho)
+    const double cR = gpR * rsqrt_fast(gpR * rR);
+    const double aL = unL - cL, aR = unR - cR;
+    const double bL = unL + cL, bR = unR + cR;
+    const double SL = aR < aL ? aR : aL;  // Davis estimates (kernel.cu:981-982)
+    const double SR = bL < bR ? bR : bL;
+    const double suL = SL - unL, suR = SR - unR;
+    const double mL = rL * suL, mR = rR * suR;
+    const double SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
+    UU = max_nonneg(dabs(SL), dabs(SR));
+
+    // Side whose state (or star state) gives the flux at x/t = 0 (kernel.cu:1119-1158).
+    const bool takeL = gt_zero(SL) || !(SM < 0.0);
+    const double r = takeL ? rL : rR;
+    const double p = takeL ? pL : pR;
+    const double un = takeL ? unL : unR;
+    const double ut = takeL ? utL : utR;
+    const double S = takeL ? SL : SR;
+    const double su = takeL ? suL : suR;
+    const double mm = takeL ? mL : mR;
+    const bool star = takeL ? !gt_zero(SL) : !(SR < 0.0);
+
+    FluxE F;
+    F.m = r * un;
+    F.mn = fma(F.m, un, p);
+    F.mt = F.m * ut;
+    const double E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
+    F.e = (E + p) * un;
+    if (star) {
+        const double inv = rcp_fast(S - SM);
+        const double rz = r * (su * inv);
+        const double pst = fma(mm, SM - un, p);
+        const double ez = (fma(E, su, pst * SM) - p * un) * inv;
+        const double drz = rz - r;
+        F.m = fma(S, drz, F.m);
+        F.mn = fma(S, fma(rz, SM, -r * un), F.mn);
+        F.mt = fma(S, ut * drz, F.mt);
+        F.e = fma(S, ez - E, F.e);
+    }
+    return F;
+}
+
+template <int ORDER>
+struct Smem {
+    static constexpr int H = ORDER == 2 ? 2 : 1;
+    static constexpr int SX = TX + 2 * H;
+    static constexpr int SY = TY + 2 * H;
+    static constexpr int kPrim = NF * SY * SX;
+    static constexpr int kSlx = ORDER == 2 ? NF * TY * (TX + 2) : 0;
+    static constexpr int kSly = ORDER == 2 ? NF * (TY + 2) * TX : 0;
+    static constexpr int kFx = NF * TY * (TX + 1);
+    static constexpr int kFy = NF * (TY + 1) * TX;
+    static constexpr size_t bytes = sizeof(double) * (kPrim + kSlx + kSly + kFx + kFy);
+};
+
+template <int ORDER>
+__global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Planes out,
+                                                        const double* __restrict__ T_do_ptr,
+                                                        unsigned long long* T_bits, Scalars* rot,
+                                                        Scalars* ctr, int dt_only) {
+    using S = Smem<ORDER>;
+    constexpr int H = S::H, SX = S::SX, SY = S::SY;
+    extern __shared__ double smem[];
+    double* prim = smem;                 // [NF][SY][SX]
+    double* slx = prim + S::kPrim;       // [NF][TY][TX+2]   cells x in [-1, TX]
+    double* sly = slx + S::kSlx;         // [NF][TY+2][TX]   cells y in [-1, TY]
+    double* fx = sly + S::kSly;          // [NF][TY][TX+1]   face between x-1 and x
+    double* fy = fx + S::kFx;            // [NF][TY+1][TX]   face between y-1 and y
+
+    const int tid = threadIdx.x;
+    const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
+    const int N = P.N, M = P.M;
+
+    // ---- L: tile + cross halo ------------------------------------------------------------
+    for (int i = tid; i < SY * SX; i += NT) {
+        const int ly = i / SX, lx = i - ly * SX;
+        const bool xh = lx < H || lx >= TX + H, yh = ly < H || ly >= TY + H;
+        if (xh && yh) continue;  // corners are never read
+        const int gx = tx0 + lx - H, gy = ty0 + ly - H;
+        double v[NF];
+        if (gx >= -2 && gx < N + 2 && gy >= -2 && gy < M + 2 &&
+            !((gx < 0 || gx >= N) && (gy < 0 || gy >= M))) {
+            fetch_cell<NF>(P, in, gx, gy, v);
+        } else {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) v[f] = 1.0;  // outside the grid, never used
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f) prim[(f * SY + ly) * SX + lx] = v[f];
+    }
+    __syncthreads();
+
+    // ---- S: slopes --------------------------------------------------------------------------
+    if (ORDER == 2) {
+        for (int i = tid; i < TY * (TX + 2); i += NT) {
+            const int ly = i / (TX + 2), c = i - ly * (TX + 2);  // cell x = c - 1
+            const double* row = prim + (ly + H) * SX + (c - 1 + H);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double* q = row + f * SY * SX;
+                slx[(f * TY + ly) * (TX + 2) + c] = minmod(q[0] - q[-1], q[1] - q[0]);
+            }
+        }
+        for (int i = tid; i < (TY + 2) * TX; i += NT) {
+            const int r = i / TX, lx = i - r * TX;  // cell y = r - 1
+            const double* col = prim + (r - 1 + H) * SX + (lx + H);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const double* q = col + f * SY * SX;
+                sly[(f * (TY + 2) + r) * TX + lx] = minmod(q[0] - q[-SX], q[SX] - q[0]);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- F: faces ---------------------------------------------------------------------------
+    double umax_x = 0.0, umax_y = 0.0;
+    constexpr int NFX = (TX + 1) * TY, NFY = TX * (TY + 1);
+    for (int i = tid; i < NFX + NFY; i += NT) {
+        const bool isx = i < NFX;
+        int lx, ly;
+        if (isx) {
+            ly = i / (TX + 1);
+            lx = i - ly * (TX + 1);
+            if (tx0 + lx > N || ty0 + ly >= M) continue;
+        } else {
+            const int j = i - NFX;
+            ly = j / TX;
+            lx = j - ly * TX;
+            if (tx0 + lx >= N || ty0 + ly > M) continue;
+        }
+        // cells on either side: A (low) and B (high)
+        const int ax = isx ? lx - 1 : lx, ay = isx ? ly : ly - 1;
+        if (P.frozen_radius > 0.0 &&
+            !cell_active(P, tx0 + ax, ty0 + ay) &&
+            !cell_active(P, tx0 + (isx ? lx : lx), ty0 + (isx ? ly : ly)))
+            continue;  // no updated cell uses this face
+        const double* pa = prim + (ay + H) * SX + (ax + H);
+        const double* pb = pa + (isx ? 1 : SX);
+        double qa[NF], qb[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const double ca = pa[f * SY * SX], cb = pb[f * SY * SX];
+            if (ORDER == 2) {
+                double da, db;
+                if (isx) {
+                    da = slx[(f * TY + ly) * (TX + 2) + lx];
+                    db = slx[(f * TY + ly) * (TX + 2) + lx + 1];
+                } else {
+                    da = sly[(f * (TY + 2) + ly) * TX + lx];
+                    db = sly[(f * (TY + 2) + ly + 1) * TX + lx];
+                }
+                double a = fma(0.5, da, ca), b = fma(-0.5, db, cb);
+                if (f < 2) {  // rho, p fall back to the cell value (kernel.cu:3436-3470)
+                    a = le_zero(a) ? ca : a;
+                    b = le_zero(b) ? cb : b;
+                }
+                qa[f] = a;
+                qb[f] = b;
+            } else {
+                qa[f] = ca;
+                qb[f] = cb;
+            }
+        }
+        double UU;
+        const FluxE F = hllc_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
+                                   qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU);
+        double* fo;
+        if (isx) {
+            fo = fx + ly * (TX + 1) + lx;
+            fo[0 * TY * (TX + 1)] = F.m;
+            fo[1 * TY * (TX + 1)] = F.e;
+            fo[2 * TY * (TX + 1)] = F.mn;  // x momentum
+            fo[3 * TY * (TX + 1)] = F.mt;  // y momentum
+            umax_x = max_nonneg(umax_x, UU);
+        } else {
+            fo = fy + ly * TX + lx;
+            fo[0 * (TY + 1) * TX] = F.m;
+            fo[1 * (TY + 1) * TX] = F.e;
+            fo[2 * (TY + 1) * TX] = F.mt;  // x momentum
+            fo[3 * (TY + 1) * TX] = F.mn;  // y momentum
+            umax_y = max_nonneg(umax_y, UU);
+        }
+    }
+    __syncthreads();
+
+    // ---- U: update --------------------------------------------------------------------------
+    const double T_do = *T_do_ptr;
+    const double kx = T_do / P.dx, ky = T_do / P.dy;
+    bool any_active = false;
+    unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
+    for (int i = tid; i < TX * TY; i += NT) {
+        const int ly = i / TX, lx = i - ly * TX;
+        const int gx = tx0 + lx, gy = ty0 + ly;
+        if (gx >= N || gy >= M) continue;
+        const double* c = prim + (ly + H) * SX + (lx + H);
+        const double r = c[0], p = c[SY * SX], u = c[2 * SY * SX], v = c[3 * SY * SX];
+        const long long k = (long long)gy * N + gx;
+        if (P.frozen_radius > 0.0) {
+            const double x = P.x0 + gx * P.dx, y = P.y0 + gy * P.dy;
+            if (sqrt(x * x + y * y) < P.frozen_radius) {
+                if (!dt_only) {
+                    out.f[0][k] = r; out.f[1][k] = p; out.f[2][k] = u; out.f[3][k] = v;
+                }
+                continue;
+            }
+        }
+        any_active = true;
+        if (dt_only) continue;
+        const double* fxc = fx + ly * (TX + 1) + lx;
+        const double* fyc = fy + ly * TX + lx;
+        double d[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const double* a = fxc + f * TY * (TX + 1);
+            const double* b = fyc + f * (TY + 1) * TX;
+            d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
+        }
+        double r2 = r - d[0];
+        if (le_zero(r2)) { r2 = 0.0001; ++nfl_r; }
+        const double E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
+        const double inv = rcp_fast(r2);
+        const double u2 = fma(r, u, -d[2]) * inv;
+        const double v2 = fma(r, v, -d[3]) * inv;
+        double p2 = ((E - d[1]) - 0.5 * r2 * fma(u2, u2, v2 * v2)) * P.gm1;
+        if (le_zero(p2)) { p2 = 0.000001; ++nfl_p; }
+        if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2)) ++nbad;
+        out.f[0][k] = r2;
+        out.f[1][k] = p2;
+        out.f[2][k] = u2;
+        out.f[3][k] = v2;
+    }
+    if (ctr != nullptr && (nfl_r | nfl_p | nbad)) {
+        if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
+        if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
+        if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
+    }
+    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot);
+}
+
+template <int ORDER>
+cudaError_t launch_euler_fast_t(const Params& P, const CPlanes& in, const Planes& out,
+                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                Scalars* ctr, int dt_only, cudaStream_t st) {
+    dim3 grid((P.N + TX - 1) / TX, (P.M + TY - 1) / TY);
+    euler_fast_kernel<ORDER><<<grid, NT, Smem<ORDER>::bytes, st>>>(P, in, out, T_do, T_bits, rot,
+                                                                    ctr, dt_only);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t prepare_euler_fast() {
+    cudaError_t e = cudaFuncSetAttribute(euler_fast_kernel<1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Smem<1>::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(euler_fast_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Smem<2>::bytes);
+}
+
+cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& out,
+                              const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                              Scalars* ctr, int dt_only, cudaStream_t st) {
+    if (P.order == 1)
+        return launch_euler_fast_t<1>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+    return launch_euler_fast_t<2>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+}  // namespace gd

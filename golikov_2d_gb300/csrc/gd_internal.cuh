@@ -1,0 +1,270 @@
+// gd_internal.cuh -- device-side types and helpers shared by the step kernels.
+//
+// FP64 on GB300 issues at a small fraction of the FP32 rate, so the step is bound by the
+// FP64 pipe, not by HBM.  Everything that does not need FP64 arithmetic is done on the
+// integer pipe here: sign tests, absolute values, minmod selection and max-reductions
+// work on the IEEE-754 bit patterns.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gd2d.h"
+
+namespace gd {
+
+constexpr int kMaxFields = 7;  // rho, p, vx, vy, Bx, By, Bz
+constexpr double kSpi4 = 3.544907701811032;                 // sqrt(4 pi), Header.h:21
+constexpr double kInvSpi4 = 0.28209479177387814347;         // 1/sqrt(4 pi)
+constexpr double kCpi4 = 12.56637061435917295384;           // 4 pi, Header.h:19
+constexpr double kCpi8 = 25.13274122871834590768;           // 8 pi, Header.h:20
+constexpr double kTReset = 10000000.0;                      // funk_time, kernel.cu:1726
+constexpr double kCellTmin0 = 1000.0;                       // per-cell start, kernel.cu:2216
+
+// Launch-invariant parameters, passed by value.
+struct Params {
+    int N, M;
+    int physics, geometry, order, method;
+    int bc[4];
+    double dx, dy, x0, y0;
+    double gamma, krit;
+    double frozen_radius;
+    // derived
+    double gm1, inv_gm1;
+    double ambient_p;   // 1/gamma
+    double krad_x;      // krit * rad used for faces with an x normal
+    double krad_y;      // krit * rad used for faces with a y normal
+};
+
+// SoA planes: f[k] + m*N + n.
+struct Planes {
+    double* f[kMaxFields];
+};
+struct CPlanes {
+    const double* f[kMaxFields];
+};
+
+// Device-resident time-step scalars of one grid (the reference's T, T_do, TT, i).
+struct Scalars {
+    unsigned long long T_bits;  // running min of the CFL dt, as the bits of a positive double
+    double T_do;                // dt used by the current step
+    double TT;                  // simulated time
+    long long step;             // steps taken
+    unsigned int done;          // blocks finished in the current launch (last-block rotation)
+    unsigned int pad;
+    unsigned long long rho_floor, p_floor, nonfinite;
+};
+
+// ---------------------------------------------------------------------------------------
+// Bit-pattern helpers (integer pipe).
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)bits(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ double dabs(double x) { return from_bits((long long)abs_bits(x)); }
+// x <= 0 (for non-NaN x): sign bit set, or +0.
+__device__ __forceinline__ bool le_zero(double x) { return bits(x) <= 0; }
+// x > 0 (for non-NaN x)
+__device__ __forceinline__ bool gt_zero(double x) { return bits(x) > 0; }
+
+// Largest of two non-negative values by bit pattern.
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+    return abs_bits(a) < abs_bits(b) ? b : a;
+}
+
+// minmod(a, b): 0 unless a and b are non-zero with the same sign, else the one of smaller
+// magnitude.  Equal, bit for bit, to the reference's (sign(a)+sign(b))/2 * min(|a|,|b|)
+// (kernel.cu:51-62) for non-NaN inputs.
+__device__ __forceinline__ double minmod(double a, double b) {
+    const long long ba = bits(a), bb = bits(b);
+    const bool zero = ((ba << 1) == 0) | ((bb << 1) == 0) | ((ba ^ bb) < 0);
+    const double m = (abs_bits(a) <= abs_bits(b)) ? a : b;
+    return zero ? 0.0 : m;
+}
+
+// ---------------------------------------------------------------------------------------
+// FP64 reciprocal and reciprocal square root for the fast path.  Each starts from the
+// FP32 special-function estimate and refines it with Newton-Raphson iterations in FP64
+// (y <- y(2 - xy) and y <- y(3 - xy^2)/2), which doubles the number of correct bits per
+// step: 2^-22 -> 2^-44 -> below 1 ulp of double.  Valid for |x| in FP32's normal range
+// (about 1e-37 .. 1e38); outside it they fall back to the correctly rounded operation.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ bool in_f32_range(double x) {
+    // biased exponent within [1023-120, 1023+120]
+    const unsigned int e = (unsigned int)((abs_bits(x) >> 52));
+    return (e - 903u) <= 240u;
+}
+
+__device__ __forceinline__ double rcp_fast(double x) {
+    if (!in_f32_range(x)) return 1.0 / x;
+    double y = (double)__frcp_rn((float)x);
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    return y;
+}
+
+__device__ __forceinline__ double rsqrt_fast(double x) {
+    if (!in_f32_range(x) || x <= 0.0) return 1.0 / sqrt(x);
+    double y = (double)rsqrtf((float)x);
+    // y <- y + y*(1 - x y^2)/2
+    double h = 0.5 * x;
+    double e = fma(-h * y, y, 0.5);
+    y = fma(y, e, y);
+    e = fma(-h * y, y, 0.5);
+    y = fma(y, e, y);
+    return y;
+}
+
+__device__ __forceinline__ double sqrt_fast(double x) {
+    // sqrt(x) = x * rsqrt(x), exact zero preserved
+    return x == 0.0 ? 0.0 : x * rsqrt_fast(x);
+}
+
+// ---------------------------------------------------------------------------------------
+// Ghost values.  Two ghost layers per side; depth 1 is adjacent to the edge cell.  The
+// reference's per-cell boundary branches (kernel.cu:2226-2405) produce exactly these values
+// for every stencil position: mirror conditions reflect the cell at the same distance from
+// the edge, the outflow and ambient conditions use the same value at both depths.
+// ---------------------------------------------------------------------------------------
+
+// Index of the interior cell that supplies ghost `g` (g < 0 or g >= n) for condition bc.
+__device__ __forceinline__ int ghost_source(int g, int n, int bc) {
+    if (bc == GD_BC_PERIODIC) return g < 0 ? g + n : g - n;
+    const bool low = g < 0;
+    const int depth = low ? -g : g - n + 1;  // 1 or 2
+    if (bc == GD_BC_MIRROR_X || bc == GD_BC_AXIS) return low ? depth - 1 : n - depth;
+    return low ? 0 : n - 1;
+}
+
+// Apply the value transformation of condition bc to a fetched state v[0..nf).
+// Field order: rho, p, vx, vy, bx, by, bz.
+template <int NF>
+__device__ __forceinline__ void ghost_transform(double* v, int bc, double ambient_p) {
+    switch (bc) {
+        case GD_BC_MIRROR_X:
+            v[2] = -v[2];
+            if (NF > 4) { v[4] = -v[4]; v[5] = -v[5]; }
+            break;
+        case GD_BC_AXIS:
+            v[3] = -v[3];
+            if (NF > 4) v[6] = -v[6];
+            break;
+        case GD_BC_AMBIENT:
+            v[0] = 1.0; v[1] = ambient_p; v[2] = 0.0; v[3] = 0.0;
+            if (NF > 4) { v[4] = 0.0; v[5] = 0.0; v[6] = 0.0; }
+            break;
+        case GD_BC_AMBIENT_KEEPB:
+            v[0] = 1.0; v[1] = ambient_p; v[2] = 0.0; v[3] = 0.0;
+            break;
+        case GD_BC_OUTFLOW:
+            if (v[2] < 0) v[2] = 0.01;
+            break;
+        default:
+            break;
+    }
+}
+
+// State of cell (gx, gy); at most one coordinate may lie outside the grid, by 1 or 2.
+template <int NF>
+__device__ __forceinline__ void fetch_cell(const Params& P, const CPlanes& in, int gx, int gy,
+                                           double* v) {
+    int sx = gx, sy = gy, bc = -1;
+    if (gx < 0 || gx >= P.N) {
+        bc = gx < 0 ? P.bc[0] : P.bc[1];
+        sx = ghost_source(gx, P.N, bc);
+    } else if (gy < 0 || gy >= P.M) {
+        bc = gy < 0 ? P.bc[2] : P.bc[3];
+        sy = ghost_source(gy, P.M, bc);
+    }
+    const long long k = (long long)sy * P.N + sx;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) v[f] = in.f[f][k];
+    if (bc >= 0) ghost_transform<NF>(v, bc, P.ambient_p);
+}
+
+// Inside the grid and not frozen (kernel.cu:2205, 2218: dist = sqrt(x*x + y*y) < ddist).
+__device__ __forceinline__ bool cell_active(const Params& P, int gx, int gy) {
+    if (gx < 0 || gx >= P.N || gy < 0 || gy >= P.M) return false;
+    if (P.frozen_radius <= 0.0) return true;
+    const double x = P.x0 + gx * P.dx, y = P.y0 + gy * P.dy;
+    return !(sqrt(x * x + y * y) < P.frozen_radius);
+}
+
+// ---------------------------------------------------------------------------------------
+// Block-level dt reduction and the fused funk_time rotation (kernel.cu:1722-1733).
+// ---------------------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Reduces the per-thread maximum wave speeds of x and y faces over the block, turns them
+// into the block's dt (min over faces of krit*rad/UU, capped at 1000) and min-combines it
+// into *T_bits.  `any_active` says whether the block contains a non-frozen cell.  Then,
+// if `sc` is given, the last block to finish performs the funk_time rotation on it.
+// Must be called by every thread of the block.
+template <int NTHREADS>
+__device__ void block_dt_and_rotate(const Params& P, double umax_x, double umax_y,
+                                    bool any_active, unsigned long long* T_bits,
+                                    Scalars* sc) {
+    __shared__ unsigned long long red[2][NTHREADS / 32];
+    __shared__ int act[NTHREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long ax = warp_max_u64(abs_bits(umax_x));
+    unsigned long long ay = warp_max_u64(abs_bits(umax_y));
+    int a = __any_sync(0xffffffffu, any_active);
+    if (lane == 0) {
+        red[0][warp] = ax;
+        red[1][warp] = ay;
+        act[warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long mx = 0, my = 0;
+        int any = 0;
+        for (int w = 0; w < NTHREADS / 32; ++w) {
+            mx = red[0][w] > mx ? red[0][w] : mx;
+            my = red[1][w] > my ? red[1][w] : my;
+            any |= act[w];
+        }
+        if (any) {
+            double t = kCellTmin0;
+            const double ux = from_bits((long long)mx), uy = from_bits((long long)my);
+            if (mx != 0) {
+                const double tx = P.krad_x / ux;
+                t = tx < t ? tx : t;
+            }
+            if (my != 0) {
+                const double ty = P.krad_y / uy;
+                t = ty < t ? ty : t;
+            }
+            atomicMin(T_bits, (unsigned long long)bits(t));
+        }
+        if (sc != nullptr) {
+            __threadfence();
+            const unsigned int nblocks = gridDim.x * gridDim.y * gridDim.z;
+            const unsigned int ticket = atomicAdd(&sc->done, 1u);
+            if (ticket == nblocks - 1) {
+                __threadfence();
+                const double T = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
+                sc->T_do = T;
+                sc->TT = sc->TT + T;
+                sc->T_bits = (unsigned long long)bits(kTReset);
+                sc->step = sc->step + 1;
+                sc->done = 0;
+                __threadfence();
+            }
+        }
+    }
+}
+
+}  // namespace gd

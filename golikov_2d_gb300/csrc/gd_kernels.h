@@ -1,0 +1,42 @@
+// gd_kernels.h -- host-side launch functions of the step kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gd_internal.cuh"
+
+namespace gd {
+
+// One-time function attributes (dynamic shared memory) of the fast kernels; called when a
+// context is created, outside any stream capture.
+cudaError_t prepare_euler_fast();
+cudaError_t prepare_mhd_fast();
+
+// Fast face-once step.  `rot` (may be null) receives the fused funk_time rotation by the
+// last block; `ctr` (may be null) receives floor / non-finite counters.  dt_only != 0
+// computes only the dt minimum.
+cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& out,
+                              const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                              Scalars* ctr, int dt_only, cudaStream_t st);
+cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& out,
+                            const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                            Scalars* ctr, int dt_only, cudaStream_t st);
+
+// Parity step: per-cell faces in the reference's arithmetic order (built without FMA
+// contraction); bit-identical to the reference step.
+cudaError_t launch_parity(const Params& P, const CPlanes& in, const Planes& out,
+                          const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                          Scalars* ctr, int dt_only, cudaStream_t st);
+
+// Utilities (gd_util.cu).
+cudaError_t launch_aos_to_soa(const double* s, const double* u, const double* b, Planes out,
+                              long long K, int nf, cudaStream_t st);
+cudaError_t launch_soa_to_aos(CPlanes in, double* s, double* u, double* b, long long K, int nf,
+                              cudaStream_t st);
+cudaError_t launch_funk_time(double* T, double* T_do, double* TT, int* i, cudaStream_t st);
+cudaError_t launch_set_time(Scalars* sc, double T_do, double TT, cudaStream_t st);
+cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
+cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
+cudaError_t probe_fp64_peak(double* flops);
+
+}  // namespace gd

@@ -1,0 +1,156 @@
+// gd_util.cu -- layout conversion, the funk_time rotation, scalar setup and the FP64
+// throughput probe.
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+
+namespace gd {
+namespace {
+
+// Reference AoS (kernel.cu:3814-3825) -> SoA planes.  s, u: double2[K]; b: double3[K].
+__global__ void aos_to_soa_kernel(const double2* __restrict__ s, const double2* __restrict__ u,
+                                  const double* __restrict__ b, Planes out, long long K, int nf) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
+         k += (long long)gridDim.x * blockDim.x) {
+        const double2 sv = s[k], uv = u[k];
+        out.f[0][k] = sv.x;
+        out.f[1][k] = sv.y;
+        out.f[2][k] = uv.x;
+        out.f[3][k] = uv.y;
+        if (nf > 4) {
+            out.f[4][k] = b[3 * k];
+            out.f[5][k] = b[3 * k + 1];
+            out.f[6][k] = b[3 * k + 2];
+        }
+    }
+}
+
+__global__ void soa_to_aos_kernel(CPlanes in, double2* __restrict__ s, double2* __restrict__ u,
+                                  double* __restrict__ b, long long K, int nf) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
+         k += (long long)gridDim.x * blockDim.x) {
+        s[k] = make_double2(in.f[0][k], in.f[1][k]);
+        u[k] = make_double2(in.f[2][k], in.f[3][k]);
+        if (nf > 4) {
+            b[3 * k] = in.f[4][k];
+            b[3 * k + 1] = in.f[5][k];
+            b[3 * k + 2] = in.f[6][k];
+        }
+    }
+}
+
+// kernel.cu:1722-1733 without the progress print.
+__global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i) {
+    *T_do = *T;
+    *TT = *TT + *T_do;
+    *T = kTReset;
+    *i = *i + 1;
+}
+
+__global__ void set_time_kernel(Scalars* sc, double T_do, double TT) {
+    sc->T_do = T_do;
+    sc->TT = TT;
+    sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
+    sc->done = 0;
+}
+
+// End of a dt-only pass: T_do <- T, T <- 1e7 (TT and the step counter unchanged).
+__global__ void dt_commit_kernel(Scalars* sc) {
+    sc->T_do = __longlong_as_double((long long)sc->T_bits);
+    sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
+    sc->done = 0;
+}
+
+__global__ void reset_T_kernel(Scalars* sc) {
+    sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
+    sc->done = 0;
+}
+
+// 8 independent DFMA chains per thread, ITER iterations each.
+template <int ITER>
+__global__ void fp64_fma_kernel(double* sink, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = threadIdx.x * 1e-9 + j;
+#pragma unroll 4
+    for (int it = 0; it < ITER; ++it) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    if (s == 1.2345) sink[threadIdx.x] = s;  // keeps the chains alive
+}
+
+int grid_for(long long K) {
+    long long g = (K + 255) / 256;
+    return (int)(g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
+}
+
+}  // namespace
+
+cudaError_t launch_aos_to_soa(const double* s, const double* u, const double* b, Planes out,
+                              long long K, int nf, cudaStream_t st) {
+    aos_to_soa_kernel<<<grid_for(K), 256, 0, st>>>((const double2*)s, (const double2*)u, b, out,
+                                                    K, nf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(CPlanes in, double* s, double* u, double* b, long long K, int nf,
+                              cudaStream_t st) {
+    soa_to_aos_kernel<<<grid_for(K), 256, 0, st>>>(in, (double2*)s, (double2*)u, b, K, nf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_funk_time(double* T, double* T_do, double* TT, int* i, cudaStream_t st) {
+    funk_time_kernel<<<1, 1, 0, st>>>(T, T_do, TT, i);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_time(Scalars* sc, double T_do, double TT, cudaStream_t st) {
+    set_time_kernel<<<1, 1, 0, st>>>(sc, T_do, TT);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st) {
+    dt_commit_kernel<<<1, 1, 0, st>>>(sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st) {
+    reset_T_kernel<<<1, 1, 0, st>>>(sc);
+    return cudaGetLastError();
+}
+
+cudaError_t probe_fp64_peak(double* flops) {
+    constexpr int ITER = 4096;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    double* sink = nullptr;
+    e = cudaMalloc(&sink, 1024 * sizeof(double));
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 4, threads = 256;
+    fp64_fma_kernel<ITER><<<blocks, threads>>>(sink, 0.999999, 1e-7);  // warm-up
+    cudaEventRecord(a);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) fp64_fma_kernel<ITER><<<blocks, threads>>>(sink, 0.999999, 1e-7);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return e;
+    const double fmas = (double)reps * blocks * threads * 8.0 * ITER;
+    *flops = 2.0 * fmas / (ms * 1e-3);
+    return cudaGetLastError();
+}
+
+}  // namespace gd

@@ -1,0 +1,171 @@
+/*
+ * gd2d.h -- C ABI of the GB300-native finite-volume step (2-D Euler and ideal MHD).
+ *
+ * Drop-in boundary for the reference's explicit step: minmod TVD reconstruction, HLLC
+ * (Euler) / HLLD and HLLC-MHD (ideal MHD) interface fluxes, the conservative update with
+ * positivity floors, and the CFL time-step minimum.  Plain C types only; every pointer
+ * argument named "device" is a CUDA device pointer, `gd_stream` is a cudaStream_t (NULL
+ * selects the legacy default stream).  Every call is asynchronous on its stream unless it
+ * says otherwise, returns a gd_status and never exits the process.
+ *
+ * The reference has no library interface.  Its de-facto API is the kernel launch
+ * protocol of main() in kernel.cu; each entry point below names the part it replaces.
+ */
+#ifndef GD2D_H
+#define GD2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GD_ABI_VERSION 1
+
+typedef void* gd_stream; /* cudaStream_t */
+
+typedef enum {
+    GD_OK = 0,
+    GD_ERR_INVALID_ARG = 1,  /* bad configuration or argument; nothing was launched      */
+    GD_ERR_CUDA = 2,         /* a CUDA call failed; see gd_last_cuda_error()              */
+    GD_ERR_NONPHYSICAL = 3,  /* non-finite state detected (gd_stats.nonfinite > 0)        */
+    GD_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up                        */
+    GD_ERR_UNSUPPORTED = 5   /* combination not implemented                               */
+} gd_status;
+
+/* physics */
+enum { GD_EULER = 0, GD_MHD = 1 };
+/* geometry: Cartesian, or axisymmetric with y the radius (kernel.cu:2615, 2619-2648) */
+enum { GD_CARTESIAN = 0, GD_AXISYM = 1 };
+/* flux method codes are the reference's `method` argument (kernel.cu:1795, Kernel_TVD's
+ * HLLDQ_Korolkov metod): 1 = HLLC (Euler, HLLC_Aleksashov kernel.cu:853),
+ * 2 = HLLC-MHD (Gas_Dinamic.cu:1137), 3 = HLLD (Gas_Dinamic.cu:1303). */
+enum { GD_METHOD_HLLC = 1, GD_METHOD_HLLC_MHD = 2, GD_METHOD_HLLD = 3 };
+/* boundary conditions, one per side (left, right, bottom, top); two ghost layers each */
+enum {
+    GD_BC_PERIODIC = 0,      /* wrap; both sides of an axis must be periodic              */
+    GD_BC_TRANSMISSIVE = 1,  /* ghosts copy the edge cell                                 */
+    GD_BC_MIRROR_X = 2,      /* reflection, vx, Bx, By odd    (kernel.cu:2268-2281)        */
+    GD_BC_AXIS = 3,          /* reflection, vy, Bz odd        (kernel.cu:2291-2302)        */
+    GD_BC_AMBIENT = 4,       /* rho=1, p=1/gamma, v=0, B=0    (kernel.cu:2234-2242)        */
+    GD_BC_OUTFLOW = 5,       /* edge cell, vx<0 -> 0.01       (kernel.cu:2249-2256)        */
+    GD_BC_AMBIENT_KEEPB = 6  /* AMBIENT with B of the edge cell (kernel.cu:1935-1940)      */
+};
+/* execution mode */
+enum {
+    GD_MODE_FAST = 0,   /* face-once tiles, hoisted reciprocals, FMA: within 1e-12 per step */
+    GD_MODE_PARITY = 1  /* per-cell faces in the reference's arithmetic order, no FMA:
+                           bit-identical to the reference's own step                      */
+};
+
+/* Grid, physics and boundaries.  Replaces the compile-time constants of Header.h:3-38
+ * and kernel.cu:11-30. */
+typedef struct gd_config {
+    int N, M;              /* cells along x (fastest in memory) and y; N, M >= 3          */
+    double dx, dy;         /* cell sizes (kernel.cu:19-20)                                 */
+    double x0, y0;         /* centre of cell (0,0): x = x0 + n*dx (kernel.cu:2203-2204)      */
+    double gamma;          /* adiabatic index (Header.h:4-5)                               */
+    double krit;           /* per-face Courant number (Header.h:3)                         */
+    int physics;           /* GD_EULER or GD_MHD                                           */
+    int geometry;          /* GD_CARTESIAN or GD_AXISYM                                    */
+    int order;             /* 1: first order (add2, Ker_Dekard); 2: minmod TVD (Kernel_TVD) */
+    int method;            /* default flux code (GD_METHOD_*)                              */
+    int bc[4];             /* left, right, bottom, top                                     */
+    double frozen_radius;  /* cells with sqrt(x^2+y^2) < r are copied, 0 = none (ddist,
+                              Header.h:36; kernel.cu:2218-2225)                            */
+    int mode;              /* GD_MODE_FAST or GD_MODE_PARITY                               */
+} gd_config;
+
+typedef struct gd_stats {
+    double t;                   /* simulated time TT (kernel.cu:1725)                       */
+    double dt;                  /* dt the next step will use (T_do)                         */
+    double dt_next;             /* running minimum being accumulated (T)                    */
+    long long steps;            /* steps taken (the reference's device counter i)           */
+    long long rho_floor_hits;   /* cells whose density was floored (kernel.cu:1862, 2622)   */
+    long long p_floor_hits;     /* cells whose pressure was floored (kernel.cu:1872, 2657)  */
+    long long nonfinite;        /* cells that produced a non-finite value                   */
+} gd_stats;
+
+typedef struct gd_ctx gd_ctx;
+
+/* ---- lifetime ------------------------------------------------------------------------ */
+
+/* Validates cfg (everything the reference assumed silently: sizes, positive h, BC pairs,
+ * method vs physics) and allocates the resident state on the current device.
+ * Replaces main()'s cudaMalloc block (kernel.cu:3838-3847). */
+gd_status gd_create(const gd_config* cfg, gd_ctx** out);
+gd_status gd_destroy(gd_ctx* ctx);
+gd_status gd_get_config(const gd_ctx* ctx, gd_config* out);
+const char* gd_status_string(gd_status s);
+/* the last cudaError_t seen by any call in this process (0 = none) */
+int gd_last_cuda_error(void);
+int gd_abi_version(void);
+
+/* ---- compat: the reference's launch protocol, reference AoS layout ------------------- */
+
+/* One step over the whole grid, reference layout (kernel.cu:3814-3825):
+ *   s = double2[K] {rho, p}, u = double2[K] {vx, vy}, b = double3[K] {Bx, By, Bz}
+ *   (b = NULL for Euler), K = N*M, index m*N + n.
+ * Reads *T_do (dt of this step), min-combines this step's CFL dt into *T.  Same roles as
+ *   Kernel_TVD<<<K/256,256>>>(s,u,b,s2,u2,b2,T,T_do,i,method)  (kernel.cu:2198, 4113)
+ *   add2<<<...>>>(...)            when cfg.order == 1, physics MHD (kernel.cu:1877, 4042)
+ *   Ker_Dekard<<<...>>>(...)      when cfg.order == 1, physics Euler (kernel.cu:1736)
+ * method <= 0 uses cfg.method.  `i` is the reference's step counter (unused, as there).
+ * All pointers are device pointers; s/s2 etc. must not alias.  Unlike the reference, the
+ * dt minimum is exact and deterministic (no racy read-compare-write, kernel.cu:2607-2611),
+ * and the launch needs no K % 256 == 0. */
+gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                      double* s2, double* u2, double* b2, double* T, const double* T_do,
+                      int i, int method, gd_stream stream);
+
+/* funk_time<<<1,1>>>(T, T_do, TT, i) (kernel.cu:1722-1733): T_do <- T, TT += T_do,
+ * T <- 1e7, ++i.  Device pointers. */
+gd_status gd_funk_time(gd_ctx* ctx, double* T, double* T_do, double* TT, int* i,
+                       gd_stream stream);
+
+/* ---- resident state (SoA planes owned by the context) -------------------------------- */
+
+/* Load / store the state in the reference AoS layout from host (is_host != 0, pageable or
+ * pinned) or device memory.  b is ignored (may be NULL) for Euler.  Replaces main()'s
+ * cudaMemcpy blocks (kernel.cu:4005-4014, 4181-4188). */
+gd_status gd_import(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                    int is_host, gd_stream stream);
+gd_status gd_export(gd_ctx* ctx, double* s, double* u, double* b, int is_host,
+                    gd_stream stream);
+
+/* Set the dt of the next step and the simulated time (main() starts T_do = 1e-8, TT = 0,
+ * kernel.cu:3860-3863). */
+gd_status gd_set_time(gd_ctx* ctx, double T_do, double TT, gd_stream stream);
+
+/* dt-only pass over the current state: T_do <- min over faces of krit*rad/max(|SL|,|SR|)
+ * (capped at 1000 as the reference's per-cell start value), without updating the state. */
+gd_status gd_init_dt(gd_ctx* ctx, gd_stream stream);
+
+/* nsteps iterations of { step(cfg.method); funk_time } with ping-pong buffers, the
+ * reference's production loop (kernel.cu:4102-4174).  The dt reduction and the
+ * funk_time rotation are fused into the step kernel; one launch per step.
+ * use_graph != 0 captures the nsteps launches in a CUDA graph on first use and replays
+ * it (the graph is cached per nsteps). */
+gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream);
+
+/* Synchronises `stream` and reads time, dt and the floor / non-finite counters. */
+gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
+
+/* Device pointer of resident field f (0 rho, 1 p, 2 vx, 3 vy, 4 Bx, 5 By, 6 Bz) of the
+ * current state; plane of N*M doubles, index m*N + n.  Valid until the next advance. */
+gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
+
+/* ---- measurement helpers -------------------------------------------------------------- */
+
+/* Number of kernel launches the library issued on behalf of this context so far. */
+long long gd_launch_count(const gd_ctx* ctx);
+
+/* Measures the device's FP64 FMA throughput (FLOP/s, FMA = 2) with a register-resident
+ * DFMA loop on every SM; blocking, ~50 ms. */
+gd_status gd_probe_fp64_peak(double* flops_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GD2D_H */

@@ -1,0 +1,718 @@
+/*
+ * gd_oracle.c -- CPU restatement of the reference's explicit finite-volume step.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle.  Loaded by tests/, __graft_entry__.smoke() and
+ * bench.py (CPU-baseline leg) as the checker or the timed CPU baseline, never by the product.
+ *
+ * Each routine restates the reference routine named beside it, keeping the reference's
+ * arithmetic order (compile with -ffp-contract=off) so that results are bit-identical; the
+ * structure around the arithmetic is this project's own:
+ *   - the reference's per-cell rotated-frame code is written as a local (normal, tangent)
+ *     frame with explicit basis vectors;
+ *   - the reference's per-cell boundary branches (kernel.cu:2226-2405) are written as two
+ *     ghost layers per side, which yields exactly the same stencil values (derivation in
+ *     stencil_value below);
+ *   - Cartesian geometry is the reference's axisymmetric update with the 1/y source terms
+ *     removed; periodic and transmissive ghosts are added for the benchmark problems.
+ * Terms that the reference evaluates as exact zeros (B = 0 in the Euler solver, v_z = 0)
+ * are dropped; dropping an exact zero from a sum changes at most the sign of a zero result.
+ */
+#include "gd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Header.h:18-21 */
+#define GDO_CPI4 12.56637061435917295384
+#define GDO_CPI8 25.13274122871834590768
+#define GDO_SPI4 3.544907701811032
+
+/* ------------------------------------------------------------------------------------- */
+/* Reconstruction: kernel.cu:51-100                                                      */
+/* ------------------------------------------------------------------------------------- */
+
+static int sign_of(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
+/* std::min / std::max as the reference calls them (first argument wins ties). */
+static double mn(double a, double b) { return (b < a) ? b : a; }
+static double mx(double a, double b) { return (a < b) ? b : a; }
+
+double gdo_minmod(double a, double b) {
+    int s = sign_of(a) + sign_of(b);
+    if (s == 0) return 0.0;
+    return (s / 2.0) * mn(fabs(a), fabs(b));
+}
+
+double gdo_linear(double x1, double t1, double x2, double t2, double x3, double t3, double y) {
+    double d = gdo_minmod((t1 - t2) / (x1 - x2), (t2 - t3) / (x2 - x3));
+    return d * (y - x2) + t2;
+}
+
+void gdo_linear2(double x1, double t1, double x2, double t2, double x3, double t3, double y1,
+                 double y2, double* A, double* B) {
+    double d = gdo_minmod((t1 - t2) / (x1 - x2), (t2 - t3) / (x2 - x3));
+    *A = d * (y1 - x2) + t2;
+    *B = d * (y2 - x2) + t2;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* Euler HLLC: HLLC_Aleksashov, kernel.cu:853-1165, with B = 0 and v_z = 0.               */
+/* ------------------------------------------------------------------------------------- */
+
+double gdo_hllc(const double* L, const double* R, double n1, double n2, double rad,
+                double gamma, double krit, double* out) {
+    const double g1 = gamma - 1.0;
+    /* Basis for B = 0 (the d <= eps branch, kernel.cu:915-945): normal n, first tangent
+     * e_z, second tangent (-n2, n1, 0). */
+    const double mvec0 = -n2, mvec1 = n1;
+    const double r1 = L[0], p1 = L[1], u1 = L[2], v1 = L[3];
+    const double r2 = R[0], p2 = R[1], u2 = R[2], v2 = R[3];
+
+    /* local-frame velocities: normal and second tangent (the first tangent is 0) */
+    const double vn1 = n1 * u1 + n2 * v1, vm1 = mvec0 * u1 + mvec1 * v1;
+    const double vn2 = n1 * u2 + n2 * v2, vm2 = mvec0 * u2 + mvec1 * v2;
+
+    /* fast speeds with zero field: (sqrt(c*c) + sqrt(c*c)) / 2 (kernel.cu:948-964) */
+    const double cL = sqrt(gamma * p1 / r1);
+    const double qL = sqrt(cL * cL);
+    const double cfL = (qL + qL) / 2.0;
+    const double cR = sqrt(gamma * p2 / r2);
+    const double qR = sqrt(cR * cR);
+    const double cfR = (qR + qR) / 2.0;
+
+    /* Davis speeds and contact speed (kernel.cu:981-986) */
+    const double SL = mn(vn1 - cfL, vn2 - cfR);
+    const double SR = mx(vn1 + cfL, vn2 + cfR);
+    const double suR = SR - vn2;
+    const double suL = SL - vn1;
+    const double SM = (suR * r2 * vn2 - p2 + p1 - suL * r1 * vn1) / (suR * r2 - suL * r1);
+
+    const double UU = mx(fabs(SL), fabs(SR));
+    const double t = krit * rad / UU;
+
+    /* total energies with the global-frame kinetic term (kernel.cu:1020-1029) */
+    const double e1 = p1 / g1 + r1 * ((u1 * u1 + v1 * v1) / 2.0);
+    const double e2 = p2 / g1 + r2 * ((u2 * u2 + v2 * v2) / 2.0);
+
+    /* physical fluxes in the local frame: mass, normal mom., tangent-2 mom., energy */
+    const double FL0 = r1 * vn1, FL1 = r1 * vn1 * vn1 + p1, FL3 = r1 * vn1 * vm1,
+                 FL4 = (e1 + p1) * vn1;
+    const double FR0 = r2 * vn2, FR1 = r2 * vn2 * vn2 + p2, FR3 = r2 * vn2 * vm2,
+                 FR4 = (e2 + p2) * vn2;
+
+    /* star states (kernel.cu:1059-1117; the |UZ[5]| < eps branch holds for B = 0) */
+    const double suRm = suR / (SR - SM);
+    const double suLm = suL / (SL - SM);
+    const double rzR = r2 * suRm;
+    const double rzL = r1 * suLm;
+    const double ptzR = p2 + r2 * suR * (SM - vn2);
+    const double ptzL = p1 + r1 * suL * (SM - vn1);
+    const double ptz = (ptzR + ptzL) / 2.0;
+    const double ezR = e2 * suRm + (ptz * SM - p2 * vn2) / (SR - SM);
+    const double ezL = e1 * suLm + (ptz * SM - p1 * vn1) / (SL - SM);
+
+    double f_mass = 0.0, f_en = 0.0, q0 = 0.0, q2 = 0.0;
+    if (SL > 0.0) {
+        f_mass = FL0;
+        f_en = FL4;
+        q0 = FL1;
+        q2 = FL3;
+    } else if (SL <= 0.0 && SM >= 0.0) {
+        f_mass = FL0 + SL * (rzL - r1);
+        f_en = FL4 + SL * (ezL - e1);
+        q0 = FL1 + SL * (SM * rzL - r1 * vn1);
+        q2 = FL3 + SL * (vm1 * rzL - r1 * vm1);
+    } else if (SM <= 0.0 && SR >= 0.0) {
+        f_mass = FR0 + SR * (rzR - r2);
+        f_en = FR4 + SR * (ezR - e2);
+        q0 = FR1 + SR * (SM * rzR - r2 * vn2);
+        q2 = FR3 + SR * (vm2 * rzR - r2 * vm2);
+    } else if (SR < 0.0) {
+        f_mass = FR0;
+        f_en = FR4;
+        q0 = FR1;
+        q2 = FR3;
+    }
+    out[0] = f_mass;
+    out[1] = f_en;
+    /* back to global axes (kernel.cu:1161-1162) */
+    out[2] = n1 * q0 + mvec0 * q2;
+    out[3] = n2 * q0 + mvec1 * q2;
+    return t;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* MHD HLLD / HLLC-MHD: HLLDQ_Korolkov, Gas_Dinamic.cu:964-1510 (v_z = 0 at call sites).  */
+/* ------------------------------------------------------------------------------------- */
+
+typedef struct {
+    double r, p, vn, vt, vm, bn, bt, bm, bb, e, pt;
+    double F[8]; /* mass, mom n, mom t, mom m, energy, (Bn), Bt, Bm */
+    double U[8];
+} mhd_side;
+
+static void mhd_side_fill(mhd_side* S, const double* Q, const double* n, const double* t,
+                          const double* m, double gamma) {
+    const double bx = Q[5] / GDO_SPI4, by = Q[6] / GDO_SPI4, bz = Q[7] / GDO_SPI4;
+    S->r = Q[0];
+    S->p = Q[1];
+    S->vn = Q[2] * n[0] + Q[3] * n[1] + Q[4] * n[2];
+    S->vt = Q[2] * t[0] + Q[3] * t[1] + Q[4] * t[2];
+    S->vm = Q[2] * m[0] + Q[3] * m[1] + Q[4] * m[2];
+    S->bn = bx * n[0] + by * n[1] + bz * n[2];
+    S->bt = bx * t[0] + by * t[1] + bz * t[2];
+    S->bm = bx * m[0] + by * m[1] + bz * m[2];
+    S->bb = bx * bx + by * by + bz * bz;
+    const double uu = (Q[2] * Q[2] + Q[3] * Q[3] + Q[4] * Q[4]) / 2.0;
+    S->pt = S->p + S->bb / 2.0;
+    S->e = S->p / (gamma - 1.0) + S->r * uu + S->bb / 2.0;
+    S->F[0] = S->r * S->vn;
+    S->F[1] = S->r * S->vn * S->vn + S->pt - S->bn * S->bn;
+    S->F[2] = S->r * S->vn * S->vt - S->bn * S->bt;
+    S->F[3] = S->r * S->vn * S->vm - S->bn * S->bm;
+    S->F[4] = (S->e + S->pt) * S->vn - S->bn * (S->vn * S->bn + S->vt * S->bt + S->vm * S->bm);
+    S->F[5] = 0.0;
+    S->F[6] = S->vn * S->bt - S->vt * S->bn;
+    S->F[7] = S->vn * S->bm - S->vm * S->bn;
+    S->U[0] = S->r;
+    S->U[1] = S->r * S->vn;
+    S->U[2] = S->r * S->vt;
+    S->U[3] = S->r * S->vm;
+    S->U[4] = S->e;
+    S->U[5] = S->bn;
+    S->U[6] = S->bt;
+    S->U[7] = S->bm;
+}
+
+/* fast magnetosonic speed, Gas_Dinamic.cu:1056-1059 */
+static double fast_speed(double r, double p, double bb, double bn, double gamma) {
+    return sqrt((gamma * p + bb + sqrt((gamma * p + bb) * (gamma * p + bb) -
+                                       4.0 * gamma * p * (bn * bn))) /
+                (2.0 * r));
+}
+
+double gdo_hlld(const double* L, const double* R, double n1, double n2, double n3, double rad,
+                int method, double gamma, double krit, double* P) {
+    /* tangent basis chosen by the sign of the normal (Gas_Dinamic.cu:986-1019) */
+    double n[3] = {n1, n2, n3}, t[3] = {0.0, 0.0, 0.0}, m[3] = {0.0, 0.0, 0.0};
+    if (n1 > 0.1) {
+        t[1] = 1.0; m[2] = 1.0;
+    } else if (n2 > 0.1) {
+        t[2] = 1.0; m[0] = 1.0;
+    } else if (n3 > 0.1) {
+        t[0] = 1.0; m[1] = 1.0;
+    } else if (n1 < -0.1) {
+        t[2] = -1.0; m[1] = -1.0;
+    } else if (n2 < -0.1) {
+        t[0] = -1.0; m[2] = -1.0;
+    } else if (n3 < -0.1) {
+        t[0] = -1.0; m[1] = -1.0;
+    }
+    mhd_side A, B;
+    mhd_side_fill(&A, L, n, t, m, gamma);
+    mhd_side_fill(&B, R, n, t, m, gamma);
+
+    const double cfL = fast_speed(A.r, A.p, A.bb, A.bn, gamma);
+    const double cfR = fast_speed(B.r, B.p, B.bb, B.bn, gamma);
+
+    /* wave speeds (Gas_Dinamic.cu:1062-1075) */
+    const double SL = mn(A.vn, B.vn) - mx(cfL, cfR);
+    const double SR = mx(A.vn, B.vn) + mx(cfL, cfR);
+    const double suR = SR - B.vn;
+    const double suL = SL - A.vn;
+    const double SM = (suR * B.r * B.vn - suL * A.r * A.vn - B.pt + A.pt) / (suR * B.r - suL * A.r);
+    const double PTT = (suR * B.r * A.pt - suL * A.r * B.pt + A.r * B.r * suR * suL * (B.vn - A.vn)) /
+                       (suR * B.r - suL * A.r);
+    const double UU = mx(fabs(SL), fabs(SR));
+    const double time = krit * rad / UU;
+
+    /* HLL average of the field (Gas_Dinamic.cu:1127-1130) */
+    const double bn = (SR * B.U[5] - SL * A.U[5] + A.F[5] - B.F[5]) / (SR - SL);
+    const double bt = (SR * B.U[6] - SL * A.U[6] + A.F[6] - B.F[6]) / (SR - SL);
+    const double bm = (SR * B.U[7] - SL * A.U[7] + A.F[7] - B.F[7]) / (SR - SL);
+    const double bbn = bn * bn;
+    const double ro_LL = A.r * (SL - A.vn) / (SL - SM);
+    const double ro_RR = B.r * (SR - B.vn) / (SR - SM);
+
+    double PO[8];
+    int k;
+    if (method == 2) {
+        /* HLLC-MHD, Gas_Dinamic.cu:1137-1302 */
+        const double sbv1 = A.vn * A.bn + A.vt * A.bt + A.vm * A.bm;
+        const double sbv2 = B.vn * B.bn + B.vt * B.bt + B.vm * B.bm;
+        double UZ[5];
+        for (k = 0; k < 5; ++k)
+            UZ[k] = (SR * B.U[k] - SL * A.U[k] + A.F[k] - B.F[k]) / (SR - SL);
+        const double suRm = suR / (SR - SM);
+        const double suLm = suL / (SL - SM);
+        const double ptzR = B.pt + B.r * suR * (SM - B.vn);
+        const double ptzL = A.pt + A.r * suL * (SM - A.vn);
+        const double ptz = (ptzR + ptzL) / 2.0;
+        const double vS = UZ[2] / UZ[0];
+        const double wS = UZ[3] / UZ[0];
+        const double sbvz = (bn * UZ[1] + bt * UZ[2] + bm * UZ[3]) / UZ[0];
+        const double ee2 = B.e * suRm + (ptz * SM - B.pt * B.vn + bn * (sbv2 - sbvz)) / (SR - SM);
+        const double ee1 = A.e * suLm + (ptz * SM - A.pt * A.vn + bn * (sbv1 - sbvz)) / (SL - SM);
+        const double ULL[8] = {ro_LL, ro_LL * SM, ro_LL * vS, ro_LL * wS, ee1, bn, bt, bm};
+        const double URR[8] = {ro_RR, ro_RR * SM, ro_RR * vS, ro_RR * wS, ee2, bn, bt, bm};
+        if (SL >= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = A.F[k];
+        } else if (SL < 0.0 && SM >= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = A.F[k] + SL * ULL[k] - SL * A.U[k];
+        } else if (SR > 0.0 && SM < 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = B.F[k] + SR * URR[k] - SR * B.U[k];
+        } else if (SR <= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = B.F[k];
+        } else {
+            for (k = 0; k < 8; ++k) PO[k] = NAN;
+        }
+    } else {
+        /* HLLD, Gas_Dinamic.cu:1303-1490 */
+        const double ttL = A.r * suL * (SL - SM) - bbn;
+        const double ttR = B.r * suR * (SR - SM) - bbn;
+        double vLL, wLL, vRR, wRR, btt1, bmm1, btt2, bmm2;
+        if (fabs(ttL) >= 0.00001) {
+            vLL = A.vt - bn * A.bt * (SM - A.vn) / ttL;
+            wLL = A.vm - bn * A.bm * (SM - A.vn) / ttL;
+            btt1 = A.bt * (A.r * suL * suL - bbn) / ttL;
+            bmm1 = A.bm * (A.r * suL * suL - bbn) / ttL;
+        } else {
+            vLL = A.vt; wLL = A.vm; btt1 = 0.0; bmm1 = 0.0;
+        }
+        if (fabs(ttR) >= 0.00001) {
+            vRR = B.vt - bn * B.bt * (SM - B.vn) / ttR;
+            wRR = B.vm - bn * B.bm * (SM - B.vn) / ttR;
+            btt2 = B.bt * (B.r * suR * suR - bbn) / ttR;
+            bmm2 = B.bm * (B.r * suR * suR - bbn) / ttR;
+        } else {
+            vRR = B.vt; wRR = B.vm; btt2 = 0.0; bmm2 = 0.0;
+        }
+        const double eLL = (A.e * suL + PTT * SM - A.pt * A.vn +
+                            bn * ((A.vn * A.bn + A.vt * A.bt + A.vm * A.bm) -
+                                  (SM * bn + vLL * btt1 + wLL * bmm1))) /
+                           (SL - SM);
+        const double eRR = (B.e * suR + PTT * SM - B.pt * B.vn +
+                            bn * ((B.vn * B.bn + B.vt * B.bt + B.vm * B.bm) -
+                                  (SM * bn + vRR * btt2 + wRR * bmm2))) /
+                           (SR - SM);
+        const double sqrtroLL = sqrt(ro_LL);
+        const double sqrtroRR = sqrt(ro_RR);
+        double SLL = SM - fabs(bn) / sqrtroLL;
+        double SRR = SM + fabs(bn) / sqrtroRR;
+        double idbn;
+        if (fabs(bn) > 0.000001) {
+            idbn = 1.0 * sign_of(bn);
+        } else {
+            idbn = 0.0;
+            SLL = SM;
+            SRR = SM;
+        }
+        const double vLLL = (sqrtroLL * vLL + sqrtroRR * vRR + idbn * (btt2 - btt1)) /
+                            (sqrtroLL + sqrtroRR);
+        const double wLLL = (sqrtroLL * wLL + sqrtroRR * wRR + idbn * (bmm2 - bmm1)) /
+                            (sqrtroLL + sqrtroRR);
+        const double bttt = (sqrtroLL * btt2 + sqrtroRR * btt1 +
+                             idbn * sqrtroLL * sqrtroRR * (vRR - vLL)) /
+                            (sqrtroLL + sqrtroRR);
+        const double bmmm = (sqrtroLL * bmm2 + sqrtroRR * bmm1 +
+                             idbn * sqrtroLL * sqrtroRR * (wRR - wLL)) /
+                            (sqrtroLL + sqrtroRR);
+        const double eLLL = eLL - idbn * sqrtroLL *
+                                      ((SM * bn + vLL * btt1 + wLL * bmm1) -
+                                       (SM * bn + vLLL * bttt + wLLL * bmmm));
+        const double eRRR = eRR + idbn * sqrtroRR *
+                                      ((SM * bn + vRR * btt2 + wRR * bmm2) -
+                                       (SM * bn + vLLL * bttt + wLLL * bmmm));
+        const double ULL[8] = {ro_LL, ro_LL * SM, ro_LL * vLL, ro_LL * wLL, eLL, bn, btt1, bmm1};
+        const double URR[8] = {ro_RR, ro_RR * SM, ro_RR * vRR, ro_RR * wRR, eRR, bn, btt2, bmm2};
+        const double ULLL[8] = {ro_LL, ro_LL * SM, ro_LL * vLLL, ro_LL * wLLL, eLLL, bn, bttt, bmmm};
+        const double URRR[8] = {ro_RR, ro_RR * SM, ro_RR * vLLL, ro_RR * wLLL, eRRR, bn, bttt, bmmm};
+        if (SL >= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = A.F[k];
+        } else if (SL < 0.0 && SLL >= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = A.F[k] + SL * ULL[k] - SL * A.U[k];
+        } else if (SLL <= 0.0 && SM >= 0.0) {
+            for (k = 0; k < 8; ++k)
+                PO[k] = A.F[k] + SLL * ULLL[k] - (SLL - SL) * ULL[k] - SL * A.U[k];
+        } else if (SM < 0.0 && SRR > 0.0) {
+            for (k = 0; k < 8; ++k)
+                PO[k] = B.F[k] + SRR * URRR[k] - (SRR - SR) * URR[k] - SR * B.U[k];
+        } else if (SR > 0.0 && SRR <= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = B.F[k] + SR * URR[k] - SR * B.U[k];
+        } else if (SR <= 0.0) {
+            for (k = 0; k < 8; ++k) PO[k] = B.F[k];
+        } else {
+            for (k = 0; k < 8; ++k) PO[k] = NAN;
+        }
+    }
+
+    /* normal-field flux replaced by the diffusive term (Gas_Dinamic.cu:1488-1490) */
+    const double SN = mx(fabs(SL), fabs(SR));
+    PO[5] = -SN * (B.bn - A.bn);
+
+    /* back to global axes, field flux to Gaussian units, energy moved last (:1492-1506) */
+    P[0] = PO[0];
+    P[1] = n[0] * PO[1] + t[0] * PO[2] + m[0] * PO[3];
+    P[2] = n[1] * PO[1] + t[1] * PO[2] + m[1] * PO[3];
+    P[3] = n[2] * PO[1] + t[2] * PO[2] + m[2] * PO[3];
+    P[4] = GDO_SPI4 * (n[0] * PO[5] + t[0] * PO[6] + m[0] * PO[7]);
+    P[5] = GDO_SPI4 * (n[1] * PO[5] + t[1] * PO[6] + m[1] * PO[7]);
+    P[6] = GDO_SPI4 * (n[2] * PO[5] + t[2] * PO[6] + m[2] * PO[7]);
+    P[7] = PO[4];
+    return time;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* Step: the per-cell structure of Kernel_TVD (kernel.cu:2198-2661), add2 (:1877-2196),   */
+/* Ker_Dekard (:1736-1875) and the reconstruction of Kernel_TVD_old (:3436-3544).         */
+/* ------------------------------------------------------------------------------------- */
+
+typedef struct {
+    double r, p, u, v, bx, by, bz;
+} prim;
+
+static prim load_cell(const gdo_config* c, const double* s, const double* u, const double* b,
+                      int n, int m) {
+    const long k = (long)m * c->N + n;
+    prim q;
+    q.r = s[2 * k];
+    q.p = s[2 * k + 1];
+    q.u = u[2 * k];
+    q.v = u[2 * k + 1];
+    if (b) {
+        q.bx = b[3 * k];
+        q.by = b[3 * k + 1];
+        q.bz = b[3 * k + 2];
+    } else {
+        q.bx = q.by = q.bz = 0.0;
+    }
+    return q;
+}
+
+/* Ghost value `depth` (1 or 2) cells beyond the edge cell `edge` of a row/column.
+ * `inner` is the interior cell at the same distance from the edge (depth 1 -> edge cell,
+ * depth 2 -> its neighbour); the reference's mirror conditions reflect that cell:
+ *   left  n==0: s_4 = mirror(s_1), n==0: s41 = mirror(s_2), n==1: s41 = mirror(s_4)
+ *   bottom m==0: s_3 = axis(s_1), m==0: s31 = axis(s_5), m==1: s31 = axis(s_3)
+ * while the outflow and ambient conditions give the same value at both depths:
+ *   right n==N-1: s_2 = clamp(s_1); n>=N-2: s21 = clamp(s_2)
+ *   top m==M-1: s_5 = ambient; m>=M-2: s51 = ambient. */
+static prim ghost(const gdo_config* c, int bc, prim edge, prim inner) {
+    prim g;
+    switch (bc) {
+        case GDO_BC_MIRROR_X:
+            g = inner;
+            g.u = -inner.u;
+            g.bx = -inner.bx;
+            g.by = -inner.by;
+            return g;
+        case GDO_BC_AXIS:
+            g = inner;
+            g.v = -inner.v;
+            g.bz = -inner.bz;
+            return g;
+        case GDO_BC_AMBIENT:
+        case GDO_BC_AMBIENT_KEEPB:
+            g.r = 1.0;
+            g.p = 1.0 / c->gamma;
+            g.u = 0.0;
+            g.v = 0.0;
+            if (bc == GDO_BC_AMBIENT_KEEPB) {
+                g.bx = edge.bx; g.by = edge.by; g.bz = edge.bz;
+            } else {
+                g.bx = 0.0; g.by = 0.0; g.bz = 0.0;
+            }
+            return g;
+        case GDO_BC_OUTFLOW:
+            g = edge;
+            if (g.u < 0) g.u = 0.01;
+            return g;
+        case GDO_BC_TRANSMISSIVE:
+        default:
+            return edge;
+    }
+}
+
+/* Value of the cell at (n, m) where exactly one of n, m may lie outside the grid by <= 2. */
+static prim stencil_value(const gdo_config* c, const double* s, const double* u, const double* b,
+                          int n, int m) {
+    const int N = c->N, M = c->M;
+    if (n < 0 || n >= N) {
+        const int left = n < 0;
+        const int bc = left ? c->bc[0] : c->bc[1];
+        const int depth = left ? -n : n - N + 1;
+        if (bc == GDO_BC_PERIODIC) return load_cell(c, s, u, b, (n + N) % N, m);
+        const int e = left ? 0 : N - 1;
+        const int in = left ? depth - 1 : N - depth;
+        return ghost(c, bc, load_cell(c, s, u, b, e, m), load_cell(c, s, u, b, in, m));
+    }
+    if (m < 0 || m >= M) {
+        const int bottom = m < 0;
+        const int bc = bottom ? c->bc[2] : c->bc[3];
+        const int depth = bottom ? -m : m - M + 1;
+        if (bc == GDO_BC_PERIODIC) return load_cell(c, s, u, b, n, (m + M) % M);
+        const int e = bottom ? 0 : M - 1;
+        const int in = bottom ? depth - 1 : M - depth;
+        return ghost(c, bc, load_cell(c, s, u, b, n, e), load_cell(c, s, u, b, n, in));
+    }
+    return load_cell(c, s, u, b, n, m);
+}
+
+/* field accessors so the 7 reconstructions can loop */
+static double* fld(prim* q, int f) {
+    switch (f) {
+        case 0: return &q->r;
+        case 1: return &q->p;
+        case 2: return &q->u;
+        case 3: return &q->v;
+        case 4: return &q->bx;
+        case 5: return &q->by;
+        default: return &q->bz;
+    }
+}
+
+typedef struct {
+    prim c1, own[4], nbr[4]; /* own face states 12,13,14,15 and neighbour face states 21,31,41,51 */
+    prim s2, s3, s4, s5;     /* first neighbours E, S, W, N (cell values, used by Pdiv) */
+} cell_faces;
+
+/* Face states of one cell, kernel.cu:2226-2548 (order 2) or the raw neighbours (order 1). */
+static void build_faces(const gdo_config* c, const double* s, const double* u, const double* b,
+                        int n, int m, double x, double y, cell_faces* F) {
+    const double dx = c->dx, dy = c->dy;
+    const int nf = c->physics == GDO_MHD ? 7 : 4;
+    prim q1 = load_cell(c, s, u, b, n, m);
+    prim q2 = stencil_value(c, s, u, b, n + 1, m);
+    prim q4 = stencil_value(c, s, u, b, n - 1, m);
+    prim q3 = stencil_value(c, s, u, b, n, m - 1);
+    prim q5 = stencil_value(c, s, u, b, n, m + 1);
+    F->c1 = q1;
+    F->s2 = q2; F->s3 = q3; F->s4 = q4; F->s5 = q5;
+    if (c->order == 1) {
+        F->own[0] = F->own[1] = F->own[2] = F->own[3] = q1;
+        F->nbr[0] = q2; F->nbr[1] = q3; F->nbr[2] = q4; F->nbr[3] = q5;
+        return;
+    }
+    prim q21 = stencil_value(c, s, u, b, n + 2, m);
+    prim q41 = stencil_value(c, s, u, b, n - 2, m);
+    prim q31 = stencil_value(c, s, u, b, n, m - 2);
+    prim q51 = stencil_value(c, s, u, b, n, m + 2);
+    prim f12 = q1, f13 = q1, f14 = q1, f15 = q1, f21 = q2, f31 = q3, f41 = q4, f51 = q5;
+    for (int f = 0; f < nf; ++f) {
+        const int positive = (f == 0 || f == 1); /* rho and p fall back when <= 0 */
+        const double v1 = *fld(&q1, f), v2 = *fld(&q2, f), v3 = *fld(&q3, f), v4 = *fld(&q4, f),
+                     v5 = *fld(&q5, f);
+        double A, B;
+        /* own x faces: linear2 over (x-dx, x, x+dx) evaluated at x -/+ dx/2 (:2407-2458) */
+        gdo_linear2(x - dx, v4, x, v1, x + dx, v2, x - dx / 2.0, x + dx / 2.0, &A, &B);
+        *fld(&f12, f) = (positive && B <= 0) ? v1 : B;
+        *fld(&f14, f) = (positive && A <= 0) ? v1 : A;
+        /* own y faces (:2461-2508) */
+        gdo_linear2(y - dy, v3, y, v1, y + dy, v5, y - dy / 2.0, y + dy / 2.0, &A, &B);
+        *fld(&f15, f) = (positive && B <= 0) ? v1 : B;
+        *fld(&f13, f) = (positive && A <= 0) ? v1 : A;
+        /* neighbours' facing states with their own stencils (:2510-2548) */
+        double w;
+        w = gdo_linear(x, v1, x + dx, v2, x + 2.0 * dx, *fld(&q21, f), x + dx / 2.0);
+        *fld(&f21, f) = (positive && w <= 0) ? v2 : w;
+        w = gdo_linear(x, v1, x - dx, v4, x - 2.0 * dx, *fld(&q41, f), x - dx / 2.0);
+        *fld(&f41, f) = (positive && w <= 0) ? v4 : w;
+        w = gdo_linear(y, v1, y - dy, v3, y - 2.0 * dy, *fld(&q31, f), y - dy / 2.0);
+        *fld(&f31, f) = (positive && w <= 0) ? v3 : w;
+        w = gdo_linear(y, v1, y + dy, v5, y + 2.0 * dy, *fld(&q51, f), y + dy / 2.0);
+        *fld(&f51, f) = (positive && w <= 0) ? v5 : w;
+    }
+    F->own[0] = f12; F->own[1] = f13; F->own[2] = f14; F->own[3] = f15;
+    F->nbr[0] = f21; F->nbr[1] = f31; F->nbr[2] = f41; F->nbr[3] = f51;
+}
+
+/* outward normals of faces 12 (E), 13 (S), 14 (W), 15 (N) */
+static const double FACE_N1[4] = {1.0, 0.0, -1.0, 0.0};
+static const double FACE_N2[4] = {0.0, -1.0, 0.0, 1.0};
+
+/* Euler cell: fluxes as Kernel_TVD_old :3560-3586, update as Ker_Dekard :1849-1874
+ * (Cartesian) or Kernel_TVD_old :3636-3665 (axisymmetric).  Returns the cell's dt. */
+static double euler_cell(const gdo_config* c, const cell_faces* F, double y, double T_do,
+                         double* out) {
+    const double dx = c->dx, dy = c->dy, gamma = c->gamma;
+    double tmin = 1000;
+    double Ps[4][2], Pu[4][2];
+    for (int f = 0; f < 4; ++f) {
+        const prim* a = &F->own[f];
+        const prim* z = &F->nbr[f];
+        const double L[4] = {a->r, a->p, a->u, a->v};
+        const double R[4] = {z->r, z->p, z->u, z->v};
+        const double rad = (f == 0 || f == 2) ? dy : dx; /* kernel.cu:3562-3586 */
+        double o[4];
+        tmin = mn(tmin, gdo_hllc(L, R, FACE_N1[f], FACE_N2[f], rad, gamma, c->krit, o));
+        Ps[f][0] = o[0]; Ps[f][1] = o[1]; Pu[f][0] = o[2]; Pu[f][1] = o[3];
+    }
+    const double PSx = Ps[0][0] * dy + Ps[1][0] * dx + Ps[2][0] * dy + Ps[3][0] * dx;
+    const double PSy = Ps[0][1] * dy + Ps[1][1] * dx + Ps[2][1] * dy + Ps[3][1] * dx;
+    const double PUx = Pu[0][0] * dy + Pu[1][0] * dx + Pu[2][0] * dy + Pu[3][0] * dx;
+    const double PUy = Pu[0][1] * dy + Pu[1][1] * dx + Pu[2][1] * dy + Pu[3][1] * dx;
+    const double dV = dx * dy;
+    const prim* q = &F->c1;
+    double r2, ux2, uy2, p2;
+    if (c->geometry == GDO_AXISYM) {
+        r2 = q->r - (T_do / dV) * PSx - T_do * q->r * q->v / y;
+        if (r2 <= 0) r2 = 0.0001;
+        ux2 = (q->r * q->u - (T_do / dV) * PUx - T_do * q->r * q->v * q->u / y) / r2;
+        uy2 = (q->r * q->v - (T_do / dV) * PUy - T_do * q->r * q->v * q->v / y) / r2;
+        p2 = (((q->p / (gamma - 1) + q->r * (q->u * q->u + q->v * q->v) * 0.5) -
+               (T_do / dV) * PSy -
+               T_do * q->v * (gamma * q->p / (gamma - 1) + q->r * (q->u * q->u + q->v * q->v) * 0.5) /
+                   y) -
+              0.5 * r2 * (ux2 * ux2 + uy2 * uy2)) *
+             (gamma - 1);
+    } else {
+        r2 = q->r - (T_do / dV) * PSx;
+        if (r2 <= 0) r2 = 0.0001;
+        ux2 = (q->r * q->u - (T_do / dV) * PUx) / r2;
+        uy2 = (q->r * q->v - (T_do / dV) * PUy) / r2;
+        p2 = (((q->p / (gamma - 1) + q->r * (q->u * q->u + q->v * q->v) * 0.5) - (T_do / dV) * PSy) -
+              0.5 * r2 * (ux2 * ux2 + uy2 * uy2)) *
+             (gamma - 1);
+    }
+    if (p2 <= 0) p2 = 0.000001;
+    out[0] = r2; out[1] = p2; out[2] = ux2; out[3] = uy2;
+    return tmin;
+}
+
+/* MHD cell: Kernel_TVD :2550-2660 (add2 :2064-2192 has the same flux and update). */
+static double mhd_cell(const gdo_config* c, const cell_faces* F, double y, double T_do,
+                       double* out) {
+    const double dx = c->dx, dy = c->dy, gamma = c->gamma;
+    const int axi = c->geometry == GDO_AXISYM;
+    double tmin = 1000;
+    double PSx = 0.0, PSy = 0.0, PUx = 0.0, PUy = 0.0, PBx = 0.0, PBy = 0.0, PBz = 0.0;
+    double Pdiv = 0.0;
+    const prim* q = &F->c1;
+    for (int f = 0; f < 4; ++f) {
+        const prim* a = &F->own[f];
+        const prim* z = &F->nbr[f];
+        const double L[8] = {a->r, a->p, a->u, a->v, 0.0, a->bx, a->by, a->bz};
+        const double R[8] = {z->r, z->p, z->u, z->v, 0.0, z->bx, z->by, z->bz};
+        const int xface = (f == 0 || f == 2);
+        const double rad = xface ? dx : dy;  /* kernel.cu:2559-2604 */
+        const double len = xface ? dy : dx;  /* face length */
+        double P[8];
+        tmin = mn(tmin, gdo_hlld(L, R, FACE_N1[f], FACE_N2[f], 0.0, rad, c->method, gamma, c->krit, P));
+        PSx = PSx + P[0] * len;
+        PSy = PSy + P[7] * len;
+        PUx = PUx + P[1] * len;
+        PUy = PUy + P[2] * len;
+        PBx = PBx + P[4] * len;
+        PBy = PBy + P[5] * len;
+        PBz = PBz + P[6] * len;
+        /* Powell divergence from cell-centred B (kernel.cu:2568, 2580, 2592, 2604) */
+        switch (f) {
+            case 0: Pdiv = Pdiv + dy * (q->bx + F->s2.bx) / 2.0; break;
+            case 1: Pdiv = Pdiv - dx * (q->by + F->s3.by) / 2.0; break;
+            case 2: Pdiv = Pdiv - dy * (q->bx + F->s4.bx) / 2.0; break;
+            default: Pdiv = Pdiv + dx * (q->by + F->s5.by) / 2.0; break;
+        }
+    }
+    const double dV = dx * dy;
+    if (axi) Pdiv = Pdiv + dV * q->by / y; /* kernel.cu:2615 */
+
+    /* update, kernel.cu:2619-2660 (Cartesian: the 1/y source terms removed) */
+    const double kvu = q->u * q->u + q->v * q->v + 0.0 * 0.0;
+    const double kvb = q->bx * q->bx + q->by * q->by + q->bz * q->bz;
+    const double U8 = q->p / (gamma - 1.0) + 0.5 * q->r * kvu + kvb / 25.13274122871834590768;
+    const double skk = q->u * q->bx + q->v * q->by + 0.0 * q->bz;
+    double r2 = q->r - T_do * PSx / dV;
+    if (axi) r2 = r2 - T_do * q->r * q->v / y;
+    if (r2 <= 0) r2 = q->r;
+    double ux2 = q->r * q->u - T_do * (PUx + (q->bx / GDO_CPI4) * Pdiv) / dV;
+    double uy2 = q->r * q->v - T_do * (PUy + (q->by / GDO_CPI4) * Pdiv) / dV;
+    double bx2 = q->bx - T_do * (PBx + q->u * Pdiv) / dV;
+    if (axi) {
+        ux2 = ux2 - T_do * (q->r * q->u * q->v - q->bx * q->by / GDO_CPI4) / y;
+        uy2 = uy2 - T_do * (q->r * q->v * q->v + (q->bz * q->bz - q->by * q->by) / GDO_CPI4) / y;
+        bx2 = bx2 - T_do * (q->v * q->bx - q->by * q->u) / y;
+    }
+    ux2 = ux2 / r2;
+    uy2 = uy2 / r2;
+    const double by2 = q->by - T_do * (PBy + q->v * Pdiv) / dV;
+    const double bz2 = q->bz - T_do * (PBz) / dV;
+    double e = U8 - T_do * (PSy + (skk / GDO_CPI4) * Pdiv) / dV;
+    if (axi) e = e - T_do * (((U8 + q->p + kvb / GDO_CPI8) * q->v - q->by * skk / GDO_CPI4) / y);
+    double p2 = (e - 0.5 * r2 * (ux2 * ux2 + uy2 * uy2 + 0.0 * 0.0) -
+                 (bx2 * bx2 + by2 * by2 + bz2 * bz2) / GDO_CPI8) *
+                (gamma - 1.0);
+    if (p2 <= 0) p2 = 0.000001;
+    out[0] = r2; out[1] = p2; out[2] = ux2; out[3] = uy2;
+    out[4] = bx2; out[5] = by2; out[6] = bz2;
+    return tmin;
+}
+
+double gdo_step(const gdo_config* c, const double* s, const double* u, const double* b,
+                double* s2, double* u2, double* b2, double T_do, double T_in, int dt_only) {
+    const int N = c->N, M = c->M;
+    double T = T_in;
+#pragma omp parallel
+    {
+        double tloc = T_in;
+#pragma omp for schedule(static)
+        for (int m = 0; m < M; ++m) {
+            for (int n = 0; n < N; ++n) {
+                const long k = (long)m * N + n;
+                const double y = c->y0 + m * c->dy;
+                const double x = c->x0 + n * c->dx;
+                if (c->frozen_radius > 0.0) {
+                    const double dist = sqrt(x * x + y * y);
+                    if (dist < c->frozen_radius) {
+                        if (!dt_only) {
+                            s2[2 * k] = s[2 * k]; s2[2 * k + 1] = s[2 * k + 1];
+                            u2[2 * k] = u[2 * k]; u2[2 * k + 1] = u[2 * k + 1];
+                            if (b && b2) {
+                                b2[3 * k] = b[3 * k]; b2[3 * k + 1] = b[3 * k + 1];
+                                b2[3 * k + 2] = b[3 * k + 2];
+                            }
+                        }
+                        continue;
+                    }
+                }
+                cell_faces F;
+                build_faces(c, s, u, b, n, m, x, y, &F);
+                double out[7] = {0, 0, 0, 0, 0, 0, 0};
+                double tcell = (c->physics == GDO_MHD) ? mhd_cell(c, &F, y, T_do, out)
+                                                       : euler_cell(c, &F, y, T_do, out);
+                if (tloc > tcell) tloc = tcell;
+                if (!dt_only) {
+                    s2[2 * k] = out[0]; s2[2 * k + 1] = out[1];
+                    u2[2 * k] = out[2]; u2[2 * k + 1] = out[3];
+                    if (c->physics == GDO_MHD) {
+                        b2[3 * k] = out[4]; b2[3 * k + 1] = out[5]; b2[3 * k + 2] = out[6];
+                    }
+                }
+            }
+        }
+#pragma omp critical
+        {
+            if (tloc < T) T = tloc;
+        }
+    }
+    return T;
+}
+
+int gdo_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+void gdo_funk_time(double* T, double* T_do, double* TT, int* i) {
+    *T_do = *T;
+    *TT = *TT + *T_do;
+    *T = 10000000;
+    *i = *i + 1;
+}

@@ -1,0 +1,93 @@
+"""GPU fast mode (face-once tiles) against the oracle.
+
+Bounds, stated here and asserted:
+  * one step from the same state: relative L1 difference of every conserved field
+    (rho, rho v, E[, B]) <= 1e-12 (PER_STEP_TOL);
+  * N steps of the full lagged-dt protocol: <= NSTEP_TOL (rounding differences between
+    face-once / reference-order arithmetic grow through the nonlinear dynamics);
+  * dt: relative difference <= 1e-12.
+Plus properties that hold for the fast path on its own: y-invariance of Sod, exact
+conservation of the face-once update on periodic grids (to rounding), graph == plain."""
+import numpy as np
+import pytest
+
+import golikov_2d_gb300 as g
+from golikov_2d_gb300 import problems
+from gpu_util import gpu_run, gpu_step_ref, grid_of, max_rel_l1, oracle_run, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+PER_STEP_TOL = 1e-12
+NSTEP_TOL = 1e-9
+
+EULER_CASES = {
+    "sod256": lambda: problems.sod(256, 256),
+    "kh128": lambda: problems.kelvin_helmholtz(128, 128),
+    "quad97": lambda: problems.four_quadrant(97, np.random.default_rng(7)),
+    "sod_o1": lambda: (lambda c: (setattr(c[0], "order", 1), c)[1])(problems.sod(80, 40)),
+}
+
+
+def evolve(o, cfg, s, u, b, n):
+    so, uo, bo, T_do, _ = oracle_run(o, cfg, s, u, b, n)
+    return so, uo, bo, T_do
+
+
+@pytest.mark.parametrize("case", sorted(EULER_CASES))
+def test_fast_one_step_within_tolerance(cuda, oracle_lib, case):
+    cfg, s, u, b = EULER_CASES[case]()
+    # develop some structure first, then compare one step from the same state and dt
+    s, u, b, T_do = evolve(oracle_lib, cfg, s, u, b, 20)
+    so, uo, bo, To = oracle_lib.step(grid_of(cfg), s, u, b, T_do)
+    sg, ug, bg, Tg = gpu_step_ref(cfg, s, u, b, T_do)
+    err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
+    assert err <= PER_STEP_TOL, err
+    assert abs(Tg - To) <= 1e-12 * To
+
+
+def test_fast_sod_200_steps(cuda, oracle_lib):
+    """BASELINE config 1: Sod 256^2, HLLC + minmod, CFL 0.4, 200 steps, transmissive."""
+    cfg, s, u, b = problems.sod(256, 256)
+    so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 200)
+    sg, ug, bg, st = gpu_run(cfg, s, u, b, 200)
+    err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
+    assert err <= NSTEP_TOL, err
+    assert abs(st.t - TT) <= 1e-10 * TT
+    # y-invariance: every row identical
+    r = sg[:, 0].reshape(cfg.M, cfg.N)
+    assert np.array_equal(r, np.broadcast_to(r[0], r.shape))
+    assert st.rho_floor_hits == 0 and st.nonfinite == 0
+
+
+def test_fast_periodic_conservation(cuda):
+    cfg, s, u, b = problems.kelvin_helmholtz(128, 128)
+    sg, ug, bg, st = gpu_run(cfg, s, u, b, 50)
+    c0 = [x.sum() for x in __import__("gpu_util").conserved(cfg, s, u, b)]
+    c1 = [x.sum() for x in __import__("gpu_util").conserved(cfg, sg, ug, bg)]
+    assert abs(c1[0] - c0[0]) <= 1e-13 * abs(c0[0])          # mass
+    assert abs(c1[3] - c0[3]) <= 1e-13 * abs(c0[3])          # energy
+    assert abs(c1[1] - c0[1]) <= 1e-13 * np.abs(s[:, 0] * u[:, 0]).sum()  # x momentum
+
+
+def test_graph_equals_plain(cuda):
+    cfg, s, u, b = problems.kelvin_helmholtz(96, 64)
+    a = gpu_run(cfg, s, u, b, 7, use_graph=False)
+    c = gpu_run(cfg, s, u, b, 7, use_graph=True)
+    assert np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
+    assert a[3].t == c[3].t and a[3].dt == c[3].dt
+
+
+def test_non_multiple_tile_sizes(cuda, oracle_lib):
+    """Grids that are not multiples of the 32 x 16 tile, both orders."""
+    for N, M in ((37, 19), (65, 33), (3, 3)):
+        for order in (1, 2):
+            cfg, s, u, b = problems.four_quadrant(max(N, M), np.random.default_rng(N))
+            cfg = g.Config(**{**cfg.__dict__, "N": N, "M": M, "dx": 1.0 / N, "dy": 1.0 / M,
+                              "x0": 0.5 / N, "y0": 0.5 / M, "order": order})
+            rng = np.random.default_rng(N + M)
+            s = np.stack([rng.uniform(0.5, 2, N * M), rng.uniform(0.5, 2, N * M)], 1)
+            u = rng.uniform(-1, 1, (N * M, 2))
+            so, uo, bo, To = oracle_lib.step(grid_of(cfg), s, u, None, 1e-3)
+            sg, ug, bg, Tg = gpu_step_ref(cfg, s, u, None, 1e-3)
+            assert max_rel_l1(cfg, (sg, ug, None), (so, uo, None)) <= PER_STEP_TOL
+            assert abs(Tg - To) <= 1e-12 * To

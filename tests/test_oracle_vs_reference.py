@@ -1,0 +1,62 @@
+"""Fresh randomized comparisons of the oracle against the reference's own compiled code.
+
+Needs oracle/_ref/libgdref.so (built from the reference sources; skipped where they are
+absent).  Complements the fixed golden vectors with new seeds on every grid shape below."""
+import numpy as np
+import pytest
+
+import oracle
+
+
+def rand_state(rng, K, bscale=2.0):
+    s = np.stack([rng.uniform(0.2, 2.0, K), rng.uniform(0.05, 2.0, K)], 1)
+    u = rng.uniform(-1.5, 1.5, (K, 2))
+    b = rng.uniform(-bscale, bscale, (K, 3))
+    return s, u, b
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+@pytest.mark.parametrize("N,M", [(33, 17), (64, 8)])
+@pytest.mark.parametrize("method", [2, 3])
+def test_kernel_tvd_random(oracle_lib, reference, seed, N, M, method):
+    rng = np.random.default_rng(seed)
+    xmax, ymax = 3.0, 1.7
+    reference.set_params(5.0 / 3.0, 0.25, N, M, xmax, ymax)
+    s, u, b = rand_state(rng, N * M)
+    s2r, u2r, b2r, Tr = reference.kernel_tvd(s, u, b, 1.5e-3, 0, method)
+    g = oracle.Grid(N, M, xmax / N, ymax / M, xmax / (2.0 * N), ymax / (2.0 * M), 5.0 / 3.0, 0.25,
+                    physics=oracle.MHD, geometry=oracle.AXISYM, order=2, method=method,
+                    bc=(oracle.BC_MIRROR_X, oracle.BC_OUTFLOW, oracle.BC_AXIS, oracle.BC_AMBIENT),
+                    frozen_radius=0.3)
+    s2, u2, b2, T = oracle_lib.step(g, s, u, b, 1.5e-3)
+    assert T == Tr
+    assert np.array_equal(s2, s2r) and np.array_equal(u2, u2r) and np.array_equal(b2, b2r)
+
+
+@pytest.mark.parametrize("gamma", [1.4, 5.0 / 3.0])
+def test_hllc_random_faces(oracle_lib, reference, gamma):
+    rng = np.random.default_rng(21)
+    reference.set_params(gamma, 0.4, 64, 64, 1.0, 1.0)
+    for _ in range(3000):
+        L = np.array([rng.uniform(0.01, 5), rng.uniform(0.01, 5), rng.uniform(-4, 4), rng.uniform(-4, 4)])
+        R = np.array([rng.uniform(0.01, 5), rng.uniform(0.01, 5), rng.uniform(-4, 4), rng.uniform(-4, 4)])
+        n1, n2 = [(1, 0), (0, -1), (-1, 0), (0, 1)][rng.integers(0, 4)]
+        t1, F1 = oracle_lib.hllc(L, R, n1, n2, 0.003, gamma, 0.4)
+        t2, F2 = reference.hllc(L, R, n1, n2, 0.003)
+        assert t1 == t2 and np.array_equal(F1, F2)
+
+
+def test_hlld_random_faces(oracle_lib, reference):
+    rng = np.random.default_rng(22)
+    reference.set_params(5.0 / 3.0, 0.4, 64, 64, 1.0, 1.0)
+    for it in range(3000):
+        def side():
+            return np.array([rng.uniform(0.01, 5), rng.uniform(0.01, 5), rng.uniform(-4, 4),
+                             rng.uniform(-4, 4), 0.0, rng.uniform(-5, 5), rng.uniform(-5, 5),
+                             rng.uniform(-5, 5)])
+        L, R = side(), side()
+        n1, n2 = [(1, 0), (0, -1), (-1, 0), (0, 1)][rng.integers(0, 4)]
+        meth = 2 + (it & 1)
+        t1, F1 = oracle_lib.hlld(L, R, n1, n2, 0.0, 0.003, meth, 5.0 / 3.0, 0.4)
+        t2, F2 = reference.hlld(L, R, n1, n2, 0.0, 0.003, meth)
+        assert t1 == t2 and np.array_equal(F1, F2, equal_nan=True)
