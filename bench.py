@@ -45,6 +45,9 @@ WORKLOADS = {
     "kh4096": "Kelvin-Helmholtz 4096x4096 periodic, Euler, HLLC + minmod, CFL 0.4, FP64",
     "ot1024": "Orszag-Tang 1024x1024 periodic, ideal MHD, HLLD + minmod, CFL 0.4, FP64",
     "sod256": "Sod 256x256 transmissive, Euler, HLLC + minmod, CFL 0.4, FP64",
+    # reduced cases for ncu captures (state still larger than L2)
+    "kh2048": "Kelvin-Helmholtz 2048x2048 periodic, Euler, HLLC + minmod, CFL 0.4, FP64",
+    "ot2048": "Orszag-Tang 2048x2048 periodic, ideal MHD, HLLD + minmod, CFL 0.4, FP64",
 }
 L2_BYTES = 129 * 2 ** 20
 
@@ -57,6 +60,10 @@ def make_problem(name, mode=0):
         return problems.orszag_tang(1024, 1024, mode=mode)
     if name == "sod256":
         return problems.sod(256, 256, mode=mode)
+    if name == "kh2048":
+        return problems.kelvin_helmholtz(2048, 2048, mode=mode)
+    if name == "ot2048":
+        return problems.orszag_tang(2048, 2048, mode=mode)
     raise ValueError(name)
 
 

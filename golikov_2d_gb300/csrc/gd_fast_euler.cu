@@ -42,15 +42,15 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
     const double cR = gpR * rsqrt_fast(gpR * rR);
     const double aL = unL - cL, aR = unR - cR;
     const double bL = unL + cL, bR = unR + cR;
-    const double SL = aR < aL ? aR : aL;  // Davis estimates (kernel.cu:981-982)
-    const double SR = bL < bR ? bR : bL;
+    const double SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
+    const double SR = dmax(bL, bR);
     const double suL = SL - unL, suR = SR - unR;
     const double mL = rL * suL, mR = rR * suR;
     const double SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
     UU = max_nonneg(dabs(SL), dabs(SR));
 
     // Side whose state (or star state) gives the flux at x/t = 0 (kernel.cu:1119-1158).
-    const bool takeL = gt_zero(SL) || !(SM < 0.0);
+    const bool takeL = gt_zero(SL) || ge_zero(SM);
     const double r = takeL ? rL : rR;
     const double p = takeL ? pL : pR;
     const double un = takeL ? unL : unR;
@@ -58,7 +58,7 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
     const double S = takeL ? SL : SR;
     const double su = takeL ? suL : suR;
     const double mm = takeL ? mL : mR;
-    const bool star = takeL ? !gt_zero(SL) : !(SR < 0.0);
+    const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
 
     FluxE F;
     F.m = r * un;

@@ -84,12 +84,31 @@ __device__ __forceinline__ double minmod(double a, double b) {
     return zero ? 0.0 : m;
 }
 
+// Order-preserving integer key of a double (non-NaN): a < b  <=>  key(a) < key(b), with
+// -0 ordered just below +0.  Comparisons on the integer pipe instead of DSETP / DMNMX,
+// which issue on the FP64 pipe.
+__device__ __forceinline__ long long okey(double x) {
+    const long long b = bits(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ double dmin(double a, double b) { return dlt(b, a) ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return dlt(a, b) ? b : a; }
+// x < 0 strictly (-0 is not negative), x >= 0
+__device__ __forceinline__ bool lt_zero(double x) { return bits(x) < 0 && (bits(x) << 1) != 0; }
+__device__ __forceinline__ bool ge_zero(double x) { return !lt_zero(x); }
+
 // ---------------------------------------------------------------------------------------
-// FP64 reciprocal and reciprocal square root for the fast path.  Each starts from the
-// FP32 special-function estimate and refines it with Newton-Raphson iterations in FP64
-// (y <- y(2 - xy) and y <- y(3 - xy^2)/2), which doubles the number of correct bits per
-// step: 2^-22 -> 2^-44 -> below 1 ulp of double.  Valid for |x| in FP32's normal range
-// (about 1e-37 .. 1e38); outside it they fall back to the correctly rounded operation.
+// FP64 reciprocal and reciprocal square root for the fast path.
+//
+// Seed: the double's high word is re-biased into an FP32 bit pattern on the integer pipe
+// (no F2F conversion, which issues on the FP64 pipe), the FP32 special-function unit gives
+// rcp / rsqrt of it (relative error ~2^-20 from the truncated mantissa), and the FP32
+// result is re-biased back into a double.  One third-order Newton-Raphson step in FP64
+// then brings the relative error from e ~ 2^-20 to O(e^3) ~ 2^-60, below double rounding:
+//   reciprocal:  e = 1 - x y,    y <- y (1 + e + e^2)
+//   rsqrt:       e = 1 - x y^2,  y <- y (1 + e/2 + 3 e^2 / 8)
+// Valid for |x| in [2^-120, 2^120]; outside it the correctly rounded operation is used.
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ bool in_f32_range(double x) {
     // biased exponent within [1023-120, 1023+120]
@@ -97,26 +116,33 @@ __device__ __forceinline__ bool in_f32_range(double x) {
     return (e - 903u) <= 240u;
 }
 
+__device__ __forceinline__ float seed_f32(double x) {
+    const int hi = __double2hiint(x);
+    return __int_as_float((hi & (int)0x80000000) | (((hi & 0x7fffffff) - (896 << 20)) << 3));
+}
+
+__device__ __forceinline__ double widen_f32(float f) {
+    const int b = __float_as_int(f);
+    return __hiloint2double((b & (int)0x80000000) | (((b & 0x7fffffff) >> 3) + (896 << 20)),
+                            (b & 7) << 29);
+}
+
 __device__ __forceinline__ double rcp_fast(double x) {
     if (!in_f32_range(x)) return 1.0 / x;
-    double y = (double)__frcp_rn((float)x);
-    double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    return y;
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
 }
 
 __device__ __forceinline__ double rsqrt_fast(double x) {
-    if (!in_f32_range(x) || x <= 0.0) return 1.0 / sqrt(x);
-    double y = (double)rsqrtf((float)x);
-    // y <- y + y*(1 - x y^2)/2
-    double h = 0.5 * x;
-    double e = fma(-h * y, y, 0.5);
-    y = fma(y, e, y);
-    e = fma(-h * y, y, 0.5);
-    y = fma(y, e, y);
-    return y;
+    if (!in_f32_range(x) || !(x > 0.0)) return 1.0 / sqrt(x);
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double e = fma(-x * y, y, 1.0);
+    return fma(y, e * fma(0.375, e, 0.5), y);
 }
 
 __device__ __forceinline__ double sqrt_fast(double x) {

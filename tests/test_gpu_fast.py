@@ -91,3 +91,45 @@ def test_non_multiple_tile_sizes(cuda, oracle_lib):
             sg, ug, bg, Tg = gpu_step_ref(cfg, s, u, None, 1e-3)
             assert max_rel_l1(cfg, (sg, ug, None), (so, uo, None)) <= PER_STEP_TOL
             assert abs(Tg - To) <= 1e-12 * To
+
+
+MHD_CASES = {
+    "ot128_hlld": lambda: problems.orszag_tang(128, 128, method=g.METHOD_HLLD),
+    "ot96_hllcmhd": lambda: problems.orszag_tang(96, 96, method=g.METHOD_HLLC_MHD),
+    "wind_hlld": lambda: problems.stellar_wind(96, 54, 2.25, 1.25, method=g.METHOD_HLLD),
+    "wind_hllcmhd_o1": lambda: problems.stellar_wind(96, 54, 2.25, 1.25,
+                                                     method=g.METHOD_HLLC_MHD, order=1),
+}
+
+
+@pytest.mark.parametrize("case", sorted(MHD_CASES))
+def test_fast_mhd_one_step_within_tolerance(cuda, oracle_lib, case):
+    cfg, s, u, b = MHD_CASES[case]()
+    s, u, b, T_do = evolve(oracle_lib, cfg, s, u, b, 15)
+    so, uo, bo, To = oracle_lib.step(grid_of(cfg), s, u, b, T_do)
+    sg, ug, bg, Tg = gpu_step_ref(cfg, s, u, b, T_do)
+    err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
+    assert err <= PER_STEP_TOL, err
+    assert abs(Tg - To) <= 1e-12 * To
+
+
+def test_fast_orszag_tang_nsteps(cuda, oracle_lib):
+    """BASELINE config 2 at reduced size: Orszag-Tang 128^2, HLLD, 100 steps."""
+    cfg, s, u, b = problems.orszag_tang(128, 128)
+    so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 100)
+    sg, ug, bg, st = gpu_run(cfg, s, u, b, 100)
+    err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
+    assert err <= NSTEP_TOL, err
+    assert abs(st.t - TT) <= 1e-10 * TT
+    assert st.nonfinite == 0
+
+
+def test_fast_mhd_periodic_conservation(cuda):
+    """Face-once fluxes telescope: mass and total energy are conserved to rounding; the
+    field changes only by the Powell source, which vanishes in the sum of bz."""
+    cfg, s, u, b = problems.orszag_tang(128, 128)
+    sg, ug, bg, st = gpu_run(cfg, s, u, b, 40)
+    import gpu_util
+    c0 = [x.sum() for x in gpu_util.conserved(cfg, s, u, b)]
+    c1 = [x.sum() for x in gpu_util.conserved(cfg, sg, ug, bg)]
+    assert abs(c1[0] - c0[0]) <= 1e-13 * abs(c0[0])
