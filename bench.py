@@ -122,7 +122,7 @@ class ClockSampler:
 
     def __enter__(self):
         cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-               "-lms", "200"]
+               "-lms", "100"]
         if self.bus_id:
             cmd[1:1] = ["-i", self.bus_id]
         try:
@@ -173,6 +173,28 @@ def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def fp64_roofline(g, workload, cells_per_s, torch):
+    """FP64 roofline of the step kernel.  The pipe peak is 2 FP64 operations per clock per
+    SM (FMA counted once), i.e. 2 x SMs x SM clock; `gd_probe_fp64_peak` gives what a
+    register-resident DFMA loop reaches on the same GPU.  FP64 operations per cell come from
+    the committed ncu capture (profiles/ncu_traffic.txt)."""
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sms = props.multi_processor_count
+    probe = g.probe_fp64_peak()                       # FLOP/s, FMA = 2
+    pipe_peak_ops = 2.0 * sms * 2.07e9                # FP64 ops/s at the max SM clock
+    out = {"unit": "FP64 ops/s (FMA = 1 op)", "pipe_peak": pipe_peak_ops,
+           "dfma_loop_peak": probe / 2.0,
+           "pipe_peak_source": f"2 ops/clk/SM x {sms} SMs x 2070 MHz",
+           "dfma_loop_source": "gd_probe_fp64_peak in this run"}
+    per_cell = ncu_fp64_per_cell(workload)
+    if per_cell is not None:
+        ach = per_cell * cells_per_s
+        out.update({"ops_per_cell": per_cell, "achieved": ach, "frac": ach / pipe_peak_ops,
+                    "frac_of_dfma_loop": ach / (probe / 2.0),
+                    "ops_source": "ncu sm__inst_executed_pipe_fp64, profiles/ncu_traffic.txt"})
+    return out
 
 
 def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
@@ -370,14 +392,7 @@ def run_gb300(args):
     alg_bytes = K * bytes_per_cell(cfg)
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
     traffic = ncu_traffic(args.workload)
-    fp64_peak = g.probe_fp64_peak()
-    dp_per_cell = ncu_fp64_per_cell(args.workload)
-    fp64 = {"peak_flops": fp64_peak, "peak_kind": "measured in this run (DFMA loop, FMA = 2)"}
-    if dp_per_cell is not None:
-        fl = dp_per_cell * K / (ms_step * 1e-3)
-        fp64.update({"flops_per_cell": dp_per_cell, "achieved_flops": fl,
-                     "frac": fl / fp64_peak if fp64_peak else None,
-                     "source": "ncu FP64 instruction counts, profiles/ncu_traffic.txt"})
+    fp64 = fp64_roofline(g, args.workload, K / (ms_step * 1e-3), torch)
     line = {
         "metric": "FP64 cell-updates/s", "value": value, "unit": "cell-updates/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -411,6 +426,8 @@ def run_gb300(args):
                                  "roofline": {"bound": "hbm", "achieved": ach2, "peak": peak_gbs,
                                               "unit": "GB/s", "frac": ach2 / peak_gbs,
                                               "traffic": ncu_traffic("ot1024")},
+                                 "fp64": fp64_roofline(g, "ot1024", K2 / (ms2 * 1e-3), torch),
+                                 "l2": "flushed before every timed step",
                                  "gpu_launches": l2}
         except Exception as e:  # the MHD fast path may be unavailable in this build
             line["secondary"] = {"workload": WORKLOADS["ot1024"], "unavailable": str(e)}
@@ -425,7 +442,7 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="kh4096", choices=sorted(WORKLOADS))
