@@ -37,7 +37,7 @@ EXPORTS = (
     "gd_create", "gd_destroy", "gd_get_config", "gd_status_string", "gd_last_cuda_error",
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
-    "gd_probe_fp64_peak",
+    "gd_probe_fp64_peak", "gd_step_ref_static",
 )
 
 
@@ -104,9 +104,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_launch_count.restype = ll
     L.gd_launch_count.argtypes = [vp]
     L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
+    L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
-                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak"):
+                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static"):
         getattr(L, name).restype = i
     _lib = L
     return L

@@ -142,6 +142,12 @@ cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const P
 
 }  // namespace
 
+namespace gd {
+// Configuration checks and launch parameters for entry points that have no context.
+gd_status validate_config(const gd_config* c) { return validate(c); }
+Params params_from_config(const gd_config& c) { return make_params(c); }
+}  // namespace gd
+
 extern "C" {
 
 int gd_abi_version(void) { return GD_ABI_VERSION; }

@@ -39,4 +39,9 @@ cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
 cudaError_t probe_fp64_peak(double* flops);
 
+// Configuration checks and launch parameters (gd_api.cu), shared with entry points that
+// work without a context.
+gd_status validate_config(const gd_config* c);
+Params params_from_config(const gd_config& c);
+
 }  // namespace gd

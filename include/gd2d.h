@@ -156,6 +156,29 @@ gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
  * current state; plane of N*M doubles, index m*N + n.  Valid until the next advance. */
 gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
 
+/* ---- one step without device allocation ----------------------------------------------
+ * No counterpart in the reference.  For callers that must not let a library allocate
+ * device memory: a host program that owns all device memory through its own pool (a
+ * coupled multi-physics driver, an in-situ analysis framework) or that runs on a
+ * latency-critical path, where cudaMalloc would allocate outside the owner's budget and
+ * cudaFree would synchronise the whole device.
+ *
+ * Same arguments and results as gd_step_ref, but no context: the grid is given by `cfg`,
+ * and the scratch (SoA staging planes and floor counters) lives in one file-scope device
+ * array of GD_STATIC_SCRATCH_BYTES that every GPU which loads this library holds until the
+ * process exits.  Grids with N*M > GD_STATIC_MAX_CELLS are rejected with
+ * GD_ERR_INVALID_ARG before anything is launched.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and sets kernel attributes, with that
+ * device current; make that first call before any stream capture.  Every call shares the
+ * one array and it keeps the last call's contents (the counters are cleared at the start
+ * of each call): calls that overlap on the GPU (other streams, other host threads) race, so
+ * serialise them.  Calls no cudaMalloc, cudaFree or other allocating routine. */
+#define GD_STATIC_MAX_CELLS 65536
+#define GD_STATIC_SCRATCH_BYTES (256 + 2 * 7 * 8 * GD_STATIC_MAX_CELLS)
+gd_status gd_step_ref_static(const gd_config* cfg, const double* s, const double* u,
+                             const double* b, double* s2, double* u2, double* b2, double* T,
+                             const double* T_do, int method, gd_stream stream);
+
 /* ---- measurement helpers -------------------------------------------------------------- */
 
 /* Number of kernel launches the library issued on behalf of this context so far. */
