@@ -197,6 +197,47 @@ def fp64_roofline(g, workload, cells_per_s, torch):
     return out
 
 
+def measure_batched(g, torch, steps, ngrids=512):
+    """BASELINE config 4: 512 independent four-quadrant Riemann problems, sides log-uniform
+    in [64, 512] (seeded), HLLC + minmod.  Persistent launch per step under a captured CUDA
+    graph (tile shape from the autotuner) vs a loop of plain launches (one per grid)."""
+    from golikov_2d_gb300 import problems
+    grids = problems.batch_four_quadrant(ngrids)
+    b = g.Batch([c for c, *_ in grids])
+    for k, (c, s, u, _) in enumerate(grids):
+        b.import_grid(k, s, u)
+    b.set_time(0.0, 0.0)
+    b.init_dt()
+    b.autotune(reps=3)
+    info = b.info()
+    cells = info.total_cells
+    stream = torch.cuda.current_stream()
+    res = {"workload": f"{ngrids} four-quadrant Riemann grids, sides log-uniform in [64, 512] "
+                       f"(seed {problems.BATCH_SEED}), Euler HLLC + minmod, FP64",
+           "total_cells": cells, "steps": steps,
+           "tile": f"{info.tile_x}x{info.tile_y}", "ctas": info.ctas, "tiles": info.tiles,
+           "autotune_ms_per_step": {f"{tx}x{ty}": round(info.tuned_ms[v], 4) for v, (tx, ty) in
+                                    enumerate(((32, 16), (32, 8), (16, 16), (64, 8)))}}
+    for name, sched, graph in (("persistent_graph", g.BATCH_PERSISTENT, True),
+                               ("looped_plain", g.BATCH_LOOPED, False)):
+        b.advance(steps, schedule=sched, use_graph=graph)  # warm-up (captures the graph)
+        torch.cuda.synchronize()
+        l0 = b.launch_count()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        b.advance(steps, schedule=sched, use_graph=graph)
+        z.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(z)
+        res[name] = {"value": cells * steps / (ms * 1e-3), "unit": "cell-updates/s",
+                     "ms_per_step": ms / steps, "gpu_launches": b.launch_count() - l0}
+    res["speedup"] = res["persistent_graph"]["value"] / res["looped_plain"]["value"]
+    bad = sum(b.stats(k, allow_nonfinite=True).nonfinite for k in range(ngrids))
+    res["nonfinite_cells"] = bad
+    b.close()
+    return res
+
+
 def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
     """The oracle on all host cores, `nsteps` full steps of the workload."""
     import oracle
@@ -431,6 +472,11 @@ def run_gb300(args):
                                  "gpu_launches": l2}
         except Exception as e:  # the MHD fast path may be unavailable in this build
             line["secondary"] = {"workload": WORKLOADS["ot1024"], "unavailable": str(e)}
+    if args.batched:
+        try:
+            line["batched"] = measure_batched(g, torch, min(args.steps, 100))
+        except Exception as e:
+            line["batched"] = {"unavailable": str(e)}
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args.workload, cfg, s, u, b)
     print(json.dumps(line), flush=True)
@@ -448,6 +494,7 @@ def main():
     ap.add_argument("--workload", default="kh4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--secondary", type=int, default=1)
+    ap.add_argument("--batched", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -38,7 +38,11 @@ EXPORTS = (
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
     "gd_probe_fp64_peak", "gd_step_ref_static",
+    "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
+    "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
+    "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
 )
+BATCH_PERSISTENT, BATCH_LOOPED = 0, 1
 
 
 class GdError(RuntimeError):
@@ -58,6 +62,14 @@ class gd_config(ctypes.Structure):
         ("bc", ctypes.c_int * 4),
         ("frozen_radius", ctypes.c_double),
         ("mode", ctypes.c_int),
+    ]
+
+
+class gd_batch_info(ctypes.Structure):
+    _fields_ = [
+        ("ngrids", ctypes.c_int), ("total_cells", ctypes.c_longlong),
+        ("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int), ("ctas", ctypes.c_int),
+        ("tiles", ctypes.c_longlong), ("tuned_ms", ctypes.c_double * 4),
     ]
 
 
@@ -105,9 +117,24 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_launch_count.argtypes = [vp]
     L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
+    L.gd_batch_create.argtypes = [cfgp, i, ctypes.POINTER(vp)]
+    L.gd_batch_destroy.argtypes = [vp]
+    L.gd_batch_import.argtypes = [vp, i, vp, vp, vp, i, vp]
+    L.gd_batch_export.argtypes = [vp, i, vp, vp, vp, i, vp]
+    L.gd_batch_set_time.argtypes = [vp, d, d, vp]
+    L.gd_batch_init_dt.argtypes = [vp, vp]
+    L.gd_batch_advance.argtypes = [vp, i, i, i, vp]
+    L.gd_batch_autotune.argtypes = [vp, i, vp]
+    L.gd_batch_get_stats.argtypes = [vp, i, ctypes.POINTER(gd_stats), vp]
+    L.gd_batch_get_info.argtypes = [vp, ctypes.POINTER(gd_batch_info)]
+    L.gd_batch_launch_count.restype = ll
+    L.gd_batch_launch_count.argtypes = [vp]
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
-                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static"):
+                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
+                 "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
+                 "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
+                 "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -242,6 +269,74 @@ class Solver:
 
     def launch_count(self) -> int:
         return int(self.lib.gd_launch_count(self.handle))
+
+
+class Batch:
+    """Many independent Euler grids advanced together (gd_batch_*)."""
+
+    def __init__(self, cfgs):
+        self.cfgs = list(cfgs)
+        self.lib = load()
+        arr = (gd_config * len(self.cfgs))(*[c.cstruct() for c in self.cfgs])
+        self._arr = arr
+        h = ctypes.c_void_p()
+        _check(self.lib.gd_batch_create(arr, len(self.cfgs), ctypes.byref(h)), "gd_batch_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.gd_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def import_grid(self, g, s, u, stream=None) -> None:
+        host, ptrs = Solver._ptrs(s, u, None)
+        _check(self.lib.gd_batch_import(self.handle, int(g), ptrs[0], ptrs[1], None,
+                                        1 if host else 0, _stream_handle(stream)),
+               "gd_batch_import")
+
+    def export_grid(self, g, s, u, stream=None) -> None:
+        host, ptrs = Solver._ptrs(s, u, None)
+        _check(self.lib.gd_batch_export(self.handle, int(g), ptrs[0], ptrs[1], None,
+                                        1 if host else 0, _stream_handle(stream)),
+               "gd_batch_export")
+
+    def set_time(self, T_do, TT=0.0, stream=None) -> None:
+        _check(self.lib.gd_batch_set_time(self.handle, float(T_do), float(TT),
+                                          _stream_handle(stream)), "gd_batch_set_time")
+
+    def init_dt(self, stream=None) -> None:
+        _check(self.lib.gd_batch_init_dt(self.handle, _stream_handle(stream)), "gd_batch_init_dt")
+
+    def advance(self, nsteps, schedule=BATCH_PERSISTENT, use_graph=False, stream=None) -> None:
+        _check(self.lib.gd_batch_advance(self.handle, int(nsteps), int(schedule),
+                                         1 if use_graph else 0, _stream_handle(stream)),
+               "gd_batch_advance")
+
+    def autotune(self, reps=3, stream=None) -> None:
+        _check(self.lib.gd_batch_autotune(self.handle, int(reps), _stream_handle(stream)),
+               "gd_batch_autotune")
+
+    def stats(self, g, stream=None, allow_nonfinite=False) -> gd_stats:
+        st = gd_stats()
+        r = self.lib.gd_batch_get_stats(self.handle, int(g), ctypes.byref(st),
+                                        _stream_handle(stream))
+        if not (r == 3 and allow_nonfinite):
+            _check(r, "gd_batch_get_stats")
+        return st
+
+    def info(self) -> gd_batch_info:
+        inf = gd_batch_info()
+        _check(self.lib.gd_batch_get_info(self.handle, ctypes.byref(inf)), "gd_batch_get_info")
+        return inf
+
+    def launch_count(self) -> int:
+        return int(self.lib.gd_batch_launch_count(self.handle))
 
 
 def probe_fp64_peak() -> float:

@@ -10,6 +10,11 @@
 // The reference computes every face twice, once from each neighbour (kernel.cu:3560-3586);
 // here each face is computed once and used with opposite signs by its two cells.
 //
+// Two kernels share the tile body: euler_fast_kernel (one grid, one CTA per tile) and
+// euler_batch_kernel (a persistent launch that walks the tiles of many independent grids,
+// each grid with its own parameters, state, dt reduction and funk_time rotation).  Tile
+// shapes 32x16, 32x8, 16x16 and 64x8 are compiled; the autotuner picks one.
+//
 // Reference semantics kept: primitive reconstruction of (rho, p, vx, vy) with the rho/p
 // face fallback to the cell value (kernel.cu:3436-3544), Davis wave speeds and the HLLC
 // star states of HLLC_Aleksashov (kernel.cu:853-1165), the Ker_Dekard update and floors
@@ -21,8 +26,6 @@
 namespace gd {
 namespace {
 
-constexpr int TX = 32;
-constexpr int TY = 16;
 constexpr int NT = 256;
 constexpr int NF = 4;
 
@@ -72,16 +75,16 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
         const double pst = fma(mm, SM - un, p);
         const double ez = (fma(E, su, pst * SM) - p * un) * inv;
         const double drz = rz - r;
+        F.mn = fma(S, fma(rz, SM, -F.m), F.mn);
         F.m = fma(S, drz, F.m);
-        F.mn = fma(S, fma(rz, SM, -r * un), F.mn);
         F.mt = fma(S, ut * drz, F.mt);
         F.e = fma(S, ez - E, F.e);
     }
     return F;
 }
 
-template <int ORDER>
-struct Smem {
+template <int ORDER, int TX, int TY>
+struct Shape {
     static constexpr int H = ORDER == 2 ? 2 : 1;
     static constexpr int SX = TX + 2 * H;
     static constexpr int SY = TY + 2 * H;
@@ -93,14 +96,20 @@ struct Smem {
     static constexpr size_t bytes = sizeof(double) * (kPrim + kSlx + kSly + kFx + kFy);
 };
 
-template <int ORDER>
-__global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Planes out,
-                                                        const double* __restrict__ T_do_ptr,
-                                                        unsigned long long* T_bits, Scalars* rot,
-                                                        Scalars* ctr, int dt_only) {
-    using S = Smem<ORDER>;
+struct TileResult {
+    double umax_x, umax_y;
+    bool any_active;
+    unsigned int nfl_r, nfl_p, nbad;
+};
+
+// One TX x TY tile whose lower-left cell is (tx0, ty0).  Reads `in`, writes `out`, returns
+// the per-thread wave-speed maxima and counters.  Every thread of the block must call it.
+template <int ORDER, int TX, int TY>
+__device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, const Planes& out,
+                                           int tx0, int ty0, double T_do, int dt_only,
+                                           double* smem, TileResult& res) {
+    using S = Shape<ORDER, TX, TY>;
     constexpr int H = S::H, SX = S::SX, SY = S::SY;
-    extern __shared__ double smem[];
     double* prim = smem;                 // [NF][SY][SX]
     double* slx = prim + S::kPrim;       // [NF][TY][TX+2]   cells x in [-1, TX]
     double* sly = slx + S::kSlx;         // [NF][TY+2][TX]   cells y in [-1, TY]
@@ -108,7 +117,6 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
     double* fy = fx + S::kFx;            // [NF][TY+1][TX]   face between y-1 and y
 
     const int tid = threadIdx.x;
-    const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
     const int N = P.N, M = P.M;
 
     // ---- L: tile + cross halo ------------------------------------------------------------
@@ -171,9 +179,8 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
         }
         // cells on either side: A (low) and B (high)
         const int ax = isx ? lx - 1 : lx, ay = isx ? ly : ly - 1;
-        if (P.frozen_radius > 0.0 &&
-            !cell_active(P, tx0 + ax, ty0 + ay) &&
-            !cell_active(P, tx0 + (isx ? lx : lx), ty0 + (isx ? ly : ly)))
+        if (P.frozen_radius > 0.0 && !cell_active(P, tx0 + ax, ty0 + ay) &&
+            !cell_active(P, tx0 + lx, ty0 + ly))
             continue;  // no updated cell uses this face
         const double* pa = prim + (ay + H) * SX + (ax + H);
         const double* pb = pa + (isx ? 1 : SX);
@@ -205,16 +212,15 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
         double UU;
         const FluxE F = hllc_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
                                    qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU);
-        double* fo;
         if (isx) {
-            fo = fx + ly * (TX + 1) + lx;
+            double* fo = fx + ly * (TX + 1) + lx;
             fo[0 * TY * (TX + 1)] = F.m;
             fo[1 * TY * (TX + 1)] = F.e;
             fo[2 * TY * (TX + 1)] = F.mn;  // x momentum
             fo[3 * TY * (TX + 1)] = F.mt;  // y momentum
             umax_x = max_nonneg(umax_x, UU);
         } else {
-            fo = fy + ly * TX + lx;
+            double* fo = fy + ly * TX + lx;
             fo[0 * (TY + 1) * TX] = F.m;
             fo[1 * (TY + 1) * TX] = F.e;
             fo[2 * (TY + 1) * TX] = F.mt;  // x momentum
@@ -225,7 +231,6 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
     __syncthreads();
 
     // ---- U: update --------------------------------------------------------------------------
-    const double T_do = *T_do_ptr;
     const double kx = T_do / P.dx, ky = T_do / P.dy;
     bool any_active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
@@ -270,41 +275,197 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
         out.f[2][k] = u2;
         out.f[3][k] = v2;
     }
-    if (ctr != nullptr && (nfl_r | nfl_p | nbad)) {
-        if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
-        if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
-        if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
-    }
-    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot);
+    res.umax_x = umax_x;
+    res.umax_y = umax_y;
+    res.any_active = any_active;
+    res.nfl_r = nfl_r;
+    res.nfl_p = nfl_p;
+    res.nbad = nbad;
 }
 
-template <int ORDER>
-cudaError_t launch_euler_fast_t(const Params& P, const CPlanes& in, const Planes& out,
-                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
-                                Scalars* ctr, int dt_only, cudaStream_t st) {
+__device__ __forceinline__ void add_counters(Scalars* ctr, const TileResult& r) {
+    if (ctr != nullptr && (r.nfl_r | r.nfl_p | r.nbad)) {
+        if (r.nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)r.nfl_r);
+        if (r.nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)r.nfl_p);
+        if (r.nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)r.nbad);
+    }
+}
+
+template <int ORDER, int TX, int TY>
+__global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Planes out,
+                                                        const double* __restrict__ T_do_ptr,
+                                                        unsigned long long* T_bits, Scalars* rot,
+                                                        Scalars* ctr, int dt_only) {
+    extern __shared__ double smem[];
+    TileResult r;
+    euler_tile<ORDER, TX, TY>(P, in, out, blockIdx.x * TX, blockIdx.y * TY, *T_do_ptr, dt_only,
+                              smem, r);
+    add_counters(ctr, r);
+    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot);
+}
+
+// Persistent batched step: CTAs stride over the flattened (grid, tile) work list; each tile
+// reports its dt to its own grid, and the last tile of a grid rotates that grid's dt.
+// With dt_only, tiles only min-combine their dt (no state write, no rotation).
+// `sc_override` (may be null) replaces every grid's scalars (the autotuner times steps
+// without touching the real dt and time).
+template <int ORDER, int TX, int TY>
+__global__ void __launch_bounds__(NT) euler_batch_kernel(const BatchGrid* __restrict__ grids,
+                                                         const int2* __restrict__ items,
+                                                         int nitems, int cur, int dt_only,
+                                                         Scalars* sc_override) {
+    extern __shared__ double smem[];
+    __shared__ BatchGrid g;
+    __shared__ int tile;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        __syncthreads();  // the previous tile is done with smem and g
+        if (threadIdx.x == 0) {
+            const int2 w = items[it];
+            g = grids[w.x];
+            if (sc_override != nullptr) g.sc = sc_override + w.x;
+            tile = w.y;
+        }
+        __syncthreads();
+        const long long K = g.K;
+        CPlanes in{};
+        Planes out{};
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            in.f[f] = g.state[cur] + f * K;
+            out.f[f] = g.state[cur ^ 1] + f * K;
+        }
+        const int tx0 = (tile % g.tiles_x) * TX, ty0 = (tile / g.tiles_x) * TY;
+        const double T_do = g.sc->T_do;
+        TileResult r;
+        euler_tile<ORDER, TX, TY>(g.P, in, out, tx0, ty0, T_do, dt_only, smem, r);
+        add_counters(dt_only ? nullptr : g.sc, r);
+        block_dt_and_rotate<NT>(g.P, r.umax_x, r.umax_y, r.any_active, &g.sc->T_bits,
+                                dt_only ? nullptr : g.sc, (unsigned int)g.ntiles);
+    }
+}
+
+template <int ORDER, int TX, int TY>
+cudaError_t set_attrs() {
+    cudaError_t e = cudaFuncSetAttribute(euler_fast_kernel<ORDER, TX, TY>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Shape<ORDER, TX, TY>::bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(euler_batch_kernel<ORDER, TX, TY>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Shape<ORDER, TX, TY>::bytes);
+}
+
+template <int ORDER, int TX, int TY>
+cudaError_t launch_single(const Params& P, const CPlanes& in, const Planes& out,
+                          const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                          Scalars* ctr, int dt_only, cudaStream_t st) {
     dim3 grid((P.N + TX - 1) / TX, (P.M + TY - 1) / TY);
-    euler_fast_kernel<ORDER><<<grid, NT, Smem<ORDER>::bytes, st>>>(P, in, out, T_do, T_bits, rot,
-                                                                    ctr, dt_only);
+    euler_fast_kernel<ORDER, TX, TY><<<grid, NT, Shape<ORDER, TX, TY>::bytes, st>>>(
+        P, in, out, T_do, T_bits, rot, ctr, dt_only);
     return cudaGetLastError();
 }
 
+template <int ORDER, int TX, int TY>
+cudaError_t launch_batch(const BatchGrid* grids, const int2* items, int nitems, int cur,
+                         int dt_only, Scalars* sc_override, int ctas, cudaStream_t st) {
+    euler_batch_kernel<ORDER, TX, TY><<<ctas, NT, Shape<ORDER, TX, TY>::bytes, st>>>(
+        grids, items, nitems, cur, dt_only, sc_override);
+    return cudaGetLastError();
+}
+
+// tile shapes of the variants: 0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8
+#define GD_EULER_DISPATCH(ORDER, VAR, CALL, ARGS) \
+    switch (VAR) {                                \
+        case 1: return CALL<ORDER, 32, 8> ARGS;   \
+        case 2: return CALL<ORDER, 16, 16> ARGS;  \
+        case 3: return CALL<ORDER, 64, 8> ARGS;   \
+        default: return CALL<ORDER, 32, 16> ARGS; \
+    }
+
 }  // namespace
 
+void euler_tile_shape(int variant, int* tx, int* ty) {
+    static const int shapes[kEulerVariants][2] = {{32, 16}, {32, 8}, {16, 16}, {64, 8}};
+    const int v = (variant >= 0 && variant < kEulerVariants) ? variant : 0;
+    *tx = shapes[v][0];
+    *ty = shapes[v][1];
+}
+
+size_t euler_smem_bytes(int order, int variant) {
+    switch (variant) {
+        case 1: return order == 1 ? Shape<1, 32, 8>::bytes : Shape<2, 32, 8>::bytes;
+        case 2: return order == 1 ? Shape<1, 16, 16>::bytes : Shape<2, 16, 16>::bytes;
+        case 3: return order == 1 ? Shape<1, 64, 8>::bytes : Shape<2, 64, 8>::bytes;
+        default: return order == 1 ? Shape<1, 32, 16>::bytes : Shape<2, 32, 16>::bytes;
+    }
+}
+
+namespace {
+template <int ORDER, int TX, int TY>
+int blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, euler_batch_kernel<ORDER, TX, TY>, NT,
+                                                      Shape<ORDER, TX, TY>::bytes) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
+}
+}  // namespace
+
+int euler_batch_blocks_per_sm(int order, int variant) {
+    if (order == 1) {
+        switch (variant) {
+            case 1: return blocks_per_sm<1, 32, 8>();
+            case 2: return blocks_per_sm<1, 16, 16>();
+            case 3: return blocks_per_sm<1, 64, 8>();
+            default: return blocks_per_sm<1, 32, 16>();
+        }
+    }
+    switch (variant) {
+        case 1: return blocks_per_sm<2, 32, 8>();
+        case 2: return blocks_per_sm<2, 16, 16>();
+        case 3: return blocks_per_sm<2, 64, 8>();
+        default: return blocks_per_sm<2, 32, 16>();
+    }
+}
+
 cudaError_t prepare_euler_fast() {
-    cudaError_t e = cudaFuncSetAttribute(euler_fast_kernel<1>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)Smem<1>::bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(euler_fast_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)Smem<2>::bytes);
+    cudaError_t e = set_attrs<1, 32, 16>();
+    if (e == cudaSuccess) e = set_attrs<2, 32, 16>();
+    if (e == cudaSuccess) e = set_attrs<1, 32, 8>();
+    if (e == cudaSuccess) e = set_attrs<2, 32, 8>();
+    if (e == cudaSuccess) e = set_attrs<1, 16, 16>();
+    if (e == cudaSuccess) e = set_attrs<2, 16, 16>();
+    if (e == cudaSuccess) e = set_attrs<1, 64, 8>();
+    if (e == cudaSuccess) e = set_attrs<2, 64, 8>();
+    return e;
+}
+
+cudaError_t launch_euler_fast_v(int variant, const Params& P, const CPlanes& in,
+                                const Planes& out, const double* T_do,
+                                unsigned long long* T_bits, Scalars* rot, Scalars* ctr,
+                                int dt_only, cudaStream_t st) {
+    if (P.order == 1) {
+        GD_EULER_DISPATCH(1, variant, launch_single,
+                          (P, in, out, T_do, T_bits, rot, ctr, dt_only, st));
+    }
+    GD_EULER_DISPATCH(2, variant, launch_single, (P, in, out, T_do, T_bits, rot, ctr, dt_only, st));
 }
 
 cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& out,
                               const double* T_do, unsigned long long* T_bits, Scalars* rot,
                               Scalars* ctr, int dt_only, cudaStream_t st) {
-    if (P.order == 1)
-        return launch_euler_fast_t<1>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
-    return launch_euler_fast_t<2>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+    return launch_euler_fast_v(0, P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, const int2* items,
+                               int nitems, int cur, int dt_only, Scalars* sc_override, int ctas,
+                               cudaStream_t st) {
+    if (order == 1) {
+        GD_EULER_DISPATCH(1, variant, launch_batch,
+                          (grids, items, nitems, cur, dt_only, sc_override, ctas, st));
+    }
+    GD_EULER_DISPATCH(2, variant, launch_batch,
+                      (grids, items, nitems, cur, dt_only, sc_override, ctas, st));
 }
 
 }  // namespace gd

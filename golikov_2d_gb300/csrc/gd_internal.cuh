@@ -44,6 +44,19 @@ struct CPlanes {
     const double* f[kMaxFields];
 };
 
+struct Scalars;
+
+// One grid of a batch, device-resident: its parameters, its two state buffers (nf planes
+// of K doubles each), its scalars, and its tiling for the kernel variant in use.
+struct BatchGrid {
+    Params P;
+    double* state[2];
+    long long K;
+    Scalars* sc;
+    int tiles_x;
+    int ntiles;
+};
+
 // Device-resident time-step scalars of one grid (the reference's T, T_do, TT, i).
 struct Scalars {
     unsigned long long T_bits;  // running min of the CFL dt, as the bits of a positive double
@@ -238,10 +251,12 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // into *T_bits.  `any_active` says whether the block contains a non-frozen cell.  Then,
 // if `sc` is given, the last block to finish performs the funk_time rotation on it.
 // Must be called by every thread of the block.
+// `nblocks` is the number of blocks (tiles) that report to `sc` in this launch; 0 means
+// every block of the grid.
 template <int NTHREADS>
 __device__ void block_dt_and_rotate(const Params& P, double umax_x, double umax_y,
                                     bool any_active, unsigned long long* T_bits,
-                                    Scalars* sc) {
+                                    Scalars* sc, unsigned int nblocks = 0) {
     __shared__ unsigned long long red[2][NTHREADS / 32];
     __shared__ int act[NTHREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -277,9 +292,9 @@ __device__ void block_dt_and_rotate(const Params& P, double umax_x, double umax_
         }
         if (sc != nullptr) {
             __threadfence();
-            const unsigned int nblocks = gridDim.x * gridDim.y * gridDim.z;
+            const unsigned int nb = nblocks ? nblocks : gridDim.x * gridDim.y * gridDim.z;
             const unsigned int ticket = atomicAdd(&sc->done, 1u);
-            if (ticket == nblocks - 1) {
+            if (ticket == nb - 1) {
                 __threadfence();
                 const double T = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
                 sc->T_do = T;

@@ -22,6 +22,26 @@ cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& ou
                             const double* T_do, unsigned long long* T_bits, Scalars* rot,
                             Scalars* ctr, int dt_only, cudaStream_t st);
 
+// Tile-shape variants of the fast Euler kernels (0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8).
+constexpr int kEulerVariants = 4;
+void euler_tile_shape(int variant, int* tx, int* ty);
+size_t euler_smem_bytes(int order, int variant);
+cudaError_t launch_euler_fast_v(int variant, const Params& P, const CPlanes& in,
+                                const Planes& out, const double* T_do,
+                                unsigned long long* T_bits, Scalars* rot, Scalars* ctr,
+                                int dt_only, cudaStream_t st);
+// Resident CTAs per SM of the persistent batched kernel of a variant.
+int euler_batch_blocks_per_sm(int order, int variant);
+// Per-grid scalar kernels of a batch (gd_util.cu).
+cudaError_t launch_batch_set_time(BatchGrid* grids, int ngrids, double T_do, double TT,
+                                  cudaStream_t st);
+cudaError_t launch_batch_reset_T(BatchGrid* grids, int ngrids, cudaStream_t st);
+cudaError_t launch_batch_dt_commit(BatchGrid* grids, int ngrids, cudaStream_t st);
+// Persistent batched step over the (grid, tile) list `items` with `ctas` CTAs.
+cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, const int2* items,
+                               int nitems, int cur, int dt_only, Scalars* sc_override, int ctas,
+                               cudaStream_t st);
+
 // Parity step: per-cell faces in the reference's arithmetic order (built without FMA
 // contraction); bit-identical to the reference step.
 cudaError_t launch_parity(const Params& P, const CPlanes& in, const Planes& out,

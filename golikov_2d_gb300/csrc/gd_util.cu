@@ -46,11 +46,15 @@ __global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i) {
     *i = *i + 1;
 }
 
-__global__ void set_time_kernel(Scalars* sc, double T_do, double TT) {
+__device__ __forceinline__ void set_time_kernel_body(Scalars* sc, double T_do, double TT) {
     sc->T_do = T_do;
     sc->TT = TT;
     sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
     sc->done = 0;
+}
+
+__global__ void set_time_kernel(Scalars* sc, double T_do, double TT) {
+    set_time_kernel_body(sc, T_do, TT);
 }
 
 // End of a dt-only pass: T_do <- T, T <- 1e7 (TT and the step counter unchanged).
@@ -61,6 +65,27 @@ __global__ void dt_commit_kernel(Scalars* sc) {
 }
 
 __global__ void reset_T_kernel(Scalars* sc) {
+    sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
+    sc->done = 0;
+}
+
+// Per-grid versions for a batch: one thread per grid.
+__global__ void batch_set_time_kernel(BatchGrid* grids, int ngrids, double T_do, double TT) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ngrids) set_time_kernel_body(grids[g].sc, T_do, TT);
+}
+__global__ void batch_reset_T_kernel(BatchGrid* grids, int ngrids) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngrids) return;
+    Scalars* sc = grids[g].sc;
+    sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
+    sc->done = 0;
+}
+__global__ void batch_dt_commit_kernel(BatchGrid* grids, int ngrids) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngrids) return;
+    Scalars* sc = grids[g].sc;
+    sc->T_do = __longlong_as_double((long long)sc->T_bits);
     sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
     sc->done = 0;
 }
@@ -109,6 +134,22 @@ cudaError_t launch_funk_time(double* T, double* T_do, double* TT, int* i, cudaSt
 
 cudaError_t launch_set_time(Scalars* sc, double T_do, double TT, cudaStream_t st) {
     set_time_kernel<<<1, 1, 0, st>>>(sc, T_do, TT);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_set_time(BatchGrid* grids, int ngrids, double T_do, double TT,
+                                  cudaStream_t st) {
+    batch_set_time_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(grids, ngrids, T_do, TT);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_reset_T(BatchGrid* grids, int ngrids, cudaStream_t st) {
+    batch_reset_T_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(grids, ngrids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_dt_commit(BatchGrid* grids, int ngrids, cudaStream_t st) {
+    batch_dt_commit_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(grids, ngrids);
     return cudaGetLastError();
 }
 

@@ -119,3 +119,22 @@ def stellar_wind(N=3226, M=1792, xmax=9.0, ymax=5.0, krit=0.25, method=METHOD_HL
     bz = np.where(inside, BE * np.sin(np.arccos(np.clip(X / dsafe, -1.0, 1.0))), 0.0)
     b = np.stack([np.zeros(K), np.zeros(K), bz], 1)
     return cfg, np.ascontiguousarray(s), np.ascontiguousarray(u), np.ascontiguousarray(b)
+
+
+BATCH_SEED = 20261203
+
+
+def batch_sides(n=512, lo=64, hi=512, seed=BATCH_SEED):
+    """Grid sides log-uniform in [lo, hi]: round(exp(U(ln lo, ln hi))) from the seed."""
+    rng = np.random.default_rng(seed)
+    return [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(n)]
+
+
+def batch_four_quadrant(n=512, lo=64, hi=512, seed=BATCH_SEED, krit=0.4):
+    """The batched workload: n independent four-quadrant Riemann problems on square grids
+    whose sides are log-uniform in [lo, hi]; per-quadrant rho, p ~ U[0.1, 2] and
+    vx, vy ~ U[-1, 1]; HLLC + minmod, transmissive boundaries.  Returns a list of
+    (Config, s, u, None)."""
+    sides = batch_sides(n, lo, hi, seed)
+    rng = np.random.default_rng(seed + 1)
+    return [four_quadrant(side, rng, krit=krit) for side in sides]

@@ -156,6 +156,41 @@ gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
  * current state; plane of N*M doubles, index m*N + n.  Valid until the next advance. */
 gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
 
+/* ---- batched: many independent grids --------------------------------------------------
+ * No counterpart in the reference (it advances one grid, kernel.cu:4102).  A batch holds
+ * ngrids independent grids of any sizes (same physics, order and mode; Euler, fast mode),
+ * each with its own boundaries, dt reduction, dt rotation and time.  Schedules:
+ *   GD_BATCH_PERSISTENT  one persistent launch per step walks the tiles of every grid
+ *   GD_BATCH_LOOPED      one plain launch per grid per step (the baseline)
+ * gd_batch_autotune times every compiled tile shape (32x16, 32x8, 16x16, 64x8; the halo
+ * width is the stencil's, 2 cells for order 2) on the batch's own grids without changing
+ * their state or time, and keeps the fastest for GD_BATCH_PERSISTENT. */
+enum { GD_BATCH_PERSISTENT = 0, GD_BATCH_LOOPED = 1 };
+typedef struct gd_batch gd_batch;
+typedef struct gd_batch_info {
+    int ngrids;
+    long long total_cells;
+    int tile_x, tile_y;        /* tile shape in use for the persistent schedule */
+    int ctas;                  /* CTAs of the persistent launch */
+    long long tiles;           /* work items per persistent step */
+    double tuned_ms[4];        /* autotuner: ms per step of each tile shape (0 = not timed) */
+} gd_batch_info;
+
+gd_status gd_batch_create(const gd_config* cfgs, int ngrids, gd_batch** out);
+gd_status gd_batch_destroy(gd_batch* b);
+gd_status gd_batch_import(gd_batch* b, int grid, const double* s, const double* u,
+                          const double* bfield, int is_host, gd_stream stream);
+gd_status gd_batch_export(gd_batch* b, int grid, double* s, double* u, double* bfield,
+                          int is_host, gd_stream stream);
+gd_status gd_batch_set_time(gd_batch* b, double T_do, double TT, gd_stream stream);
+gd_status gd_batch_init_dt(gd_batch* b, gd_stream stream);
+gd_status gd_batch_advance(gd_batch* b, int nsteps, int schedule, int use_graph,
+                           gd_stream stream);
+gd_status gd_batch_autotune(gd_batch* b, int reps, gd_stream stream);
+gd_status gd_batch_get_stats(gd_batch* b, int grid, gd_stats* out, gd_stream stream);
+gd_status gd_batch_get_info(const gd_batch* b, gd_batch_info* out);
+long long gd_batch_launch_count(const gd_batch* b);
+
 /* ---- one step without device allocation ----------------------------------------------
  * No counterpart in the reference.  For callers that must not let a library allocate
  * device memory: a host program that owns all device memory through its own pool (a

@@ -1,0 +1,79 @@
+"""Batched form: many independent grids of uneven sizes in one persistent launch per step.
+
+The persistent schedule, the looped schedule (one launch per grid), CUDA-graph replay and
+every autotuned tile shape run the same per-face arithmetic, so they must agree bit for
+bit; each grid must also agree bit for bit with the single-grid context and, to the fast
+path's tolerance, with the oracle."""
+import numpy as np
+import pytest
+
+import golikov_2d_gb300 as g
+from golikov_2d_gb300 import problems
+from gpu_util import gpu_run, max_rel_l1, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(n=12, seed=3):
+    return problems.batch_four_quadrant(n, lo=20, hi=90, seed=seed)
+
+
+def run_batch(grids, nsteps, schedule=g.BATCH_PERSISTENT, use_graph=False, autotune=False):
+    b = g.Batch([c for c, *_ in grids])
+    for k, (c, s, u, _) in enumerate(grids):
+        b.import_grid(k, s, u)
+    b.set_time(0.0, 0.0)
+    b.init_dt()
+    if autotune:
+        b.autotune(reps=2)
+    b.advance(nsteps, schedule=schedule, use_graph=use_graph)
+    out = []
+    for k, (c, s, u, _) in enumerate(grids):
+        s2, u2 = np.zeros_like(s), np.zeros_like(u)
+        b.export_grid(k, s2, u2)
+        out.append((s2, u2, b.stats(k)))
+    info = b.info()
+    b.close()
+    return out, info
+
+
+def same(a, c):
+    return all(np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1]) and
+               x[2].t == y[2].t and x[2].dt == y[2].dt for x, y in zip(a, c))
+
+
+def test_persistent_equals_looped_and_graph(cuda):
+    grids = small_batch()
+    a, info = run_batch(grids, 9)
+    assert info.ngrids == len(grids) and info.tiles > 0
+    c, _ = run_batch(grids, 9, schedule=g.BATCH_LOOPED)
+    d, _ = run_batch(grids, 9, use_graph=True)
+    assert same(a, c) and same(a, d)
+    for x in a:
+        assert x[2].steps == 9 and x[2].nonfinite == 0
+
+
+def test_autotune_keeps_state_and_any_tile_shape_agrees(cuda):
+    grids = small_batch(seed=4)
+    a, _ = run_batch(grids, 6)
+    c, info = run_batch(grids, 6, autotune=True)
+    assert all(t > 0 for t in info.tuned_ms)
+    assert same(a, c)
+
+
+def test_batch_grid_equals_single_grid_context(cuda):
+    grids = small_batch(n=5, seed=5)
+    a, _ = run_batch(grids, 7)
+    for (cfg, s, u, b), (s2, u2, st) in zip(grids, a):
+        ss, us, _, sst = gpu_run(cfg, s, u, b, 7)
+        assert np.array_equal(ss, s2) and np.array_equal(us, u2)
+        assert sst.t == st.t and sst.dt == st.dt
+
+
+def test_batch_against_oracle(cuda, oracle_lib):
+    grids = small_batch(n=4, seed=6)
+    a, _ = run_batch(grids, 10)
+    for (cfg, s, u, b), (s2, u2, st) in zip(grids, a):
+        so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 10)
+        assert max_rel_l1(cfg, (s2, u2, None), (so, uo, None)) <= 1e-10
+        assert abs(st.t - TT) <= 1e-11 * TT
