@@ -168,6 +168,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_aggregate(t_local, cells_local, device):
+    """Whole-job numbers of a replicated run: the slowest rank's time (MAX over ranks) and
+    the cell-updates of all ranks (SUM).  Identity when torch.distributed is not running."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return t_local, cells_local
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    c = torch.tensor([float(cells_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(c.item())
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -388,13 +402,10 @@ def run_gb300(args):
             torch.cuda.synchronize()
             ms_total = a.elapsed_time(z)
     launches = sol.launch_count() - l0
-    if ws > 1:
-        t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total, job_cells = job_aggregate(ms_total, K * args.steps, "cuda")
     stats = sol.stats(allow_nonfinite=True)
     ms_step = ms_total / args.steps
-    value = ws * K * args.steps / (ms_total * 1e-3)
+    value = job_cells / (ms_total * 1e-3)
 
     # ---- e2e: host buffers through the C ABI, copies inside the timed region ---------------
     hs = torch.from_numpy(s).pin_memory()
@@ -416,12 +427,9 @@ def run_gb300(args):
         sol.export_state(hs2, hu2, hb2)  # synchronises the stream
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s, e2e_cells = job_aggregate(e2e_s, K * e2e_steps, "cuda")
     io_bytes = K * (4 + (3 if b is not None else 0)) * 8
-    e2e = {"value": ws * K * e2e_steps / e2e_s, "unit": "cell-updates/s",
+    e2e = {"value": e2e_cells / e2e_s, "unit": "cell-updates/s",
            "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
            "path": "gd_import(host, pinned) + gd_advance(1) + gd_export(host) per step"}
     sol.close()
