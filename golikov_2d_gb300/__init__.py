@@ -41,6 +41,7 @@ EXPORTS = (
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
+    "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
 )
 BATCH_PERSISTENT, BATCH_LOOPED = 0, 1
 
@@ -117,6 +118,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_launch_count.argtypes = [vp]
     L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
+    L.gd_adj_forward.argtypes = [vp, i, i, vp]
+    for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
+        getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.gd_batch_create.argtypes = [cfgp, i, ctypes.POINTER(vp)]
     L.gd_batch_destroy.argtypes = [vp]
     L.gd_batch_import.argtypes = [vp, i, vp, vp, vp, i, vp]
@@ -134,7 +138,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
-                 "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info"):
+                 "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
+                 "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -261,6 +266,25 @@ class Solver:
         if not (r == 3 and allow_nonfinite):
             _check(r, "gd_get_stats")
         return st
+
+    # -- differentiation (device tensors, reference AoS layout) --------------------------------
+    def adj_forward(self, nsteps: int, ckpt_every: int, stream=None) -> None:
+        _check(self.lib.gd_adj_forward(self.handle, int(nsteps), int(ckpt_every),
+                                       _stream_handle(stream)), "gd_adj_forward")
+
+    def _vec_call(self, fn, what, ins, outs, stream):
+        p = [t.data_ptr() for t in ins] + [t.data_ptr() for t in outs]
+        _check(fn(self.handle, *p, _stream_handle(stream)), what)
+
+    def adj_backward(self, gs, gu, gb, os_, ou, ob, stream=None) -> None:
+        self._vec_call(self.lib.gd_adj_backward, "gd_adj_backward", (gs, gu, gb), (os_, ou, ob),
+                       stream)
+
+    def tangent(self, vs, vu, vb, os_, ou, ob, stream=None) -> None:
+        self._vec_call(self.lib.gd_tangent, "gd_tangent", (vs, vu, vb), (os_, ou, ob), stream)
+
+    def adj_replay(self, s, u, b, os_, ou, ob, stream=None) -> None:
+        self._vec_call(self.lib.gd_adj_replay, "gd_adj_replay", (s, u, b), (os_, ou, ob), stream)
 
     def field_ptr(self, f: int) -> int:
         p = ctypes.c_void_p()

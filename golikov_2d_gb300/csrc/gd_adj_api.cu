@@ -1,0 +1,184 @@
+// gd_adj_api.cu -- C ABI of the differentiation entry points (include/gd2d.h):
+// gd_adj_forward, gd_adj_backward, gd_tangent, gd_adj_replay.
+//
+// Checkpointing: the forward run stores the state every `ckpt_every` steps and the dt of
+// every step.  The backward sweep walks the segments from last to first; each segment is
+// recomputed once from its checkpoint (storing each step's input state and the flux
+// differences / Powell term the update used), then stepped back in reverse.  Memory is
+// O(nsteps / every + every) states instead of O(nsteps).
+#include <cstring>
+#include <new>
+
+#include "../../include/gd2d.h"
+#include "gd_ctx.h"
+#include "gd_kernels.h"
+
+namespace gd {
+
+void adj_free(gd_ctx* ctx) {
+    AdjStore* a = ctx->adj;
+    if (!a) return;
+    cudaFree(a->dts);
+    cudaFree(a->ckpt);
+    cudaFree(a->seg);
+    cudaFree(a->aux);
+    cudaFree(a->lam);
+    cudaFree(a->scratch);
+    cudaFree(a->tbits);
+    delete a;
+    ctx->adj = nullptr;
+}
+
+}  // namespace gd
+
+namespace {
+
+#define GD_TRY(call)                                          \
+    do {                                                      \
+        if ((call) != cudaSuccess) return GD_ERR_CUDA;        \
+    } while (0)
+
+bool adj_supported(const gd_ctx* ctx) {
+    const gd_config& c = ctx->cfg;
+    for (int s = 0; s < 4; ++s)
+        if (c.bc[s] != GD_BC_PERIODIC) return false;
+    return c.physics == GD_MHD && c.method == GD_METHOD_HLLD && c.order == 2 &&
+           c.geometry == GD_CARTESIAN && c.mode == GD_MODE_FAST && c.frozen_radius == 0.0;
+}
+
+Planes planes_at(double* base, int nf, long long K) {
+    Planes p{};
+    for (int f = 0; f < nf; ++f) p.f[f] = base + (size_t)f * K;
+    return p;
+}
+
+CPlanes cplanes_at(const double* base, int nf, long long K) {
+    CPlanes p{};
+    for (int f = 0; f < nf; ++f) p.f[f] = base + (size_t)f * K;
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stream) {
+    if (!ctx || nsteps < 1 || ckpt_every < 1) return GD_ERR_INVALID_ARG;
+    if (!adj_supported(ctx)) return GD_ERR_UNSUPPORTED;
+    gd::adj_free(ctx);
+    gd::AdjStore* a = new (std::nothrow) gd::AdjStore();
+    if (!a) return GD_ERR_INVALID_ARG;
+    ctx->adj = a;
+    const long long K = ctx->K;
+    const int nf = ctx->nf;
+    const int every = ckpt_every < nsteps ? ckpt_every : nsteps;
+    a->nsteps = nsteps;
+    a->every = every;
+    a->nckpt = (nsteps + every - 1) / every;
+    const size_t state = sizeof(double) * (size_t)nf * K;
+    GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
+    GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
+    GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
+    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
+    GD_TRY(cudaMalloc(&a->lam, 2 * state));
+    GD_TRY(cudaMalloc(&a->scratch, sizeof(double) * 15 * (size_t)K));
+    GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
+    GD_TRY(gd::prepare_adjoint());
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int s = 0; s < nsteps; ++s) {
+        if (s % every == 0)
+            GD_TRY(cudaMemcpyAsync(a->ckpt + (size_t)(s / every) * nf * K, ctx->state[ctx->cur],
+                                   state, cudaMemcpyDeviceToDevice, st));
+        GD_TRY(cudaMemcpyAsync(a->dts + s, &ctx->sc->T_do, sizeof(double),
+                               cudaMemcpyDeviceToDevice, st));
+        const gd_status r = gd_advance(ctx, 1, 0, stream);
+        if (r != GD_OK) return r;
+    }
+    return GD_OK;
+}
+
+gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const double* gb,
+                          double* os, double* ou, double* ob, gd_stream stream) {
+    if (!ctx || !ctx->adj || !gs || !gu || !gb || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    gd::AdjStore* a = ctx->adj;
+    const long long K = ctx->K;
+    const int nf = ctx->nf;
+    const Params& P = ctx->P;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t state = sizeof(double) * (size_t)nf * K;
+    double* lam[2] = {a->lam, a->lam + (size_t)nf * K};
+    int c = 0;
+    GD_TRY(gd::launch_aos_to_soa(gs, gu, gb, planes_at(lam[0], nf, K), K, nf, st));
+    for (int sg = a->nckpt - 1; sg >= 0; --sg) {
+        const int k0 = sg * a->every;
+        const int k1 = k0 + a->every < a->nsteps ? k0 + a->every : a->nsteps;
+        const int len = k1 - k0;
+        // recompute the segment: input states and update terms of every step
+        GD_TRY(cudaMemcpyAsync(a->seg, a->ckpt + (size_t)sg * nf * K, state,
+                               cudaMemcpyDeviceToDevice, st));
+        for (int j = 0; j < len; ++j) {
+            GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
+                                           planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
+                                           a->dts + k0 + j, (unsigned long long*)a->tbits,
+                                           a->aux + (size_t)j * 8 * K, st));
+            ctx->launches += 1;
+        }
+        // reverse through the segment
+        for (int j = len - 1; j >= 0; --j) {
+            GD_TRY(gd::launch_adjoint_step(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
+                                           a->aux + (size_t)j * 8 * K, cplanes_at(lam[c], nf, K),
+                                           planes_at(lam[c ^ 1], nf, K), a->scratch,
+                                           a->dts + k0 + j, st));
+            ctx->launches += 2;
+            c ^= 1;
+        }
+    }
+    GD_TRY(gd::launch_soa_to_aos(cplanes_at(lam[c], nf, K), os, ou, ob, K, nf, st));
+    return GD_OK;
+}
+
+gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const double* vb,
+                     double* os, double* ou, double* ob, gd_stream stream) {
+    if (!ctx || !ctx->adj || !vs || !vu || !vb || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    gd::AdjStore* a = ctx->adj;
+    const long long K = ctx->K;
+    const int nf = ctx->nf;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t state = sizeof(double) * (size_t)nf * K;
+    double* t[2] = {a->lam, a->lam + (size_t)nf * K};
+    double* u[2] = {a->seg, a->seg + (size_t)nf * K};
+    GD_TRY(gd::launch_aos_to_soa(vs, vu, vb, planes_at(t[0], nf, K), K, nf, st));
+    GD_TRY(cudaMemcpyAsync(u[0], a->ckpt, state, cudaMemcpyDeviceToDevice, st));
+    int c = 0;
+    for (int k = 0; k < a->nsteps; ++k) {
+        GD_TRY(gd::launch_mhd_tangent(ctx->P, cplanes_at(u[c], nf, K), cplanes_at(t[c], nf, K),
+                                      planes_at(u[c ^ 1], nf, K), planes_at(t[c ^ 1], nf, K),
+                                      a->dts + k, st));
+        ctx->launches += 1;
+        c ^= 1;
+    }
+    GD_TRY(gd::launch_soa_to_aos(cplanes_at(t[c], nf, K), os, ou, ob, K, nf, st));
+    return GD_OK;
+}
+
+gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                        double* os, double* ou, double* ob, gd_stream stream) {
+    if (!ctx || !ctx->adj || !s || !u || !b || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    gd::AdjStore* a = ctx->adj;
+    const long long K = ctx->K;
+    const int nf = ctx->nf;
+    cudaStream_t st = (cudaStream_t)stream;
+    double* w[2] = {a->seg, a->seg + (size_t)nf * K};
+    GD_TRY(gd::launch_aos_to_soa(s, u, b, planes_at(w[0], nf, K), K, nf, st));
+    int c = 0;
+    for (int k = 0; k < a->nsteps; ++k) {
+        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(w[c], nf, K), planes_at(w[c ^ 1], nf, K),
+                                       a->dts + k, (unsigned long long*)a->tbits, nullptr, st));
+        ctx->launches += 1;
+        c ^= 1;
+    }
+    GD_TRY(gd::launch_soa_to_aos(cplanes_at(w[c], nf, K), os, ou, ob, K, nf, st));
+    return GD_OK;
+}
+
+}  // extern "C"

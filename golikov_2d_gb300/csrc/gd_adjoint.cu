@@ -1,0 +1,938 @@
+// gd_adjoint.cu -- hand-written discrete adjoint (reverse mode, VJP) of the fast MHD step.
+//
+// The step U' = S(U; dt) of gd_fast_mhd.cu (HLLD, minmod TVD, Powell source, Cartesian,
+// periodic) is differentiated with dt held fixed and every non-smooth choice (minmod
+// selection, wave-speed min/max, region selection, guards, floors) frozen at the branch
+// the forward values take.  Given lambda' = dL/dU', one reverse step returns
+// lambda = dL/dU = S'(U)^T lambda' in two passes:
+//
+//   A  per cell (adj_update_kernel): the transpose of the cell update.  Inputs: U, the
+//      forward flux differences d[7] and the Powell term divb of that cell (stored by the
+//      recompute pass), lambda'.  Outputs: the direct adjoint of the cell state, the adjoint
+//      of d[7] and of divb.
+//   B  per tile (adj_faces_kernel): every face touching the tile's stencil recomputes its
+//      forward states and HLLD flux and runs the flux's reverse sweep on
+//      Fbar = k (dbar_low - dbar_high); the adjoints of the two face states are gathered
+//      into the cells through the reconstruction (c +- slope/2, minmod choice, rho/p
+//      fallback) and the Powell central difference, in a fixed order (deterministic).
+//
+// All internal arithmetic is in Heaviside-Lorentz field units (b = B / sqrt(4 pi)), as in
+// the forward kernel; adjoints w.r.t. the stored Gaussian field are converted at the ends.
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+
+namespace gd {
+namespace {
+
+constexpr int NF = 7;
+constexpr int NT = 256;
+constexpr int ATX = 32, ATY = 8;
+
+// ---------------------------------------------------------------------------------------
+// Pass A: transpose of the cell update (Cartesian).
+// aux layout per cell: d[0..6] (slot order m, e, mx, my, bx, by, bz), divb.  Adjoint
+// scratch per cell: qbar[0..6] (field order rho, p, vx, vy, bx, by, bz, field in b units),
+// dbar[0..6] (slot order), divbbar.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, const double* aux,
+                                                        CPlanes lam_out, double* scratch) {
+    const long long K = (long long)P.N * P.M;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
+         k += (long long)gridDim.x * blockDim.x) {
+        const double r = U.f[0][k], p = U.f[1][k], u = U.f[2][k], v = U.f[3][k];
+        const double bx = U.f[4][k] * kInvSpi4, by = U.f[5][k] * kInvSpi4;
+        const double bz = U.f[6][k] * kInvSpi4;
+        double d[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) d[f] = aux[(size_t)f * K + k];
+        const double divb = aux[(size_t)7 * K + k];
+        // forward (same operations as the tile update)
+        const double ub = fma(u, bx, v * by);
+        const double bb = fma(bz, bz, fma(by, by, bx * bx));
+        const double E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(u, u, v * v), bb));
+        double r2 = r - d[0];
+        const bool rfl = le_zero(r2);
+        if (rfl) r2 = r;
+        const double mx2 = fma(r, u, -fma(bx, divb, d[2]));
+        const double my2 = fma(r, v, -fma(by, divb, d[3]));
+        const double bx2 = bx - fma(u, divb, d[4]);
+        const double by2 = by - fma(v, divb, d[5]);
+        const double bz2 = bz - d[6];
+        const double E2 = E - fma(ub, divb, d[1]);
+        const double inv = rcp_fast(r2);
+        const double u2 = mx2 * inv, v2 = my2 * inv;
+        const double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2),
+                                          fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+        const bool pfl = le_zero(p2);
+        // reverse
+        double r2b = lam_out.f[0][k], p2b = lam_out.f[1][k];
+        double u2b = lam_out.f[2][k], v2b = lam_out.f[3][k];
+        double bx2b = lam_out.f[4][k] * kSpi4, by2b = lam_out.f[5][k] * kSpi4;
+        double bz2b = lam_out.f[6][k] * kSpi4;
+        double E2b = 0.0;
+        if (!pfl) {
+            E2b = p2b * P.gm1;
+            const double Xb = -0.5 * p2b * P.gm1;
+            r2b += Xb * fma(u2, u2, v2 * v2);
+            u2b += Xb * 2.0 * r2 * u2;
+            v2b += Xb * 2.0 * r2 * v2;
+            bx2b += Xb * 2.0 * bx2;
+            by2b += Xb * 2.0 * by2;
+            bz2b += Xb * 2.0 * bz2;
+        }
+        const double mx2b = u2b * inv, my2b = v2b * inv;
+        const double invb = u2b * mx2 + v2b * my2;
+        r2b += -invb * inv * inv;
+        double rb = 0.0, pb = 0.0, ub_ = 0.0, vb = 0.0, bxb = 0.0, byb = 0.0, bzb = 0.0;
+        double db[NF] = {0, 0, 0, 0, 0, 0, 0};
+        double divbb = 0.0, Eb = 0.0, ubb = 0.0;
+        rb += r2b;
+        if (!rfl) db[0] -= r2b;
+        Eb += E2b;
+        ubb -= E2b * divb;
+        divbb -= E2b * ub;
+        db[1] -= E2b;
+        bzb += bz2b;
+        db[6] -= bz2b;
+        byb += by2b;
+        vb -= by2b * divb;
+        divbb -= by2b * v;
+        db[5] -= by2b;
+        bxb += bx2b;
+        ub_ -= bx2b * divb;
+        divbb -= bx2b * u;
+        db[4] -= bx2b;
+        rb += my2b * v;
+        vb += my2b * r;
+        byb -= my2b * divb;
+        divbb -= my2b * by;
+        db[3] -= my2b;
+        rb += mx2b * u;
+        ub_ += mx2b * r;
+        bxb -= mx2b * divb;
+        divbb -= mx2b * bx;
+        db[2] -= mx2b;
+        pb += Eb * P.inv_gm1;
+        rb += 0.5 * Eb * fma(u, u, v * v);
+        ub_ += Eb * r * u;
+        vb += Eb * r * v;
+        const double bbb = 0.5 * Eb;
+        bxb += 2.0 * bbb * bx + ubb * u;
+        byb += 2.0 * bbb * by + ubb * v;
+        bzb += 2.0 * bbb * bz;
+        ub_ += ubb * bx;
+        vb += ubb * by;
+        double* s = scratch;
+        s[0 * K + k] = rb;
+        s[1 * K + k] = pb;
+        s[2 * K + k] = ub_;
+        s[3 * K + k] = vb;
+        s[4 * K + k] = bxb;
+        s[5 * K + k] = byb;
+        s[6 * K + k] = bzb;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) s[(size_t)(7 + f) * K + k] = db[f];
+        s[(size_t)14 * K + k] = divbb;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Reverse sweep of one HLLD face flux (method 3) in the local frame.
+// Inputs: the two face states A (low) and B (high) as (r, p, un, ut, bn, bt, bz) and the
+// adjoint of the flux (m, mn, mt, e, bn, bt, bz).  Adds the adjoints of A and B to Ab, Bb.
+// The forward part repeats hlld_local<double> of gd_fast_mhd.cu operation for operation.
+// ---------------------------------------------------------------------------------------
+struct SideV {
+    double r, p, un, ut, bn, bt, bz;
+    double bn2, bb, pT, kin, E, gp, a, disc, sq, X, rs, cf;
+    double F0, F1, F2, F4, F6, F7;
+    bool disc0;
+};
+
+__device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params& P) {
+    S.r = q[0]; S.p = q[1]; S.un = q[2]; S.ut = q[3]; S.bn = q[4]; S.bt = q[5]; S.bz = q[6];
+    S.bn2 = S.bn * S.bn;
+    S.bb = fma(S.bz, S.bz, fma(S.bt, S.bt, S.bn2));
+    S.pT = fma(0.5, S.bb, S.p);
+    S.kin = fma(S.r, fma(S.un, S.un, S.ut * S.ut), S.bb);
+    S.E = fma(S.p, P.inv_gm1, 0.5 * S.kin);
+    S.gp = P.gamma * S.p;
+    S.a = S.gp + S.bb;
+    double disc = fma(S.a, S.a, -4.0 * S.gp * S.bn2);
+    S.disc0 = le_zero(disc);
+    S.disc = S.disc0 ? 0.0 : disc;
+    S.sq = sqrt_fast(S.disc);
+    S.X = 0.5 * (S.a + S.sq);
+    S.rs = rsqrt_fast(S.X * S.r);
+    S.cf = S.X * S.rs;
+    S.F0 = S.r * S.un;
+    S.F1 = fma(S.F0, S.un, S.pT - S.bn2);
+    S.F2 = fma(S.F0, S.ut, -S.bn * S.bt);
+    S.F4 = fma(S.E + S.pT, S.un, -S.bn * fma(S.ut, S.bt, S.un * S.bn));
+    S.F6 = fma(S.un, S.bt, -S.ut * S.bn);
+    S.F7 = S.un * S.bz;
+}
+
+// adjoints of the side's derived quantities -> adjoints of its inputs (qb[7], added)
+struct SideB {
+    double r, p, un, ut, bn, bt, bz, pT, E, cf, F0, F1, F2, F4, F6, F7;
+};
+
+__device__ __forceinline__ void side_rev(const SideV& S, SideB& b, const Params& P, double* qb) {
+    // F7 = un bz
+    b.un += b.F7 * S.bz;
+    b.bz += b.F7 * S.un;
+    // F6 = un bt - ut bn
+    b.un += b.F6 * S.bt;
+    b.bt += b.F6 * S.un;
+    b.ut -= b.F6 * S.bn;
+    b.bn -= b.F6 * S.ut;
+    // F4 = (E + pT) un - bn (ut bt + un bn)
+    {
+        const double w = fma(S.ut, S.bt, S.un * S.bn);
+        b.E += b.F4 * S.un;
+        b.pT += b.F4 * S.un;
+        b.un += b.F4 * (S.E + S.pT);
+        b.bn -= b.F4 * w;
+        const double wb = -b.F4 * S.bn;
+        b.ut += wb * S.bt;
+        b.bt += wb * S.ut;
+        b.un += wb * S.bn;
+        b.bn += wb * S.un;
+    }
+    // F2 = F0 ut - bn bt
+    b.F0 += b.F2 * S.ut;
+    b.ut += b.F2 * S.F0;
+    b.bn -= b.F2 * S.bt;
+    b.bt -= b.F2 * S.bn;
+    // F1 = F0 un + pT - bn^2
+    b.F0 += b.F1 * S.un;
+    b.un += b.F1 * S.F0;
+    b.pT += b.F1;
+    b.bn -= 2.0 * b.F1 * S.bn;
+    // F0 = r un
+    b.r += b.F0 * S.un;
+    b.un += b.F0 * S.r;
+    // cf = X * rsqrt(X r) = sqrt(X / r)
+    double Xb = 0.0, rb_cf = 0.0;
+    {
+        // d cf / dX = 0.5 / sqrt(X r) = 0.5 rs; d cf / dr = -0.5 cf / r = -0.5 X rs / r
+        Xb += b.cf * 0.5 * S.rs;
+        rb_cf = -b.cf * 0.5 * S.cf * rcp_fast(S.r);
+    }
+    b.r += rb_cf;
+    // X = 0.5 (a + sq)
+    double ab = 0.5 * Xb, sqb = 0.5 * Xb;
+    // sq = sqrt(disc), disc = a^2 - 4 gp bn^2 (clamped at 0)
+    double gpb = 0.0, bn2b = 0.0;
+    if (!S.disc0 && S.sq > 0.0) {
+        const double discb = sqb * 0.5 / S.sq;
+        ab += discb * 2.0 * S.a;
+        gpb -= discb * 4.0 * S.bn2;
+        bn2b -= discb * 4.0 * S.gp;
+    }
+    // a = gp + bb ; gp = gamma p
+    gpb += ab;
+    double bbb = ab;
+    b.p += gpb * P.gamma;
+    // E = p inv_gm1 + 0.5 kin ; kin = r (un^2 + ut^2) + bb
+    b.p += b.E * P.inv_gm1;
+    const double kinb = 0.5 * b.E;
+    b.r += kinb * fma(S.un, S.un, S.ut * S.ut);
+    b.un += kinb * 2.0 * S.r * S.un;
+    b.ut += kinb * 2.0 * S.r * S.ut;
+    bbb += kinb;
+    // pT = 0.5 bb + p
+    bbb += 0.5 * b.pT;
+    b.p += b.pT;
+    // bb = bz^2 + bt^2 + bn2 ; bn2 = bn^2
+    b.bz += 2.0 * bbb * S.bz;
+    b.bt += 2.0 * bbb * S.bt;
+    bn2b += bbb;
+    b.bn += 2.0 * bn2b * S.bn;
+    qb[0] += b.r;
+    qb[1] += b.p;
+    qb[2] += b.un;
+    qb[3] += b.ut;
+    qb[4] += b.bn;
+    qb[5] += b.bt;
+    qb[6] += b.bz;
+}
+
+__device__ __forceinline__ double isel(double v, int idbn) {
+    return idbn == 0 ? 0.0 : (idbn < 0 ? -v : v);
+}
+
+// Fb = (m, mn, mt, e, bn, bt, bz); qa_b, qb_b accumulate (r, p, un, ut, bn, bt, bz).
+__device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
+                         const Params& P, double* qa_b, double* qb_b) {
+    SideV A, B;
+    side_fwd(A, qa, P);
+    side_fwd(B, qb, P);
+    // ---- forward, shared part
+    const bool minA = !dlt(B.un, A.un);              // uminN = A.un (else B.un)
+    const bool maxB = dlt(A.un, B.un);               // umaxN = B.un (else A.un)
+    const double uminN = minA ? A.un : B.un;
+    const double umaxN = maxB ? B.un : A.un;
+    const bool cfB = abs_bits(A.cf) < abs_bits(B.cf);
+    const double cmax = cfB ? B.cf : A.cf;
+    const double SL = uminN - cmax, SR = umaxN + cmax;
+    const double suL = SL - A.un, suR = SR - B.un;
+    const double mL = A.r * suL, mR = B.r * suR;
+    const double iden = rcp_fast(mR - mL);
+    const double SMn = (fma(mR, B.un, -mL * A.un) - B.pT) + A.pT;
+    const double SM = SMn * iden;
+    const double PTTn = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT));
+    const double PTT = PTTn * iden;
+    const bool UUR = abs_bits(SL) < abs_bits(SR);
+    const double UU = UUR ? dabs(SR) : dabs(SL);
+    const double iS = rcp_fast(SR - SL);
+    const double bnn = fma(SR, B.bn, -SL * A.bn);
+    const double btn = fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6);
+    const double bzn = fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7);
+    const double bn = bnn * iS, bt = btn * iS, bz = bzn * iS;
+    const double iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
+    const double rLL = mL * iL, rRR = mR * iR;
+    const double bbn = bn * bn;
+    // star states
+    const double ttL = fma(mL, SL - SM, -bbn);
+    const bool gL = abs_bits(ttL) >= 0x3EE4F8B588E368F1ULL;
+    double itL = 0, cL = 0, dL = 0, vLL, wLL, btL, bzL;
+    if (gL) {
+        itL = rcp_fast(ttL);
+        cL = bn * (SM - A.un) * itL;
+        dL = fma(mL, suL, -bbn) * itL;
+        vLL = fma(-cL, A.bt, A.ut);
+        wLL = -cL * A.bz;
+        btL = A.bt * dL;
+        bzL = A.bz * dL;
+    } else {
+        vLL = A.ut; wLL = 0.0; btL = 0.0; bzL = 0.0;
+    }
+    const double ttR = fma(mR, SR - SM, -bbn);
+    const bool gR = abs_bits(ttR) >= 0x3EE4F8B588E368F1ULL;
+    double itR = 0, cR = 0, dR = 0, vRR, wRR, btR, bzR;
+    if (gR) {
+        itR = rcp_fast(ttR);
+        cR = bn * (SM - B.un) * itR;
+        dR = fma(mR, suR, -bbn) * itR;
+        vRR = fma(-cR, B.bt, B.ut);
+        wRR = -cR * B.bz;
+        btR = B.bt * dR;
+        bzR = B.bz * dR;
+    } else {
+        vRR = B.ut; wRR = 0.0; btR = 0.0; bzR = 0.0;
+    }
+    const double SMbn = SM * bn;
+    const double sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
+    const double sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
+    const double wA = fma(A.un, A.bn, A.ut * A.bt), wB = fma(B.un, B.bn, B.ut * B.bt);
+    const double eLLn = fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) + bn * (wA - sbLL);
+    const double eRRn = fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) + bn * (wB - sbRR);
+    const double eLL = eLLn * iL, eRR = eRRn * iR;
+    const double isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
+    const double sLL = rLL * isLL, sRR = rRR * isRR;
+    const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
+    const double abn = dabs(bn);
+    const double sgn_bn = gt_zero(bn) ? 1.0 : -1.0;
+    const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
+    const double SRR = bnz ? fma(abn, isRR, SM) : SM;
+    const int idbn = bnz ? (gt_zero(bn) ? 1 : -1) : 0;
+    const bool takeL = ge_zero(SL) || ge_zero(SM);
+    int level;
+    if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
+    else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
+    const SideV& Kf = takeL ? A : B;
+    const double S = takeL ? SL : SR;
+    const double rK = takeL ? rLL : rRR;
+    const double vK = takeL ? vLL : vRR;
+    const double eK = takeL ? eLL : eRR;
+    const double btK = takeL ? btL : btR;
+    const double bzK = takeL ? bzL : bzR;
+    // double-star (only needed for level 2)
+    double is = 0, vL3 = 0, wL3 = 0, s2 = 0, bt3 = 0, bz3 = 0, sb3 = 0, sK = 0, e3 = 0, S2 = 0;
+    if (level == 2) {
+        is = rcp_fast(sLL + sRR);
+        vL3 = (fma(sLL, vLL, sRR * vRR) + isel(btR - btL, idbn)) * is;
+        wL3 = (fma(sLL, wLL, sRR * wRR) + isel(bzR - bzL, idbn)) * is;
+        s2 = isel(sLL * sRR, idbn);
+        bt3 = fma(s2, vRR - vLL, fma(sLL, btR, sRR * btL)) * is;
+        bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
+        sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
+        sK = takeL ? -sLL : sRR;
+        e3 = fma(isel(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
+        S2 = takeL ? SLL : SRR;
+    }
+
+    // ---- reverse ------------------------------------------------------------------------
+    SideB Ab = {}, Bb = {};
+    SideB& Kb = takeL ? Ab : Bb;
+    // adjoints of intermediates
+    double SLb = 0, SRb = 0, SMb = 0, PTTb = 0, UUb = 0, bnb = 0, btb = 0, bzb = 0;
+    double rLLb = 0, rRRb = 0, iLb = 0, iRb = 0;
+    double vLLb = 0, wLLb = 0, btLb = 0, bzLb = 0, vRRb = 0, wRRb = 0, btRb = 0, bzRb = 0;
+    double eLLb = 0, eRRb = 0, sLLb = 0, sRRb = 0, SLLb = 0, SRRb = 0, SMbnb = 0;
+    double sbLLb = 0, sbRRb = 0;
+    const double Fm = Fb[0], Fmn = Fb[1], Fmt = Fb[2], Fe = Fb[3], Fbn = Fb[4], Fbt = Fb[5],
+                 Fbz = Fb[6];
+    // F.bn = -UU (B.bn - A.bn)
+    UUb -= Fbn * (B.bn - A.bn);
+    Bb.bn -= Fbn * UU;
+    Ab.bn += Fbn * UU;
+    // base fluxes of side K
+    Kb.F0 += Fm;
+    Kb.F1 += Fmn;
+    Kb.F2 += Fmt;
+    Kb.F4 += Fe;
+    Kb.F6 += Fbt;
+    Kb.F7 += Fbz;
+    double Sb = 0, rKb = 0, vKb = 0, eKb = 0, btKb = 0, bzKb = 0;
+    if (level >= 1) {
+        if (level == 2) {
+            // F.mt += S2 rK (vL3 - vK); F.e += S2 (e3 - eK); F.bt += S2 (bt3 - btK);
+            // F.bz += S2 (bz3 - bzK)
+            const double S2b = Fmt * rK * (vL3 - vK) + Fe * (e3 - eK) + Fbt * (bt3 - btK) +
+                               Fbz * (bz3 - bzK);
+            rKb += Fmt * S2 * (vL3 - vK);
+            double vL3b = Fmt * S2 * rK;
+            vKb -= Fmt * S2 * rK;
+            double e3b = Fe * S2;
+            eKb -= Fe * S2;
+            double bt3b = Fbt * S2;
+            btKb -= Fbt * S2;
+            double bz3b = Fbz * S2;
+            bzKb -= Fbz * S2;
+            if (takeL) SLLb += S2b; else SRRb += S2b;
+            // e3 = eK + isel(sK) (sbK - sb3)
+            eKb += e3b;
+            const double sKv = isel(sK, idbn);
+            const double sbK = takeL ? sbLL : sbRR;
+            const double sKvb = e3b * (sbK - sb3);
+            if (takeL) sbLLb += e3b * sKv; else sbRRb += e3b * sKv;
+            double sb3b = -e3b * sKv;
+            const double sKb = isel(sKvb, idbn);
+            if (takeL) sLLb -= sKb; else sRRb += sKb;
+            // sb3 = wL3 bz3 + vL3 bt3 + SMbn
+            double wL3b = sb3b * bz3;
+            bz3b += sb3b * wL3;
+            vL3b += sb3b * bt3;
+            bt3b += sb3b * vL3;
+            SMbnb += sb3b;
+            // bz3 = (s2 (wRR - wLL) + sLL bzR + sRR bzL) is
+            double isb = bz3b * (bz3 * (sLL + sRR));  // bz3 / is = numerator
+            {
+                const double nb = bz3b * is;
+                double s2b = nb * (wRR - wLL);
+                wRRb += nb * s2;
+                wLLb -= nb * s2;
+                sLLb += nb * bzR;
+                bzRb += nb * sLL;
+                sRRb += nb * bzL;
+                bzLb += nb * sRR;
+                // bt3 = (s2 (vRR - vLL) + sLL btR + sRR btL) is
+                isb += bt3b * (bt3 * (sLL + sRR));
+                const double mb = bt3b * is;
+                s2b += mb * (vRR - vLL);
+                vRRb += mb * s2;
+                vLLb -= mb * s2;
+                sLLb += mb * btR;
+                btRb += mb * sLL;
+                sRRb += mb * btL;
+                btLb += mb * sRR;
+                // s2 = isel(sLL sRR)
+                const double pb = isel(s2b, idbn);
+                sLLb += pb * sRR;
+                sRRb += pb * sLL;
+            }
+            // wL3 = (sLL wLL + sRR wRR + isel(bzR - bzL)) is
+            {
+                isb += wL3b * (wL3 * (sLL + sRR));
+                const double nb = wL3b * is;
+                sLLb += nb * wLL;
+                wLLb += nb * sLL;
+                sRRb += nb * wRR;
+                wRRb += nb * sRR;
+                const double tb = isel(nb, idbn);
+                bzRb += tb;
+                bzLb -= tb;
+            }
+            // vL3 = (sLL vLL + sRR vRR + isel(btR - btL)) is
+            {
+                isb += vL3b * (vL3 * (sLL + sRR));
+                const double nb = vL3b * is;
+                sLLb += nb * vLL;
+                vLLb += nb * sLL;
+                sRRb += nb * vRR;
+                vRRb += nb * sRR;
+                const double tb = isel(nb, idbn);
+                btRb += tb;
+                btLb -= tb;
+            }
+            // is = 1 / (sLL + sRR)
+            const double db = -isb * is * is;
+            sLLb += db;
+            sRRb += db;
+        }
+        // level-1 terms: F.m += S (rK - K.r); F.mn += S (rK SM - K.r K.un);
+        // F.mt += S (rK vK - K.r K.ut); F.e += S (eK - K.E); F.bt += S (btK - K.bt);
+        // F.bz += S (bzK - K.bz)
+        Sb += Fm * (rK - Kf.r) + Fmn * fma(rK, SM, -Kf.r * Kf.un) +
+              Fmt * fma(rK, vK, -Kf.r * Kf.ut) + Fe * (eK - Kf.E) + Fbt * (btK - Kf.bt) +
+              Fbz * (bzK - Kf.bz);
+        rKb += S * (Fm + Fmn * SM + Fmt * vK);
+        SMb += S * Fmn * rK;
+        vKb += S * Fmt * rK;
+        eKb += S * Fe;
+        btKb += S * Fbt;
+        bzKb += S * Fbz;
+        Kb.r -= S * (Fm + Fmn * Kf.un + Fmt * Kf.ut);
+        Kb.un -= S * Fmn * Kf.r;
+        Kb.ut -= S * Fmt * Kf.r;
+        Kb.E -= S * Fe;
+        Kb.bt -= S * Fbt;
+        Kb.bz -= S * Fbz;
+    }
+    // distribute the K-selected adjoints
+    if (takeL) {
+        SLb += Sb; rLLb += rKb; vLLb += vKb; eLLb += eKb; btLb += btKb; bzLb += bzKb;
+    } else {
+        SRb += Sb; rRRb += rKb; vRRb += vKb; eRRb += eKb; btRb += btKb; bzRb += bzKb;
+    }
+    // SLL = SM - abn isLL ; SRR = SM + abn isRR  (if bnz, else = SM)
+    double isLLb = 0, isRRb = 0, abnb = 0;
+    if (bnz) {
+        SMb += SLLb + SRRb;
+        abnb += -SLLb * isLL + SRRb * isRR;
+        isLLb += -SLLb * abn;
+        isRRb += SRRb * abn;
+    } else {
+        SMb += SLLb + SRRb;
+    }
+    bnb += abnb * sgn_bn;
+    // sLL = rLL isLL, isLL = rsqrt(rLL)  =>  d sLL / d rLL = 0.5 isLL
+    rLLb += sLLb * 0.5 * isLL;
+    rRRb += sRRb * 0.5 * isRR;
+    rLLb += isLLb * (-0.5) * isLL * isLL * isLL;
+    rRRb += isRRb * (-0.5) * isRR * isRR * isRR;
+    // eLL = eLLn iL
+    iLb += eLLb * eLLn;
+    iRb += eRRb * eRRn;
+    {
+        const double nb = eLLb * iL;  // eLLn = A.E suL + PTT SM - A.pT A.un + bn (wA - sbLL)
+        Ab.E += nb * suL;
+        double suLb_e = nb * A.E;
+        PTTb += nb * SM;
+        SMb += nb * PTT;
+        Ab.pT -= nb * A.un;
+        Ab.un -= nb * A.pT;
+        bnb += nb * (wA - sbLL);
+        const double wAb = nb * bn;
+        sbLLb -= nb * bn;
+        Ab.un += wAb * A.bn;
+        Ab.bn += wAb * A.un;
+        Ab.ut += wAb * A.bt;
+        Ab.bt += wAb * A.ut;
+        // suL adjoint accumulated below
+        SLb += suLb_e;
+        Ab.un -= suLb_e;
+    }
+    {
+        const double nb = eRRb * iR;
+        Bb.E += nb * suR;
+        const double suRb_e = nb * B.E;
+        PTTb += nb * SM;
+        SMb += nb * PTT;
+        Bb.pT -= nb * B.un;
+        Bb.un -= nb * B.pT;
+        bnb += nb * (wB - sbRR);
+        const double wBb = nb * bn;
+        sbRRb -= nb * bn;
+        Bb.un += wBb * B.bn;
+        Bb.bn += wBb * B.un;
+        Bb.ut += wBb * B.bt;
+        Bb.bt += wBb * B.ut;
+        SRb += suRb_e;
+        Bb.un -= suRb_e;
+    }
+    // sbLL = wLL bzL + vLL btL + SMbn
+    wLLb += sbLLb * bzL;
+    bzLb += sbLLb * wLL;
+    vLLb += sbLLb * btL;
+    btLb += sbLLb * vLL;
+    SMbnb += sbLLb;
+    wRRb += sbRRb * bzR;
+    bzRb += sbRRb * wRR;
+    vRRb += sbRRb * btR;
+    btRb += sbRRb * vRR;
+    SMbnb += sbRRb;
+    // SMbn = SM bn
+    SMb += SMbnb * bn;
+    bnb += SMbnb * SM;
+    // star states L
+    double bbnb = 0;
+    if (gL) {
+        // vLL = A.ut - cL A.bt ; wLL = -cL A.bz ; btL = A.bt dL ; bzL = A.bz dL
+        Ab.ut += vLLb;
+        double cLb = -vLLb * A.bt - wLLb * A.bz;
+        Ab.bt += -vLLb * cL + btLb * dL;
+        Ab.bz += -wLLb * cL + bzLb * dL;
+        const double dLb = btLb * A.bt + bzLb * A.bz;
+        // dL = (mL suL - bbn) itL ; cL = bn (SM - A.un) itL
+        const double itLb = dLb * fma(mL, suL, -bbn) + cLb * bn * (SM - A.un);
+        const double dnb = dLb * itL;
+        double mLb_s = dnb * suL;
+        double suLb_s = dnb * mL;
+        bbnb -= dnb;
+        const double cnb = cLb * itL;
+        bnb += cnb * (SM - A.un);
+        SMb += cnb * bn;
+        Ab.un -= cnb * bn;
+        // itL = 1 / ttL ; ttL = mL (SL - SM) - bbn
+        const double ttLb = -itLb * itL * itL;
+        mLb_s += ttLb * (SL - SM);
+        SLb += ttLb * mL;
+        SMb -= ttLb * mL;
+        bbnb -= ttLb;
+        // mL and suL adjoints
+        Ab.r += mLb_s * suL;
+        suLb_s += mLb_s * A.r;
+        SLb += suLb_s;
+        Ab.un -= suLb_s;
+    } else {
+        Ab.ut += vLLb;
+    }
+    if (gR) {
+        Bb.ut += vRRb;
+        double cRb = -vRRb * B.bt - wRRb * B.bz;
+        Bb.bt += -vRRb * cR + btRb * dR;
+        Bb.bz += -wRRb * cR + bzRb * dR;
+        const double dRb = btRb * B.bt + bzRb * B.bz;
+        const double itRb = dRb * fma(mR, suR, -bbn) + cRb * bn * (SM - B.un);
+        const double dnb = dRb * itR;
+        double mRb_s = dnb * suR;
+        double suRb_s = dnb * mR;
+        bbnb -= dnb;
+        const double cnb = cRb * itR;
+        bnb += cnb * (SM - B.un);
+        SMb += cnb * bn;
+        Bb.un -= cnb * bn;
+        const double ttRb = -itRb * itR * itR;
+        mRb_s += ttRb * (SR - SM);
+        SRb += ttRb * mR;
+        SMb -= ttRb * mR;
+        bbnb -= ttRb;
+        Bb.r += mRb_s * suR;
+        suRb_s += mRb_s * B.r;
+        SRb += suRb_s;
+        Bb.un -= suRb_s;
+    } else {
+        Bb.ut += vRRb;
+    }
+    // bbn = bn^2
+    bnb += 2.0 * bbnb * bn;
+    // rLL = mL iL ; rRR = mR iR ; iL = 1 / (SL - SM) ; iR = 1 / (SR - SM)
+    double mLb = rLLb * iL, mRb = rRRb * iR;
+    iLb += rLLb * mL;
+    iRb += rRRb * mR;
+    {
+        const double dLb = -iLb * iL * iL;
+        SLb += dLb;
+        SMb -= dLb;
+        const double dRb = -iRb * iR * iR;
+        SRb += dRb;
+        SMb -= dRb;
+    }
+    // bn = bnn iS, bt = btn iS, bz = bzn iS
+    double iSb = bnb * bnn + btb * btn + bzb * bzn;
+    {
+        const double nb = bnb * iS;  // bnn = SR B.bn - SL A.bn
+        SRb += nb * B.bn;
+        Bb.bn += nb * SR;
+        SLb -= nb * A.bn;
+        Ab.bn -= nb * SL;
+    }
+    // (bt, bz are not used by HLLD beyond the HLLC-MHD branch: btb = bzb = 0 here)
+    // iS = 1 / (SR - SL)
+    {
+        const double db = -iSb * iS * iS;
+        SRb += db;
+        SLb -= db;
+    }
+    // UU = max(|SL|, |SR|)
+    if (UUR) SRb += UUb * (lt_zero(SR) ? -1.0 : 1.0);
+    else SLb += UUb * (lt_zero(SL) ? -1.0 : 1.0);
+    // PTT = PTTn iden ; SM = SMn iden
+    double idenb = PTTb * PTTn + SMb * SMn;
+    {
+        const double nb = PTTb * iden;  // PTTn = mL mR (B.un - A.un) + mR A.pT - mL B.pT
+        mLb += nb * (mR * (B.un - A.un) - B.pT);
+        mRb += nb * (mL * (B.un - A.un) + A.pT);
+        Bb.un += nb * mL * mR;
+        Ab.un -= nb * mL * mR;
+        Ab.pT += nb * mR;
+        Bb.pT -= nb * mL;
+    }
+    {
+        const double nb = SMb * iden;  // SMn = mR B.un - mL A.un - B.pT + A.pT
+        mRb += nb * B.un;
+        Bb.un += nb * mR;
+        mLb -= nb * A.un;
+        Ab.un -= nb * mL;
+        Bb.pT -= nb;
+        Ab.pT += nb;
+    }
+    // iden = 1 / (mR - mL)
+    {
+        const double db = -idenb * iden * iden;
+        mRb += db;
+        mLb -= db;
+    }
+    // mL = A.r suL, mR = B.r suR ; suL = SL - A.un ; suR = SR - B.un
+    Ab.r += mLb * suL;
+    double suLb = mLb * A.r;
+    Bb.r += mRb * suR;
+    double suRb = mRb * B.r;
+    SLb += suLb;
+    Ab.un -= suLb;
+    SRb += suRb;
+    Bb.un -= suRb;
+    // SL = uminN - cmax ; SR = umaxN + cmax
+    double cmaxb = -SLb + SRb;
+    if (minA) Ab.un += SLb; else Bb.un += SLb;
+    if (maxB) Bb.un += SRb; else Ab.un += SRb;
+    if (cfB) Bb.cf += cmaxb; else Ab.cf += cmaxb;
+    side_rev(A, Ab, P, qa_b);
+    side_rev(B, Bb, P, qb_b);
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass B: face adjoints and the gather into cells.
+// ---------------------------------------------------------------------------------------
+constexpr int HU = 3;  // halo of the state tile (cells needed by the slopes of halo faces)
+constexpr int HD = 2;  // halo of the dbar tile
+constexpr int USX = ATX + 2 * HU, USY = ATY + 2 * HU;
+constexpr int DSX = ATX + 2 * HD, DSY = ATY + 2 * HD;
+constexpr int NXF = ATX + 3;  // x-faces per row: between cells x0-2 | x0-1 ... x0+TX | x0+TX+1
+constexpr int NYF = ATY + 3;
+
+struct AdjSmem {
+    double U[NF][USY][USX];       // state (b units), cross-shaped halo 3
+    double Db[NF][DSY][DSX];      // dbar, cross-shaped halo 2
+    double qax[NF][ATY][NXF];     // adjoint of the low-side face state, x-faces
+    double qbx[NF][ATY][NXF];     // adjoint of the high-side face state, x-faces
+    double qay[NF][NYF][ATX];
+    double qby[NF][NYF][ATX];
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// minmod slope and which difference it took: +1 right (c_{+1} - c), -1 left (c - c_{-1}), 0
+__device__ __forceinline__ double slope_sel(double cm, double c, double cp, int& sel) {
+    const double l = c - cm, r = cp - c;
+    const double s = minmod(l, r);
+    sel = (bits(s) << 1) == 0 ? 0 : ((abs_bits(l) <= abs_bits(r)) ? -1 : 1);
+    return s;
+}
+
+__global__ void __launch_bounds__(NT) adj_faces_kernel(Params P, CPlanes U, const double* scratch,
+                                                       Planes lam_in,
+                                                       const double* __restrict__ T_do_ptr) {
+    extern __shared__ __align__(16) double smem_raw[];
+    AdjSmem& sm = *reinterpret_cast<AdjSmem*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int N = P.N, M = P.M;
+    const long long K = (long long)N * M;
+    const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
+    const double T_do = *T_do_ptr;
+    const double kx = T_do / P.dx, ky = T_do / P.dy;
+
+    // ---- load U (cross halo HU) and dbar (cross halo HD), periodic wrap ---------------------
+    for (int i = tid; i < USY * USX; i += NT) {
+        const int ly = i / USX, lx = i - ly * USX;
+        const bool xh = lx < HU || lx >= ATX + HU, yh = ly < HU || ly >= ATY + HU;
+        if (xh && yh) continue;
+        const int gx = wrap(x0 + lx - HU, N), gy = wrap(y0 + ly - HU, M);
+        const long long k = (long long)gy * N + gx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) sm.U[f][ly][lx] = U.f[f][k] * (f >= 4 ? kInvSpi4 : 1.0);
+    }
+    for (int i = tid; i < DSY * DSX; i += NT) {
+        const int ly = i / DSX, lx = i - ly * DSX;
+        const bool xh = lx < HD || lx >= ATX + HD, yh = ly < HD || ly >= ATY + HD;
+        if (xh && yh) continue;
+        const int gx = wrap(x0 + lx - HD, N), gy = wrap(y0 + ly - HD, M);
+        const long long k = (long long)gy * N + gx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) sm.Db[f][ly][lx] = scratch[(size_t)(7 + f) * K + k];
+    }
+    __syncthreads();
+
+    // ---- faces: recompute states and flux, reverse sweep ------------------------------------
+    for (int i = tid; i < NXF * ATY + NYF * ATX; i += NT) {
+        const bool isx = i < NXF * ATY;
+        int a, row;  // a: face index along the normal (face between a-1 and a, tile-local)
+        if (isx) {
+            row = i / NXF;
+            a = i - row * NXF - 1;  // x-face index in [-1, ATX+1]
+        } else {
+            const int j = i - NXF * ATY;
+            row = j / NYF;          // here: column
+            a = j - row * NYF - 1;
+        }
+        // cell values along the normal at positions a-2 .. a+1: the face's low cell a-1 and
+        // high cell a, each with the neighbour its slope needs
+        double c[4][NF];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int pos = a - 2 + t;  // tile-local cell index along the normal, >= -3
+#pragma unroll
+            for (int f = 0; f < NF; ++f)
+                c[t][f] = isx ? sm.U[f][row + HU][pos + HU] : sm.U[f][pos + HU][row + HU];
+        }
+        // face states: low cell = pos a-1 (t=1), high cell = pos a (t=2)
+        double qa[NF], qb[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            int sa, sb_;
+            const double da = slope_sel(c[0][f], c[1][f], c[2][f], sa);
+            const double db = slope_sel(c[1][f], c[2][f], c[3][f], sb_);
+            const double va = fma(0.5, da, c[1][f]), vb = fma(-0.5, db, c[2][f]);
+            qa[f] = (f < 2 && le_zero(va)) ? c[1][f] : va;
+            qb[f] = (f < 2 && le_zero(vb)) ? c[2][f] : vb;
+        }
+        // flux adjoint: d_low += k F, d_high -= k F
+        const double kk = isx ? kx : ky;
+        double Fslot[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const double dlo = isx ? sm.Db[f][row + HD][a - 1 + HD] : sm.Db[f][a - 1 + HD][row + HD];
+            const double dhi = isx ? sm.Db[f][row + HD][a + HD] : sm.Db[f][a + HD][row + HD];
+            Fslot[f] = kk * (dlo - dhi);
+        }
+        // slots: 0 m, 1 e, 2 mx, 3 my, 4 bx, 5 by, 6 bz -> local (m, mn, mt, e, bn, bt, bz)
+        const double Fb[7] = {Fslot[0], isx ? Fslot[2] : Fslot[3], isx ? Fslot[3] : Fslot[2],
+                              Fslot[1], isx ? Fslot[4] : Fslot[5], isx ? Fslot[5] : Fslot[4],
+                              Fslot[6]};
+        const double la[7] = {qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
+                              isx ? qa[4] : qa[5], isx ? qa[5] : qa[4], qa[6]};
+        const double lb[7] = {qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2],
+                              isx ? qb[4] : qb[5], isx ? qb[5] : qb[4], qb[6]};
+        double lab[7] = {0, 0, 0, 0, 0, 0, 0}, lbb[7] = {0, 0, 0, 0, 0, 0, 0};
+        hlld_vjp(la, lb, Fb, P, lab, lbb);
+        // back to field order (rho, p, vx, vy, bx, by, bz)
+        const double gab[7] = {lab[0], lab[1], isx ? lab[2] : lab[3], isx ? lab[3] : lab[2],
+                               isx ? lab[4] : lab[5], isx ? lab[5] : lab[4], lab[6]};
+        const double gbb[7] = {lbb[0], lbb[1], isx ? lbb[2] : lbb[3], isx ? lbb[3] : lbb[2],
+                               isx ? lbb[4] : lbb[5], isx ? lbb[5] : lbb[4], lbb[6]};
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            if (isx) {
+                sm.qax[f][row][a + 1] = gab[f];
+                sm.qbx[f][row][a + 1] = gbb[f];
+            } else {
+                sm.qay[f][a + 1][row] = gab[f];
+                sm.qby[f][a + 1][row] = gbb[f];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- gather into the tile's cells ----------------------------------------------------------
+    // Cell c gets: the direct adjoint of its update; the face-state adjoints of its two faces
+    // (value part), its own slope adjoint through its minmod choice, and its neighbours'
+    // slope adjoints where their minmod choice used c; the Powell terms of its neighbours.
+    for (int i = tid; i < ATX * ATY; i += NT) {
+        const int ly = i / ATX, lx = i - ly * ATX;
+        const int gx = x0 + lx, gy = y0 + ly;
+        if (gx >= N || gy >= M) continue;
+        const long long k = (long long)gy * N + gx;
+        double lam[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) lam[f] = scratch[(size_t)f * K + k];
+        // two directions
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+            const bool isx = dir == 0;
+            const int a = isx ? lx : ly;      // position along the normal
+            const int o = isx ? ly : lx;      // row (x) or column (y)
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                // cell values at positions a-2 .. a+2
+                double cv[5];
+#pragma unroll
+                for (int t = 0; t < 5; ++t)
+                    cv[t] = isx ? sm.U[f][o + HU][a - 2 + t + HU] : sm.U[f][a - 2 + t + HU][o + HU];
+                // slope adjoint of the cells at positions a-1, a, a+1 (face j between j-1 and
+                // j is stored at index j+1)
+                double sb[3];
+                int sel[3];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const int pc = a - 1 + t;
+                    const double qa_up = isx ? sm.qax[f][o][pc + 2] : sm.qay[f][pc + 2][o];
+                    const double qb_dn = isx ? sm.qbx[f][o][pc + 1] : sm.qby[f][pc + 1][o];
+                    double s = slope_sel(cv[t], cv[t + 1], cv[t + 2], sel[t]);
+                    // face states of cell pc: low side of face pc+1 (c + s/2), high side of
+                    // face pc (c - s/2); a fallback removes the slope term
+                    const bool fbu = f < 2 && le_zero(fma(0.5, s, cv[t + 1]));
+                    const bool fbd = f < 2 && le_zero(fma(-0.5, s, cv[t + 1]));
+                    sb[t] = (fbu ? 0.0 : 0.5 * qa_up) - (fbd ? 0.0 : 0.5 * qb_dn);
+                }
+                // value parts: cell a is the low side of face a+1 and the high side of face a
+                double acc = (isx ? sm.qax[f][o][a + 2] : sm.qay[f][a + 2][o]) +
+                             (isx ? sm.qbx[f][o][a + 1] : sm.qby[f][a + 1][o]);
+                // own slope: left difference (c - c_{-1}) -> +1, right (c_{+1} - c) -> -1
+                acc += sel[1] == -1 ? sb[1] : (sel[1] == 1 ? -sb[1] : 0.0);
+                // neighbour a-1 took its right difference (c_a - c_{a-1})
+                acc += sel[0] == 1 ? sb[0] : 0.0;
+                // neighbour a+1 took its left difference (c_{a+1} - c_a)
+                acc -= sel[2] == -1 ? sb[2] : 0.0;
+                lam[f] += acc;
+            }
+        }
+        // Powell: divb_c' = 0.5 kx (bx_{c'+1} - bx_{c'-1}) + 0.5 ky (by_{c'+N} - by_{c'-N})
+        {
+            const long long kW = (long long)gy * N + wrap(gx - 1, N);
+            const long long kE = (long long)gy * N + wrap(gx + 1, N);
+            const long long kS = (long long)wrap(gy - 1, M) * N + gx;
+            const long long kN = (long long)wrap(gy + 1, M) * N + gx;
+            const double* dvb = scratch + (size_t)14 * K;
+            lam[4] += 0.5 * kx * (dvb[kW] - dvb[kE]);
+            lam[5] += 0.5 * ky * (dvb[kS] - dvb[kN]);
+        }
+        // field adjoint back to the stored Gaussian units: b = B / sqrt(4 pi)
+        lam[4] *= kInvSpi4;
+        lam[5] *= kInvSpi4;
+        lam[6] *= kInvSpi4;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) lam_in.f[f][k] = lam[f];
+    }
+}
+
+int grid_cells(long long K) {
+    long long g = (K + NT - 1) / NT;
+    return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
+}
+
+}  // namespace
+
+size_t adj_faces_smem_bytes() { return sizeof(AdjSmem); }
+
+cudaError_t prepare_adjoint() {
+    return cudaFuncSetAttribute(adj_faces_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(AdjSmem));
+}
+
+cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
+                                const CPlanes& lam_out, const Planes& lam_in, double* scratch,
+                                const double* T_do, cudaStream_t st) {
+    const long long K = (long long)P.N * P.M;
+    adj_update_kernel<<<grid_cells(K), NT, 0, st>>>(P, U, aux, lam_out, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 grid((P.N + ATX - 1) / ATX, (P.M + ATY - 1) / ATY);
+    adj_faces_kernel<<<grid, NT, sizeof(AdjSmem), st>>>(P, U, scratch, lam_in, T_do);
+    return cudaGetLastError();
+}
+
+}  // namespace gd

@@ -14,6 +14,7 @@
 
 #include "../../include/gd2d.h"
 #include "gd_internal.cuh"
+#include "gd_ctx.h"
 #include "gd_kernels.h"
 
 using gd::CPlanes;
@@ -36,38 +37,6 @@ gd_status cuda_fail(cudaError_t e) {
         if (e_ != cudaSuccess) return cuda_fail(e_);  \
     } while (0)
 
-struct gd_ctx {
-    gd_config cfg;
-    Params P;
-    int nf = 4;
-    long long K = 0;
-    int device = 0;
-    double* state[2] = {nullptr, nullptr};  // nf planes of K doubles each
-    int cur = 0;
-    Scalars* sc = nullptr;                  // device scalars of the resident state
-    double* ref_planes = nullptr;           // 2 * nf * K: SoA in/out for gd_step_ref
-    double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
-    long long launches = 0;
-    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
-
-    Planes planes(int which) const {
-        Planes p{};
-        for (int f = 0; f < gd::kMaxFields; ++f)
-            p.f[f] = f < nf ? state[which] + (size_t)f * K : nullptr;
-        return p;
-    }
-    static CPlanes cplanes(const Planes& p) {
-        CPlanes c{};
-        for (int f = 0; f < gd::kMaxFields; ++f) c.f[f] = p.f[f];
-        return c;
-    }
-    Planes ref_plane_set(int which) const {
-        Planes p{};
-        for (int f = 0; f < gd::kMaxFields; ++f)
-            p.f[f] = f < nf ? ref_planes + ((size_t)which * nf + f) * K : nullptr;
-        return p;
-    }
-};
 
 namespace {
 
@@ -210,6 +179,7 @@ gd_status gd_destroy(gd_ctx* ctx) {
     cudaFree(ctx->sc);
     cudaFree(ctx->ref_planes);
     cudaFree(ctx->aos);
+    gd::adj_free(ctx);
     delete ctx;
     return GD_OK;
 }

@@ -1,0 +1,68 @@
+// gd_ctx.h -- the context behind the C ABI's gd_ctx handle (internal).
+#pragma once
+
+#include <map>
+#include <utility>
+
+#include "../../include/gd2d.h"
+#include "gd_internal.cuh"
+
+namespace gd {
+
+// Record of a differentiated forward run (gd_adj_forward): dt sequence, checkpoints and
+// work buffers of the reverse and tangent sweeps.
+struct AdjStore {
+    int nsteps = 0, every = 0, nckpt = 0;
+    double* dts = nullptr;       // nsteps
+    double* ckpt = nullptr;      // nckpt * nf * K: state at steps 0, every, 2 every, ...
+    double* seg = nullptr;       // (every + 1) * nf * K: states of one segment
+    double* aux = nullptr;       // every * 8 * K: flux differences and Powell term per step
+    double* lam = nullptr;       // 2 * nf * K
+    double* scratch = nullptr;   // 15 * K
+    double* tbits = nullptr;     // dt accumulator the recompute pass writes (unused value)
+};
+
+}  // namespace gd
+
+using gd::CPlanes;
+using gd::Params;
+using gd::Planes;
+using gd::Scalars;
+
+struct gd_ctx {
+    gd_config cfg;
+    Params P;
+    int nf = 4;
+    long long K = 0;
+    int device = 0;
+    double* state[2] = {nullptr, nullptr};  // nf planes of K doubles each
+    int cur = 0;
+    Scalars* sc = nullptr;                  // device scalars of the resident state
+    double* ref_planes = nullptr;           // 2 * nf * K: SoA in/out for gd_step_ref
+    double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
+    long long launches = 0;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
+    gd::AdjStore* adj = nullptr;            // differentiation record (gd_adj_forward)
+
+    Planes planes(int which) const {
+        Planes p{};
+        for (int f = 0; f < gd::kMaxFields; ++f)
+            p.f[f] = f < nf ? state[which] + (size_t)f * K : nullptr;
+        return p;
+    }
+    static CPlanes cplanes(const Planes& p) {
+        CPlanes c{};
+        for (int f = 0; f < gd::kMaxFields; ++f) c.f[f] = p.f[f];
+        return c;
+    }
+    Planes ref_plane_set(int which) const {
+        Planes p{};
+        for (int f = 0; f < gd::kMaxFields; ++f)
+            p.f[f] = f < nf ? ref_planes + ((size_t)which * nf + f) * K : nullptr;
+        return p;
+    }
+};
+
+namespace gd {
+void adj_free(gd_ctx* ctx);
+}  // namespace gd

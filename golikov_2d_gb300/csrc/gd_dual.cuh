@@ -1,0 +1,87 @@
+// gd_dual.cuh -- forward-mode dual numbers for the tangent (JVP) of the fast step.
+//
+// A Dual carries a value and one directional derivative.  The overloads mirror the double
+// helpers of gd_internal.cuh, so the templated tile code (gd_mhd_tile.cuh) runs unchanged
+// on either type: arithmetic propagates derivatives by the chain rule; comparisons,
+// selections, guards and the minmod choice look at the value only, i.e. the derivative is
+// taken along the branch the value takes (minmod, wave-speed min/max, region selection,
+// floors).
+#pragma once
+
+#include "gd_internal.cuh"
+
+namespace gd {
+
+// keep the double overloads visible next to the Dual ones inside this namespace
+using ::fma;
+using ::isfinite;
+
+struct Dual {
+    double v, d;
+};
+
+__device__ __forceinline__ Dual make_dual(double v, double d = 0.0) { return Dual{v, d}; }
+
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
+    return {a.v * b.v, fma(a.v, b.d, a.d * b.v)};
+}
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+__device__ __forceinline__ Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+
+__device__ __forceinline__ Dual fma(Dual a, Dual b, Dual c) {
+    return {::fma(a.v, b.v, c.v), ::fma(a.v, b.d, ::fma(a.d, b.v, c.d))};
+}
+__device__ __forceinline__ Dual fma(double a, Dual b, Dual c) {
+    return {::fma(a, b.v, c.v), ::fma(a, b.d, c.d)};
+}
+__device__ __forceinline__ Dual fma(Dual a, double b, Dual c) {
+    return {::fma(a.v, b, c.v), ::fma(a.d, b, c.d)};
+}
+__device__ __forceinline__ Dual fma(Dual a, Dual b, double c) {
+    return {::fma(a.v, b.v, c), ::fma(a.v, b.d, a.d * b.v)};
+}
+
+__device__ __forceinline__ Dual rcp_fast(Dual x) {
+    const double r = rcp_fast(x.v);
+    return {r, -x.d * r * r};
+}
+__device__ __forceinline__ Dual rsqrt_fast(Dual x) {
+    const double r = rsqrt_fast(x.v);
+    return {r, -0.5 * x.d * r * r * r};
+}
+__device__ __forceinline__ Dual sqrt_fast(Dual x) {
+    if (x.v == 0.0) return {0.0, 0.0};
+    const double r = rsqrt_fast(x.v);
+    return {x.v * r, 0.5 * x.d * r};
+}
+
+// value-only predicates and selections (derivative follows the selected branch)
+__device__ __forceinline__ unsigned long long abs_bits(Dual x) { return abs_bits(x.v); }
+__device__ __forceinline__ bool le_zero(Dual x) { return le_zero(x.v); }
+__device__ __forceinline__ bool gt_zero(Dual x) { return gt_zero(x.v); }
+__device__ __forceinline__ bool lt_zero(Dual x) { return lt_zero(x.v); }
+__device__ __forceinline__ bool ge_zero(Dual x) { return ge_zero(x.v); }
+__device__ __forceinline__ bool isfinite(Dual x) { return ::isfinite(x.v); }
+__device__ __forceinline__ Dual dabs(Dual x) { return lt_zero(x.v) ? -x : x; }
+__device__ __forceinline__ Dual dmin(Dual a, Dual b) { return dlt(b.v, a.v) ? b : a; }
+__device__ __forceinline__ Dual dmax(Dual a, Dual b) { return dlt(a.v, b.v) ? b : a; }
+__device__ __forceinline__ Dual max_nonneg(Dual a, Dual b) {
+    return abs_bits(a.v) < abs_bits(b.v) ? b : a;
+}
+__device__ __forceinline__ Dual minmod(Dual a, Dual b) {
+    const long long ba = bits(a.v), bb = bits(b.v);
+    const bool zero = ((ba << 1) == 0) | ((bb << 1) == 0) | ((ba ^ bb) < 0);
+    const Dual m = (abs_bits(a.v) <= abs_bits(b.v)) ? a : b;
+    return zero ? Dual{0.0, 0.0} : m;
+}
+__device__ __forceinline__ double value_of(Dual x) { return x.v; }
+__device__ __forceinline__ double value_of(double x) { return x; }
+
+}  // namespace gd

@@ -1,6 +1,10 @@
 // gd_fast_mhd.cu -- fused minmod-TVD + HLLD / HLLC-MHD + Powell-source update for 2-D ideal
 // MHD, face-once tiles (same phase structure as gd_fast_euler.cu: load, slopes, faces,
-// update).
+// update), and its forward-mode tangent.
+//
+// The flux and the tile body are templates on the scalar type: `double` gives the step,
+// `Dual` (gd_dual.cuh) gives the tangent (JVP) of exactly the same arithmetic, with the dt
+// held fixed and derivatives taken along the branches the values take.
 //
 // Field units.  The reference stores Gaussian B and divides by sqrt(4 pi) inside every flux
 // call (Gas_Dinamic.cu:970-976), multiplying the field fluxes back (:1497-1499).  Here the
@@ -18,6 +22,9 @@
 // (kernel.cu:2568-2604); axisymmetric sources (kernel.cu:2615-2648); floors rho <= 0 ->
 // old rho, p <= 0 -> 1e-6; dt = min over faces of krit*rad/max(|SL|,|SR|), rad = dx on
 // x-faces (kernel.cu:2560).
+#include <type_traits>
+
+#include "gd_dual.cuh"
 #include "gd_internal.cuh"
 #include "gd_kernels.h"
 
@@ -28,29 +35,39 @@ constexpr int TX = 32;
 constexpr int NT = 256;
 constexpr int NF = 7;  // rho, p, vx, vy, bx, by, bz
 
+template <class T>
+__device__ __forceinline__ T cst(double x);
+template <>
+__device__ __forceinline__ double cst<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ Dual cst<Dual>(double x) { return Dual{x, 0.0}; }
+
+template <class T>
 struct FluxM {
-    double m, mn, mt, e, bn, bt, bz;  // mass, normal / tangential momentum, energy, field
+    T m, mn, mt, e, bn, bt, bz;  // mass, normal / tangential momentum, energy, field
 };
 
 // One side of the face in the local frame (un normal, ut in-plane tangential, uz = 0).
+template <class T>
 struct Side {
-    double r, p, un, ut, bn, bt, bz, bb, pT, E, cf;
-    double F0, F1, F2, F4, F6, F7;
+    T r, p, un, ut, bn, bt, bz, bb, pT, E, cf;
+    T F0, F1, F2, F4, F6, F7;
 };
 
-__device__ __forceinline__ void side(Side& S, double r, double p, double un, double ut, double bn,
-                                     double bt, double bz, const Params& P) {
+template <class T>
+__device__ __forceinline__ void side(Side<T>& S, T r, T p, T un, T ut, T bn, T bt, T bz,
+                                     const Params& P) {
     S.r = r; S.p = p; S.un = un; S.ut = ut; S.bn = bn; S.bt = bt; S.bz = bz;
-    const double bn2 = bn * bn;
+    const T bn2 = bn * bn;
     S.bb = fma(bz, bz, fma(bt, bt, bn2));
     S.pT = fma(0.5, S.bb, p);
     S.E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(un, un, ut * ut), S.bb));
-    const double gp = P.gamma * p;
-    const double a = gp + S.bb;
-    double disc = fma(a, a, -4.0 * gp * bn2);
-    disc = le_zero(disc) ? 0.0 : disc;
-    const double X = 0.5 * (a + sqrt_fast(disc));  // rho cf^2
-    S.cf = X * rsqrt_fast(X * r);                   // sqrt(X / r)
+    const T gp = P.gamma * p;
+    const T a = gp + S.bb;
+    T disc = fma(a, a, -4.0 * gp * bn2);
+    disc = le_zero(disc) ? cst<T>(0.0) : disc;
+    const T X = 0.5 * (a + sqrt_fast(disc));  // rho cf^2
+    S.cf = X * rsqrt_fast(X * r);              // sqrt(X / r)
     S.F0 = r * un;
     S.F1 = fma(S.F0, un, S.pT - bn2);
     S.F2 = fma(S.F0, ut, -bn * bt);
@@ -64,118 +81,120 @@ __device__ __forceinline__ double sgn_select(double v, int idbn) {
     const double w = idbn < 0 ? from_bits(bits(v) ^ (long long)0x8000000000000000ULL) : v;
     return idbn == 0 ? 0.0 : w;
 }
+__device__ __forceinline__ Dual sgn_select(Dual v, int idbn) {
+    return idbn == 0 ? Dual{0.0, 0.0} : (idbn < 0 ? -v : v);
+}
 
 // HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = max(|SL|, |SR|).
-__device__ __forceinline__ FluxM hlld_local(const Side& A, const Side& B, int method,
-                                            double& UU) {
-    const double uminN = dmin(A.un, B.un);
-    const double umaxN = dmax(A.un, B.un);
-    const double cmax = max_nonneg(A.cf, B.cf);
-    const double SL = uminN - cmax, SR = umaxN + cmax;
-    const double suL = SL - A.un, suR = SR - B.un;
-    const double mL = A.r * suL, mR = B.r * suR;
-    const double iden = rcp_fast(mR - mL);
-    const double SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
-    const double PTT = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT)) * iden;
+template <class T>
+__device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& B, int method,
+                                               T& UU) {
+    const T uminN = dmin(A.un, B.un);
+    const T umaxN = dmax(A.un, B.un);
+    const T cmax = max_nonneg(A.cf, B.cf);
+    const T SL = uminN - cmax, SR = umaxN + cmax;
+    const T suL = SL - A.un, suR = SR - B.un;
+    const T mL = A.r * suL, mR = B.r * suR;
+    const T iden = rcp_fast(mR - mL);
+    const T SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
+    const T PTT = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT)) * iden;
     UU = max_nonneg(dabs(SL), dabs(SR));
-    const double iS = rcp_fast(SR - SL);
-    const double bn = fma(SR, B.bn, -SL * A.bn) * iS;
-    const double bt = (fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6)) * iS;
-    const double bz = (fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7)) * iS;
-    const double iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
-    const double rLL = mL * iL, rRR = mR * iR;
+    const T iS = rcp_fast(SR - SL);
+    const T bn = fma(SR, B.bn, -SL * A.bn) * iS;
+    const T bt = (fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6)) * iS;
+    const T bz = (fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7)) * iS;
+    const T iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
+    const T rLL = mL * iL, rRR = mR * iR;
 
-    // region: takeL, level 0 (F), 1 (star), 2 (double star)
-    FluxM F;
+    FluxM<T> F;
     if (method == GD_METHOD_HLLC_MHD) {
         const bool takeL = ge_zero(SL) || ge_zero(SM);
-        const Side& K = takeL ? A : B;
-        const double S = takeL ? SL : SR;
+        const Side<T>& K = takeL ? A : B;
+        const T S = takeL ? SL : SR;
         const bool star = takeL ? lt_zero(SL) : gt_zero(SR);
         F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
         if (star) {
             // HLL state of the fan (Gas_Dinamic.cu:1145-1149); mom_z: U = 0, F = -bn bz
-            const double UZ0 = (fma(SR, B.r, -SL * A.r) + (A.F0 - B.F0)) * iS;
-            const double UZ1 = (fma(SR, B.r * B.un, -SL * A.r * A.un) + (A.F1 - B.F1)) * iS;
-            const double UZ2 = (fma(SR, B.r * B.ut, -SL * A.r * A.ut) + (A.F2 - B.F2)) * iS;
-            const double UZ3 = (B.bn * B.bz - A.bn * A.bz) * iS;
-            const double iU0 = rcp_fast(UZ0);
-            const double vS = UZ2 * iU0, wS = UZ3 * iU0;
-            const double ptz = 0.5 * (fma(mR, SM - B.un, B.pT) + fma(mL, SM - A.un, A.pT));
-            const double sbvz = fma(bn, UZ1, fma(bt, UZ2, bz * UZ3)) * iU0;
-            const double sbvK = fma(K.un, K.bn, K.ut * K.bt);
-            const double iK = takeL ? iL : iR;
-            const double suK = takeL ? suL : suR;
-            const double eK = (fma(K.E, suK, fma(ptz, SM, -K.pT * K.un)) + bn * (sbvK - sbvz)) * iK;
-            const double rK = takeL ? rLL : rRR;
+            const T UZ0 = (fma(SR, B.r, -SL * A.r) + (A.F0 - B.F0)) * iS;
+            const T UZ1 = (fma(SR, B.r * B.un, -SL * A.r * A.un) + (A.F1 - B.F1)) * iS;
+            const T UZ2 = (fma(SR, B.r * B.ut, -SL * A.r * A.ut) + (A.F2 - B.F2)) * iS;
+            const T UZ3 = (B.bn * B.bz - A.bn * A.bz) * iS;
+            const T iU0 = rcp_fast(UZ0);
+            const T vS = UZ2 * iU0;
+            const T ptz = 0.5 * (fma(mR, SM - B.un, B.pT) + fma(mL, SM - A.un, A.pT));
+            const T sbvz = fma(bn, UZ1, fma(bt, UZ2, bz * UZ3)) * iU0;
+            const T sbvK = fma(K.un, K.bn, K.ut * K.bt);
+            const T iK = takeL ? iL : iR;
+            const T suK = takeL ? suL : suR;
+            const T eK = (fma(K.E, suK, fma(ptz, SM, -K.pT * K.un)) + bn * (sbvK - sbvz)) * iK;
+            const T rK = takeL ? rLL : rRR;
             F.m = fma(S, rK - K.r, F.m);
             F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
             F.mt = fma(S, fma(rK, vS, -K.r * K.ut), F.mt);
             F.e = fma(S, eK - K.E, F.e);
             F.bt = fma(S, bt - K.bt, F.bt);
             F.bz = fma(S, bz - K.bz, F.bz);
-            (void)wS;
         }
     } else {
-        const double bbn = bn * bn;
+        const T bbn = bn * bn;
         // star states of both sides (Gas_Dinamic.cu:1306-1350)
-        double vLL, wLL, btL, bzL, vRR, wRR, btR, bzR;
+        T vLL, wLL, btL, bzL, vRR, wRR, btR, bzR;
         {
-            const double tt = fma(mL, SL - SM, -bbn);
+            const T tt = fma(mL, SL - SM, -bbn);
             if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {  // |tt| >= 1e-5
-                const double it = rcp_fast(tt);
-                const double c = bn * (SM - A.un) * it;
-                const double d = fma(mL, suL, -bbn) * it;
+                const T it = rcp_fast(tt);
+                const T c = bn * (SM - A.un) * it;
+                const T d = fma(mL, suL, -bbn) * it;
                 vLL = fma(-c, A.bt, A.ut);
                 wLL = -c * A.bz;
                 btL = A.bt * d;
                 bzL = A.bz * d;
             } else {
-                vLL = A.ut; wLL = 0.0; btL = 0.0; bzL = 0.0;
+                vLL = A.ut; wLL = cst<T>(0.0); btL = cst<T>(0.0); bzL = cst<T>(0.0);
             }
         }
         {
-            const double tt = fma(mR, SR - SM, -bbn);
+            const T tt = fma(mR, SR - SM, -bbn);
             if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {
-                const double it = rcp_fast(tt);
-                const double c = bn * (SM - B.un) * it;
-                const double d = fma(mR, suR, -bbn) * it;
+                const T it = rcp_fast(tt);
+                const T c = bn * (SM - B.un) * it;
+                const T d = fma(mR, suR, -bbn) * it;
                 vRR = fma(-c, B.bt, B.ut);
                 wRR = -c * B.bz;
                 btR = B.bt * d;
                 bzR = B.bz * d;
             } else {
-                vRR = B.ut; wRR = 0.0; btR = 0.0; bzR = 0.0;
+                vRR = B.ut; wRR = cst<T>(0.0); btR = cst<T>(0.0); bzR = cst<T>(0.0);
             }
         }
-        const double SMbn = SM * bn;
-        const double sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
-        const double sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
-        const double eLL = (fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) +
-                            bn * (fma(A.un, A.bn, A.ut * A.bt) - sbLL)) * iL;
-        const double eRR = (fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) +
-                            bn * (fma(B.un, B.bn, B.ut * B.bt) - sbRR)) * iR;
-        const double isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
-        const double sLL = rLL * isLL, sRR = rRR * isRR;
+        const T SMbn = SM * bn;
+        const T sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
+        const T sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
+        const T eLL = (fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) +
+                       bn * (fma(A.un, A.bn, A.ut * A.bt) - sbLL)) * iL;
+        const T eRR = (fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) +
+                       bn * (fma(B.un, B.bn, B.ut * B.bt) - sbRR)) * iR;
+        const T isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
+        const T sLL = rLL * isLL, sRR = rRR * isRR;
         const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;  // |bn| > 1e-6
-        const double abn = dabs(bn);
-        const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
-        const double SRR = bnz ? fma(abn, isRR, SM) : SM;
+        const T abn = dabs(bn);
+        const T SLL = bnz ? fma(-abn, isLL, SM) : SM;
+        const T SRR = bnz ? fma(abn, isRR, SM) : SM;
         const int idbn = bnz ? (gt_zero(bn) ? 1 : -1) : 0;
 
         const bool takeL = ge_zero(SL) || ge_zero(SM);
         int level;
         if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
         else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
-        const Side& K = takeL ? A : B;
+        const Side<T>& K = takeL ? A : B;
         F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
         if (level >= 1) {
-            const double S = takeL ? SL : SR;
-            const double rK = takeL ? rLL : rRR;
-            const double vK = takeL ? vLL : vRR;
-            const double eK = takeL ? eLL : eRR;
-            const double btK = takeL ? btL : btR;
-            const double bzK = takeL ? bzL : bzR;
+            const T S = takeL ? SL : SR;
+            const T rK = takeL ? rLL : rRR;
+            const T vK = takeL ? vLL : vRR;
+            const T eK = takeL ? eLL : eRR;
+            const T btK = takeL ? btL : btR;
+            const T bzK = takeL ? bzL : bzR;
             F.m = fma(S, rK - K.r, F.m);
             F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
             F.mt = fma(S, fma(rK, vK, -K.r * K.ut), F.mt);
@@ -184,16 +203,16 @@ __device__ __forceinline__ FluxM hlld_local(const Side& A, const Side& B, int me
             F.bz = fma(S, bzK - K.bz, F.bz);
             if (level == 2) {
                 // double-star states (Gas_Dinamic.cu:1371-1430)
-                const double is = rcp_fast(sLL + sRR);
-                const double vL3 = (fma(sLL, vLL, sRR * vRR) + sgn_select(btR - btL, idbn)) * is;
-                const double wL3 = (fma(sLL, wLL, sRR * wRR) + sgn_select(bzR - bzL, idbn)) * is;
-                const double s2 = sgn_select(sLL * sRR, idbn);
-                const double bt3 = fma(s2, vRR - vLL, fma(sLL, btR, sRR * btL)) * is;
-                const double bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
-                const double sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
-                const double sK = takeL ? -sLL : sRR;
-                const double e3 = fma(sgn_select(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
-                const double S2 = takeL ? SLL : SRR;
+                const T is = rcp_fast(sLL + sRR);
+                const T vL3 = (fma(sLL, vLL, sRR * vRR) + sgn_select(btR - btL, idbn)) * is;
+                const T wL3 = (fma(sLL, wLL, sRR * wRR) + sgn_select(bzR - bzL, idbn)) * is;
+                const T s2 = sgn_select(sLL * sRR, idbn);
+                const T bt3 = fma(s2, vRR - vLL, fma(sLL, btR, sRR * btL)) * is;
+                const T bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
+                const T sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
+                const T sK = takeL ? -sLL : sRR;
+                const T e3 = fma(sgn_select(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
+                const T S2 = takeL ? SLL : SRR;
                 F.mt = fma(S2, rK * (vL3 - vK), F.mt);
                 F.e = fma(S2, e3 - eK, F.e);
                 F.bt = fma(S2, bt3 - btK, F.bt);
@@ -206,7 +225,65 @@ __device__ __forceinline__ FluxM hlld_local(const Side& A, const Side& B, int me
     return F;
 }
 
-template <int ORDER, int TY>
+// ---- state access: planes of doubles for the step, value + tangent planes for the JVP ----
+
+struct DualCPlanes {
+    CPlanes v, d;
+};
+struct DualPlanes {
+    Planes v, d;
+};
+
+__device__ __forceinline__ void load_state(const Params& P, const CPlanes& in, int gx, int gy,
+                                           double* v) {
+    fetch_cell<NF>(P, in, gx, gy, v);
+}
+
+// Tangent of a ghost value: the linear part of the boundary condition.  Copies and sign
+// flips carry the derivative; constants (ambient) and the active outflow clamp have none.
+__device__ __forceinline__ void load_state(const Params& P, const DualCPlanes& in, int gx,
+                                           int gy, Dual* v) {
+    double a[NF], b[NF];
+    fetch_cell<NF>(P, in.v, gx, gy, a);
+    fetch_cell<NF>(P, in.d, gx, gy, b);
+    int bc = -1;
+    if (gx < 0 || gx >= P.N) bc = gx < 0 ? P.bc[0] : P.bc[1];
+    else if (gy < 0 || gy >= P.M) bc = gy < 0 ? P.bc[2] : P.bc[3];
+    if (bc == GD_BC_AMBIENT || bc == GD_BC_AMBIENT_KEEPB) {
+        for (int f = 0; f < (bc == GD_BC_AMBIENT ? NF : 4); ++f) b[f] = 0.0;
+    } else if (bc == GD_BC_OUTFLOW) {
+        double raw[NF];
+        CPlanes plain = in.v;
+        int sx = gx < 0 ? 0 : (gx >= P.N ? P.N - 1 : gx);
+        int sy = gy < 0 ? 0 : (gy >= P.M ? P.M - 1 : gy);
+        raw[2] = plain.f[2][(long long)sy * P.N + sx];
+        if (raw[2] < 0) b[2] = 0.0;
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) v[f] = Dual{a[f], b[f]};
+}
+
+__device__ __forceinline__ void store_state(const Planes& out, long long k, int f, double x) {
+    out.f[f][k] = x;
+}
+__device__ __forceinline__ void store_state(const DualPlanes& out, long long k, int f, Dual x) {
+    out.v.f[f][k] = x.v;
+    out.d.f[f][k] = x.d;
+}
+__device__ __forceinline__ void copy_cell(const CPlanes& in, const Planes& out, long long k) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+}
+__device__ __forceinline__ void copy_cell(const DualCPlanes& in, const DualPlanes& out,
+                                          long long k) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        out.v.f[f][k] = in.v.f[f][k];
+        out.d.f[f][k] = in.d.f[f][k];
+    }
+}
+
+template <class T, int ORDER, int TY>
 struct SmemM {
     static constexpr int H = ORDER == 2 ? 2 : 1;
     static constexpr int SX = TX + 2 * H;
@@ -216,26 +293,33 @@ struct SmemM {
     static constexpr int kSly = ORDER == 2 ? NF * (TY + 2) * TX : 0;
     static constexpr int kFx = NF * TY * (TX + 1);
     static constexpr int kFy = NF * (TY + 1) * TX;
-    static constexpr size_t bytes = sizeof(double) * (kPrim + kSlx + kSly + kFx + kFy);
+    static constexpr size_t bytes = sizeof(T) * (kPrim + kSlx + kSly + kFx + kFy);
 };
 
+struct MhdTileResult {
+    double umax_x, umax_y;
+    bool any_active;
+    unsigned int nfl_r, nfl_p, nbad;
+};
+
+// One TX x TY tile at (tx0, ty0): load, slopes, faces, update.  IN/OUT are CPlanes/Planes
+// for T = double and DualCPlanes/DualPlanes for T = Dual.
 // flux component slots in smem: 0 mass, 1 energy, 2 mom x, 3 mom y, 4 bx, 5 by, 6 bz
-template <int ORDER, int TY>
-__global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Planes out,
-                                                      const double* __restrict__ T_do_ptr,
-                                                      unsigned long long* T_bits, Scalars* rot,
-                                                      Scalars* ctr, int dt_only) {
-    using S = SmemM<ORDER, TY>;
+// `aux` (T = double only; may be null) receives, per cell, the flux differences d[0..6]
+// and the Powell term divb that the update used (planes of N*M), for the adjoint.
+template <class T, int ORDER, int TY, class IN, class OUT>
+__device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OUT& out, int tx0,
+                                         int ty0, double T_do, int dt_only, T* smem,
+                                         MhdTileResult& res, double* aux = nullptr) {
+    using S = SmemM<T, ORDER, TY>;
     constexpr int H = S::H, SX = S::SX, SY = S::SY;
-    extern __shared__ double smem[];
-    double* prim = smem;
-    double* slx = prim + S::kPrim;
-    double* sly = slx + S::kSlx;
-    double* fx = sly + S::kSly;
-    double* fy = fx + S::kFx;
+    T* prim = smem;
+    T* slx = prim + S::kPrim;
+    T* sly = slx + S::kSlx;
+    T* fx = sly + S::kSly;
+    T* fy = fx + S::kFx;
 
     const int tid = threadIdx.x;
-    const int tx0 = blockIdx.x * TX, ty0 = blockIdx.y * TY;
     const int N = P.N, M = P.M;
 
     // ---- L: tile + cross halo, field to Heaviside-Lorentz units --------------------------
@@ -244,17 +328,17 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
         const bool xh = lx < H || lx >= TX + H, yh = ly < H || ly >= TY + H;
         if (xh && yh) continue;
         const int gx = tx0 + lx - H, gy = ty0 + ly - H;
-        double v[NF];
+        T v[NF];
         if (gx >= -2 && gx < N + 2 && gy >= -2 && gy < M + 2 &&
             !((gx < 0 || gx >= N) && (gy < 0 || gy >= M))) {
-            fetch_cell<NF>(P, in, gx, gy, v);
+            load_state(P, in, gx, gy, v);
         } else {
 #pragma unroll
-            for (int f = 0; f < NF; ++f) v[f] = f < 2 ? 1.0 : 0.0;  // never used
+            for (int f = 0; f < NF; ++f) v[f] = cst<T>(f < 2 ? 1.0 : 0.0);  // never used
         }
-        v[4] *= kInvSpi4;
-        v[5] *= kInvSpi4;
-        v[6] *= kInvSpi4;
+        v[4] = v[4] * kInvSpi4;
+        v[5] = v[5] * kInvSpi4;
+        v[6] = v[6] * kInvSpi4;
 #pragma unroll
         for (int f = 0; f < NF; ++f) prim[(f * SY + ly) * SX + lx] = v[f];
     }
@@ -264,19 +348,19 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
     if (ORDER == 2) {
         for (int i = tid; i < TY * (TX + 2); i += NT) {
             const int ly = i / (TX + 2), c = i - ly * (TX + 2);
-            const double* row = prim + (ly + H) * SX + (c - 1 + H);
+            const T* row = prim + (ly + H) * SX + (c - 1 + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                const double* q = row + f * SY * SX;
+                const T* q = row + f * SY * SX;
                 slx[(f * TY + ly) * (TX + 2) + c] = minmod(q[0] - q[-1], q[1] - q[0]);
             }
         }
         for (int i = tid; i < (TY + 2) * TX; i += NT) {
             const int r = i / TX, lx = i - r * TX;
-            const double* col = prim + (r - 1 + H) * SX + (lx + H);
+            const T* col = prim + (r - 1 + H) * SX + (lx + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                const double* q = col + f * SY * SX;
+                const T* q = col + f * SY * SX;
                 sly[(f * (TY + 2) + r) * TX + lx] = minmod(q[0] - q[-SX], q[SX] - q[0]);
             }
         }
@@ -303,14 +387,14 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
         if (P.frozen_radius > 0.0 && !cell_active(P, tx0 + ax, ty0 + ay) &&
             !cell_active(P, tx0 + lx, ty0 + ly))
             continue;
-        const double* pa = prim + (ay + H) * SX + (ax + H);
-        const double* pb = pa + (isx ? 1 : SX);
-        double qa[NF], qb[NF];
+        const T* pa = prim + (ay + H) * SX + (ax + H);
+        const T* pb = pa + (isx ? 1 : SX);
+        T qa[NF], qb[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            const double ca = pa[f * SY * SX], cb = pb[f * SY * SX];
+            const T ca = pa[f * SY * SX], cb = pb[f * SY * SX];
             if (ORDER == 2) {
-                double da, db;
+                T da, db;
                 if (isx) {
                     da = slx[(f * TY + ly) * (TX + 2) + lx];
                     db = slx[(f * TY + ly) * (TX + 2) + lx + 1];
@@ -318,7 +402,7 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
                     da = sly[(f * (TY + 2) + ly) * TX + lx];
                     db = sly[(f * (TY + 2) + ly + 1) * TX + lx];
                 }
-                double a = fma(0.5, da, ca), b = fma(-0.5, db, cb);
+                T a = fma(0.5, da, ca), b = fma(-0.5, db, cb);
                 if (f < 2) {
                     a = le_zero(a) ? ca : a;
                     b = le_zero(b) ? cb : b;
@@ -331,15 +415,15 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
             }
         }
         // local frame: x-face (n, t) = (x, y); y-face (n, t) = (y, x); z stays z
-        Side A, B;
+        Side<T> A, B;
         side(A, qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], isx ? qa[4] : qa[5],
              isx ? qa[5] : qa[4], qa[6], P);
         side(B, qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], isx ? qb[4] : qb[5],
              isx ? qb[5] : qb[4], qb[6], P);
-        double UU;
-        const FluxM F = hlld_local(A, B, P.method, UU);
+        T UU;
+        const FluxM<T> F = hlld_local(A, B, P.method, UU);
         if (isx) {
-            double* fo = fx + ly * (TX + 1) + lx;
+            T* fo = fx + ly * (TX + 1) + lx;
             constexpr int st = TY * (TX + 1);
             fo[0 * st] = F.m;
             fo[1 * st] = F.e;
@@ -348,9 +432,9 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
             fo[4 * st] = F.bn;
             fo[5 * st] = F.bt;
             fo[6 * st] = F.bz;
-            umax_x = max_nonneg(umax_x, UU);
+            umax_x = max_nonneg(umax_x, value_of(UU));
         } else {
-            double* fo = fy + ly * TX + lx;
+            T* fo = fy + ly * TX + lx;
             constexpr int st = (TY + 1) * TX;
             fo[0 * st] = F.m;
             fo[1 * st] = F.e;
@@ -359,13 +443,12 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
             fo[4 * st] = F.bt;
             fo[5 * st] = F.bn;
             fo[6 * st] = F.bz;
-            umax_y = max_nonneg(umax_y, UU);
+            umax_y = max_nonneg(umax_y, value_of(UU));
         }
     }
     __syncthreads();
 
     // ---- U: update (kernel.cu:2606-2660 in Heaviside-Lorentz field units) ----------------------
-    const double T_do = *T_do_ptr;
     const double kx = T_do / P.dx, ky = T_do / P.dy;
     const bool axi = P.geometry == GD_AXISYM;
     bool any_active = false;
@@ -374,49 +457,54 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
         const int ly = i / TX, lx = i - ly * TX;
         const int gx = tx0 + lx, gy = ty0 + ly;
         if (gx >= N || gy >= M) continue;
-        const double* c = prim + (ly + H) * SX + (lx + H);
+        const T* c = prim + (ly + H) * SX + (lx + H);
         constexpr int PS = SY * SX;
-        const double r = c[0], p = c[PS], u = c[2 * PS], v = c[3 * PS];
-        const double bx = c[4 * PS], by = c[5 * PS], bz = c[6 * PS];
+        const T r = c[0], p = c[PS], u = c[2 * PS], v = c[3 * PS];
+        const T bx = c[4 * PS], by = c[5 * PS], bz = c[6 * PS];
         const long long k = (long long)gy * N + gx;
         const double y = P.y0 + gy * P.dy;
         if (P.frozen_radius > 0.0) {
             const double x = P.x0 + gx * P.dx;
             if (sqrt(x * x + y * y) < P.frozen_radius) {
-                if (!dt_only) {
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
-                }
+                if (!dt_only) copy_cell(in, out, k);
                 continue;
             }
         }
         any_active = true;
         if (dt_only) continue;
-        const double* fxc = fx + ly * (TX + 1) + lx;
-        const double* fyc = fy + ly * TX + lx;
-        double d[NF];
+        const T* fxc = fx + ly * (TX + 1) + lx;
+        const T* fyc = fy + ly * TX + lx;
+        T d[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            const double* a = fxc + f * TY * (TX + 1);
-            const double* b = fyc + f * (TY + 1) * TX;
+            const T* a = fxc + f * TY * (TX + 1);
+            const T* b = fyc + f * (TY + 1) * TX;
             d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
         }
         // Powell divergence from cell-centred field: dx dy div b (kernel.cu:2568-2604)
-        const double bxE = c[4 * PS + 1], bxW = c[4 * PS - 1];
-        const double byN = c[5 * PS + SX], byS = c[5 * PS - SX];
-        double divb = fma(0.5 * kx, bxE - bxW, 0.5 * ky * (byN - byS));  // T_do * div b
+        const T bxE = c[4 * PS + 1], bxW = c[4 * PS - 1];
+        const T byN = c[5 * PS + SX], byS = c[5 * PS - SX];
+        T divb = fma(0.5 * kx, bxE - bxW, 0.5 * ky * (byN - byS));  // T_do * div b
         const double iy = axi ? rcp_fast(y) : 0.0;
-        if (axi) divb = fma(T_do * by, iy, divb);                      // kernel.cu:2615
-        const double ub = fma(u, bx, v * by);
-        const double bb = fma(bz, bz, fma(by, by, bx * bx));
-        const double E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(u, u, v * v), bb));
-        double r2 = r - d[0];
-        double mx2 = fma(r, u, -fma(bx, divb, d[2]));
-        double my2 = fma(r, v, -fma(by, divb, d[3]));
-        double bx2 = bx - fma(u, divb, d[4]);
-        const double by2 = by - fma(v, divb, d[5]);
-        const double bz2 = bz - d[6];
-        double E2 = E - fma(ub, divb, d[1]);
+        if (axi) divb = fma(T_do * by, iy, divb);                 // kernel.cu:2615
+        if constexpr (std::is_same<T, double>::value) {
+            if (aux != nullptr) {
+                const long long KK = (long long)N * M;
+#pragma unroll
+                for (int f = 0; f < NF; ++f) aux[f * KK + k] = d[f];
+                aux[7 * KK + k] = divb;
+            }
+        }
+        const T ub = fma(u, bx, v * by);
+        const T bb = fma(bz, bz, fma(by, by, bx * bx));
+        const T E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(u, u, v * v), bb));
+        T r2 = r - d[0];
+        T mx2 = fma(r, u, -fma(bx, divb, d[2]));
+        T my2 = fma(r, v, -fma(by, divb, d[3]));
+        T bx2 = bx - fma(u, divb, d[4]);
+        const T by2 = by - fma(v, divb, d[5]);
+        const T bz2 = bz - d[6];
+        T E2 = E - fma(ub, divb, d[1]);
         if (axi) {
             // geometric sources / y (kernel.cu:2619-2648) in field units b
             const double ty = T_do * iy;
@@ -427,38 +515,79 @@ __global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Plan
             E2 = fma(-ty, fma(E + p + 0.5 * bb, v, -by * ub), E2);
         }
         if (le_zero(r2)) { r2 = r; ++nfl_r; }
-        const double inv = rcp_fast(r2);
-        const double u2 = mx2 * inv, v2 = my2 * inv;
-        double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2), fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
-        if (le_zero(p2)) { p2 = 0.000001; ++nfl_p; }
+        const T inv = rcp_fast(r2);
+        const T u2 = mx2 * inv, v2 = my2 * inv;
+        T p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2), fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+        if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
         if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2) || !isfinite(bx2) ||
             !isfinite(by2) || !isfinite(bz2))
             ++nbad;
-        out.f[0][k] = r2;
-        out.f[1][k] = p2;
-        out.f[2][k] = u2;
-        out.f[3][k] = v2;
-        out.f[4][k] = bx2 * kSpi4;
-        out.f[5][k] = by2 * kSpi4;
-        out.f[6][k] = bz2 * kSpi4;
+        store_state(out, k, 0, r2);
+        store_state(out, k, 1, p2);
+        store_state(out, k, 2, u2);
+        store_state(out, k, 3, v2);
+        store_state(out, k, 4, bx2 * kSpi4);
+        store_state(out, k, 5, by2 * kSpi4);
+        store_state(out, k, 6, bz2 * kSpi4);
     }
-    if (ctr != nullptr && (nfl_r | nfl_p | nbad)) {
-        if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
-        if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
-        if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
+    res.umax_x = umax_x;
+    res.umax_y = umax_y;
+    res.any_active = any_active;
+    res.nfl_r = nfl_r;
+    res.nfl_p = nfl_p;
+    res.nbad = nbad;
+}
+
+template <int ORDER, int TY>
+__global__ void __launch_bounds__(NT) mhd_fast_kernel(Params P, CPlanes in, Planes out,
+                                                      const double* __restrict__ T_do_ptr,
+                                                      unsigned long long* T_bits, Scalars* rot,
+                                                      Scalars* ctr, int dt_only, double* aux) {
+    extern __shared__ __align__(16) double smem[];
+    MhdTileResult r;
+    mhd_tile<double, ORDER, TY>(P, in, out, blockIdx.x * TX, blockIdx.y * TY, *T_do_ptr, dt_only,
+                                smem, r, aux);
+    if (ctr != nullptr && (r.nfl_r | r.nfl_p | r.nbad)) {
+        if (r.nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)r.nfl_r);
+        if (r.nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)r.nfl_p);
+        if (r.nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)r.nbad);
     }
-    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot);
+    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot);
+}
+
+// Tangent of one step: (U, dU) -> (U', dU') with the dt read from *T_do_ptr (held fixed).
+template <int ORDER, int TY>
+__global__ void __launch_bounds__(NT) mhd_tangent_kernel(Params P, CPlanes in, CPlanes din,
+                                                         Planes out, Planes dout,
+                                                         const double* __restrict__ T_do_ptr) {
+    extern __shared__ __align__(16) double smem[];
+    MhdTileResult r;
+    const DualCPlanes I{in, din};
+    const DualPlanes O{out, dout};
+    mhd_tile<Dual, ORDER, TY>(P, I, O, blockIdx.x * TX, blockIdx.y * TY, *T_do_ptr, 0,
+                              reinterpret_cast<Dual*>(smem), r);
 }
 
 constexpr int kTY = 16;
+constexpr int kTYDual = 8;
 
 template <int ORDER>
 cudaError_t launch_t(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
                      unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
-                     cudaStream_t st) {
+                     cudaStream_t st, double* aux = nullptr) {
     dim3 grid((P.N + TX - 1) / TX, (P.M + kTY - 1) / kTY);
-    mhd_fast_kernel<ORDER, kTY><<<grid, NT, SmemM<ORDER, kTY>::bytes, st>>>(
-        P, in, out, T_do, T_bits, rot, ctr, dt_only);
+    mhd_fast_kernel<ORDER, kTY><<<grid, NT, SmemM<double, ORDER, kTY>::bytes, st>>>(
+        P, in, out, T_do, T_bits, rot, ctr, dt_only, aux);
+    return cudaGetLastError();
+}
+
+template <int ORDER>
+cudaError_t launch_tangent_t(const Params& P, const CPlanes& in, const CPlanes& din,
+                             const Planes& out, const Planes& dout, const double* T_do,
+                             cudaStream_t st) {
+    dim3 grid((P.N + TX - 1) / TX, (P.M + kTYDual - 1) / kTYDual);
+    mhd_tangent_kernel<ORDER, kTYDual><<<grid, NT, SmemM<Dual, ORDER, kTYDual>::bytes, st>>>(
+        P, in, din, out, dout, T_do);
     return cudaGetLastError();
 }
 
@@ -467,10 +596,20 @@ cudaError_t launch_t(const Params& P, const CPlanes& in, const Planes& out, cons
 cudaError_t prepare_mhd_fast() {
     cudaError_t e = cudaFuncSetAttribute(mhd_fast_kernel<1, kTY>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SmemM<1, kTY>::bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(mhd_fast_kernel<2, kTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)SmemM<2, kTY>::bytes);
+                                         (int)SmemM<double, 1, kTY>::bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mhd_fast_kernel<2, kTY>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SmemM<double, 2, kTY>::bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mhd_tangent_kernel<1, kTYDual>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SmemM<Dual, 1, kTYDual>::bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mhd_tangent_kernel<2, kTYDual>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SmemM<Dual, 2, kTYDual>::bytes);
+    return e;
 }
 
 cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& out,
@@ -478,6 +617,20 @@ cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& ou
                             Scalars* ctr, int dt_only, cudaStream_t st) {
     if (P.order == 1) return launch_t<1>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
     return launch_t<2>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+cudaError_t launch_mhd_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
+                                const double* T_do, unsigned long long* T_bits, double* aux,
+                                cudaStream_t st) {
+    if (P.order == 1) return launch_t<1>(P, in, out, T_do, T_bits, nullptr, nullptr, 0, st, aux);
+    return launch_t<2>(P, in, out, T_do, T_bits, nullptr, nullptr, 0, st, aux);
+}
+
+cudaError_t launch_mhd_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
+                               const Planes& out, const Planes& dout, const double* T_do,
+                               cudaStream_t st) {
+    if (P.order == 1) return launch_tangent_t<1>(P, in, din, out, dout, T_do, st);
+    return launch_tangent_t<2>(P, in, din, out, dout, T_do, st);
 }
 
 }  // namespace gd

@@ -42,6 +42,25 @@ cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, c
                                int nitems, int cur, int dt_only, Scalars* sc_override, int ctas,
                                cudaStream_t st);
 
+// Tangent (forward-mode JVP) of one fast MHD step with the dt read from *T_do:
+// (in, din) -> (out, dout).
+cudaError_t launch_mhd_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
+                               const Planes& out, const Planes& dout, const double* T_do,
+                               cudaStream_t st);
+
+// Fast MHD step that also stores, per cell, the flux differences and the Powell term the
+// update used (8 planes of N*M in `aux`), for the adjoint.  No dt rotation.
+cudaError_t launch_mhd_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
+                                const double* T_do, unsigned long long* T_bits, double* aux,
+                                cudaStream_t st);
+// One reverse step of the fast MHD step (HLLD, order 2, Cartesian, periodic):
+// lam_in = S'(U)^T lam_out, with U, aux of the forward step and the dt *T_do.
+// `scratch` holds 15 planes of N*M.
+cudaError_t prepare_adjoint();
+cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
+                                const CPlanes& lam_out, const Planes& lam_in, double* scratch,
+                                const double* T_do, cudaStream_t st);
+
 // Parity step: per-cell faces in the reference's arithmetic order (built without FMA
 // contraction); bit-identical to the reference step.
 cudaError_t launch_parity(const Params& P, const CPlanes& in, const Planes& out,

@@ -156,6 +156,29 @@ gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
  * current state; plane of N*M doubles, index m*N + n.  Valid until the next advance. */
 gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
 
+/* ---- differentiation: discrete adjoint and tangent ------------------------------------
+ * No counterpart in the reference.  The map differentiated is n steps of the fast step
+ * with the dt sequence of a recorded forward run held fixed (the CFL minimum is not
+ * differentiated); minmod, wave-speed min/max, HLLD region and guard choices and floors
+ * are differentiated along the branch the forward values take.  Supported: MHD, HLLD,
+ * order 2, Cartesian, periodic on all sides, fast mode, no frozen cells (the Orszag-Tang
+ * configuration); other configurations return GD_ERR_UNSUPPORTED.  All vectors are device
+ * pointers in the reference AoS layout (d/ds: K x 2, d/du: K x 2, d/dB: K x 3, Gaussian B).
+ *
+ * gd_adj_forward: advance nsteps from the current state (as gd_advance), recording the dt
+ *   of every step and a checkpoint of the state every ckpt_every steps.
+ * gd_adj_backward: given dL/dU at the final state, return dL/dU at the recorded initial
+ *   state; each checkpoint segment is recomputed once, then stepped back in reverse.
+ * gd_tangent: J v, the derivative of the recorded map at the initial state along v.
+ * gd_adj_replay: the recorded map (same dt sequence) applied to another initial state. */
+gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stream);
+gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const double* gb,
+                          double* os, double* ou, double* ob, gd_stream stream);
+gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const double* vb,
+                     double* os, double* ou, double* ob, gd_stream stream);
+gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                        double* os, double* ou, double* ob, gd_stream stream);
+
 /* ---- batched: many independent grids --------------------------------------------------
  * No counterpart in the reference (it advances one grid, kernel.cu:4102).  A batch holds
  * ngrids independent grids of any sizes (same physics, order and mode; Euler, fast mode),

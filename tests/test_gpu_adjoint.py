@@ -1,0 +1,136 @@
+"""Discrete adjoint and tangent of the fast MHD step (Orszag-Tang, HLLD, periodic).
+
+The differentiated map is n steps with the recorded dt sequence held fixed.  Checks:
+  * dot-product identity <lam, J v> = <J^T lam, v> between the forward-mode tangent kernel
+    and the reverse sweep (both hand-written), relative difference <= 1e-10;
+  * the gradient of L = 1/2 sum (rho_n - rho_target)^2 against FP64 central finite
+    differences of the same map on random directions, relative difference <= 1e-6;
+  * the gradient does not depend on the checkpoint interval (bit-identical).
+"""
+import numpy as np
+import pytest
+
+import golikov_2d_gb300 as g
+from golikov_2d_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def setup(N=64, nsteps=12, every=5):
+    cfg, s, u, b = problems.orszag_tang(N, N)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.adj_forward(nsteps, every)
+    sf, uf, bf = np.zeros_like(s), np.zeros_like(u), np.zeros_like(b)
+    sol.export_state(sf, uf, bf)
+    return cfg, sol, (s, u, b), (sf, uf, bf)
+
+
+def vjp(sol, gs, gu, gb):
+    import torch
+    o = [torch.zeros_like(dev(x)) for x in (gs, gu, gb)]
+    sol.adj_backward(dev(gs), dev(gu), dev(gb), *o)
+    torch.cuda.synchronize()
+    return [host(x) for x in o]
+
+
+def jvp(sol, vs, vu, vb):
+    import torch
+    o = [torch.zeros_like(dev(x)) for x in (vs, vu, vb)]
+    sol.tangent(dev(vs), dev(vu), dev(vb), *o)
+    torch.cuda.synchronize()
+    return [host(x) for x in o]
+
+
+def replay(sol, s, u, b):
+    import torch
+    o = [torch.zeros_like(dev(x)) for x in (s, u, b)]
+    sol.adj_replay(dev(s), dev(u), dev(b), *o)
+    torch.cuda.synchronize()
+    return [host(x) for x in o]
+
+
+def dot(a, b):
+    return sum(float((x * y).sum()) for x, y in zip(a, b))
+
+
+def test_replay_reproduces_the_recorded_run(cuda):
+    cfg, sol, U0, Uf = setup()
+    R = replay(sol, *U0)
+    for x, y in zip(R, Uf):
+        assert np.array_equal(x, y)
+    sol.close()
+
+
+def test_tangent_adjoint_dot_product(cuda):
+    cfg, sol, U0, _ = setup()
+    rng = np.random.default_rng(1)
+    lam = [rng.standard_normal(x.shape) for x in U0]
+    v = [rng.standard_normal(x.shape) for x in U0]
+    Jv = jvp(sol, *v)
+    JTl = vjp(sol, *lam)
+    a, b = dot(lam, Jv), dot(JTl, v)
+    assert abs(a - b) <= 1e-10 * max(abs(a), abs(b)), (a, b)
+    sol.close()
+
+
+def test_gradient_matches_central_differences(cuda):
+    N, n = 48, 16
+    cfg, sol, U0, Uf = setup(N, n, 5)
+    s0, u0, b0 = U0
+    # target: the same map from a seeded 1 % perturbation of the initial velocity
+    rng = np.random.default_rng(20261203)
+    ut = u0 * (1.0 + 0.01 * rng.uniform(-1.0, 1.0, u0.shape))
+    rho_t = replay(sol, s0, ut, b0)[0][:, 0]
+
+    def loss(U):
+        r = replay(sol, *U)[0][:, 0]
+        return 0.5 * float(((r - rho_t) ** 2).sum())
+
+    gs = np.zeros_like(s0)
+    gs[:, 0] = Uf[0][:, 0] - rho_t
+    grad = vjp(sol, gs, np.zeros_like(u0), np.zeros_like(b0))
+    for k in range(8):
+        d = [rng.standard_normal(x.shape) for x in U0]
+        nrm = np.sqrt(sum(float((x * x).sum()) for x in d))
+        d = [x / nrm for x in d]
+        eps = 1e-5
+        Lp = loss([x + eps * y for x, y in zip(U0, d)])
+        Lm = loss([x - eps * y for x, y in zip(U0, d)])
+        fd = (Lp - Lm) / (2 * eps)
+        ad = dot(grad, d)
+        assert abs(fd - ad) <= 1e-6 * max(abs(fd), abs(ad)), (k, fd, ad)
+    sol.close()
+
+
+def test_gradient_independent_of_checkpoint_interval(cuda):
+    rng = np.random.default_rng(3)
+    grads = []
+    for every in (1, 4, 12):
+        cfg, sol, U0, _ = setup(40, 12, every)
+        lam = [np.random.default_rng(3).standard_normal(x.shape) for x in U0]
+        grads.append(vjp(sol, *lam))
+        sol.close()
+    for gr in grads[1:]:
+        for x, y in zip(gr, grads[0]):
+            assert np.array_equal(x, y)
+
+
+def test_unsupported_configurations(cuda):
+    cfg, s, u, b = problems.sod(32, 32)
+    sol = g.Solver(cfg)
+    with pytest.raises(g.GdError) as e:
+        sol.adj_forward(3, 1)
+    assert e.value.status == 5
+    sol.close()
