@@ -724,7 +724,11 @@ struct AdjSmem {
     double qby[NF][NYF][ATX];
 };
 
-__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// periodic index for any i (tiles past the last cell of a grid read their periodic images)
+__device__ __forceinline__ int wrap(int i, int n) {
+    const int r = i % n;
+    return r < 0 ? r + n : r;
+}
 
 // minmod slope and which difference it took: +1 right (c_{+1} - c), -1 left (c - c_{-1}), 0
 __device__ __forceinline__ double slope_sel(double cm, double c, double cp, int& sel) {
