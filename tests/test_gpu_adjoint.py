@@ -8,7 +8,13 @@ state after `pre` steps, where the fields vary smoothly.  Checks:
   * dot-product identity <lam, J v> = <J^T lam, v> between the forward-mode tangent kernel
     and the reverse sweep (both hand-written), relative difference <= 1e-10;
   * the gradient of L = 1/2 sum (rho_n - rho_target)^2 against FP64 central finite
-    differences of the same map on random directions, relative difference <= 1e-6;
+    differences of the same map on random directions, relative difference <= 1e-6.  The
+    TVD map is only piecewise smooth: where a minmod choice switches inside +-eps the
+    central difference straddles a kink and is not the derivative the adjoint computes
+    (measured: errors ~1e-3 at eps >= 1e-6, ~1e-8 at 1e-7, rounding-dominated below 1e-8).
+    The check uses eps = 1e-7 and, for a direction whose difference exceeds the bound,
+    repeats at eps/2 and eps/4, taking the closest -- the switch leaves the stencil as eps
+    shrinks, a wrong derivative would not;
   * the gradient does not depend on the checkpoint interval (bit-identical).
 """
 import numpy as np
@@ -111,12 +117,16 @@ def test_gradient_matches_central_differences(cuda):
         d = [rng.standard_normal(x.shape) for x in U0]
         nrm = np.sqrt(sum(float((x * x).sum()) for x in d))
         d = [x / nrm for x in d]
-        eps = 1e-5
-        Lp = loss([x + eps * y for x, y in zip(U0, d)])
-        Lm = loss([x - eps * y for x, y in zip(U0, d)])
-        fd = (Lp - Lm) / (2 * eps)
         ad = dot(grad, d)
-        assert abs(fd - ad) <= 1e-6 * max(abs(fd), abs(ad)), (k, fd, ad)
+        best = None
+        for eps in (1e-7, 5e-8, 2.5e-8):
+            Lp = loss([x + eps * y for x, y in zip(U0, d)])
+            Lm = loss([x - eps * y for x, y in zip(U0, d)])
+            err = abs((Lp - Lm) / (2 * eps) - ad) / abs(ad)
+            best = err if best is None else min(best, err)
+            if best <= 1e-6:
+                break
+        assert best <= 1e-6, (k, best)
     sol.close()
 
 
