@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -249,6 +250,196 @@ def measure_batched(g, torch, steps, ngrids=512):
     bad = sum(b.stats(k, allow_nonfinite=True).nonfinite for k in range(ngrids))
     res["nonfinite_cells"] = bad
     b.close()
+    return res
+
+
+class AdjointHarness:
+    """One Orszag-Tang grid with its solver and the device-side helpers of the gradient
+    checks (device tensors in the reference AoS layout)."""
+
+    def __init__(self, g, torch, N):
+        from golikov_2d_gb300 import problems
+        self.torch = torch
+        self.cfg, s, u, b = problems.orszag_tang(N, N)
+        self.sol = g.Solver(self.cfg)
+        self.U_ic = [self.dev(x) for x in (s, u, b)]
+
+    def dev(self, a):
+        return self.torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+    def zeros(self, U):
+        return [self.torch.zeros_like(x) for x in U]
+
+    def start(self, U, steps=0):
+        self.sol.import_state(*U)
+        self.sol.set_time(0.0, 0.0)
+        self.sol.init_dt()
+        if steps:
+            self.sol.advance(steps)
+
+    def state(self):
+        out = self.zeros(self.U_ic)
+        self.sol.export_state(*out)
+        return out
+
+    def replay(self, U):
+        o = self.zeros(U)
+        self.sol.adj_replay(*U, *o)
+        return o
+
+    def jvp(self, V):
+        o = self.zeros(V)
+        self.sol.tangent(*V, *o)
+        return o
+
+    def target_density(self, U, n):
+        """Final density of the target run: its own run (own CFL dt sequence) of n steps from
+        U with the velocity perturbed by a seeded 1 % per-cell factor."""
+        rng = np.random.default_rng(20261203)
+        pert = self.dev(1.0 + 0.01 * rng.uniform(-1.0, 1.0, tuple(U[1].shape)))
+        self.start([U[0], U[1] * pert, U[2]])
+        self.sol.advance(n)
+        return self.state()[0][:, 0].clone()
+
+    def gradient(self, U0, n, every):
+        """Records n steps from U0 and returns (grad, G, rho_t) of
+        L = 1/2 |rho_n - rho_target|^2."""
+        rho_t = self.target_density(U0, n)
+        self.start(U0)
+        self.sol.adj_forward(n, every)
+        Uf = self.state()
+        G = self.zeros(U0)
+        G[0][:, 0] = Uf[0][:, 0] - rho_t
+        grad = self.zeros(U0)
+        self.sol.adj_backward(*G, *grad)
+        return grad, G, rho_t
+
+    def fd_window(self, U0, n, every, ndir, label, bound=None):
+        """Gradient of the n-step loss from U0 against central differences and the tangent
+        on `ndir` seeded random unit directions.  The difference quotient is formed per cell,
+        (L+ - L-) = sum (r+ - r-) ((r+ + r-) / 2 - t), exact algebra that keeps the
+        cancellation in the per-cell differences.  A step that straddles a minmod switch or
+        a clamp is not the derivative of the active branch; such a direction is retaken at
+        eps / 10 and eps / 100 and the closest quotient kept (a wrong derivative stays wrong
+        at every eps)."""
+        grad, G, rho_t = self.gradient(U0, n, every)
+        f0 = self.sol.stats(allow_nonfinite=True).p_floor_hits
+        fd_rel, tan_rel, eps_used, first = [], [], [], []
+        rng = np.random.default_rng(11)
+        for _ in range(ndir):
+            d = [self.dev(rng.standard_normal(tuple(x.shape))) for x in U0]
+            nrm = math.sqrt(sum(float((x * x).sum()) for x in d))
+            d = [x / nrm for x in d]
+            ad = sum(float((x * y).sum()) for x, y in zip(grad, d))
+            tn = float((G[0][:, 0] * self.jvp(d)[0][:, 0]).sum())
+            tan_rel.append(abs(ad - tn) / abs(ad))
+            best, beps = None, None
+            for eps in (1e-7, 1e-8, 1e-9):
+                rp = self.replay([x + eps * y for x, y in zip(U0, d)])[0][:, 0]
+                rm = self.replay([x - eps * y for x, y in zip(U0, d)])[0][:, 0]
+                fd = float(((rp - rm) * (0.5 * (rp + rm) - rho_t)).sum()) / (2 * eps)
+                err = abs(fd - ad) / abs(ad)
+                if best is None:
+                    first.append(err)
+                if best is None or err < best:
+                    best, beps = err, eps
+                if best <= 1e-6:
+                    break
+            fd_rel.append(best)
+            eps_used.append(beps)
+        self.start(U0)            # pressure clamps inside the window: a plain run
+        self.sol.advance(n)
+        floors = self.sol.stats(allow_nonfinite=True).p_floor_hits - f0
+        out = {"grid": f"{self.cfg.N}x{self.cfg.M}", "start": label, "steps": n,
+               "ckpt_every": every, "directions": ndir,
+               "p_floor_clamps_in_window": int(floors),
+               "max_rel": max(fd_rel), "median_rel": float(np.median(fd_rel)),
+               "max_rel_at_eps_1e-7": max(first),
+               "eps_counts": {f"{e:g}": eps_used.count(e) for e in sorted(set(eps_used))},
+               "tangent_max_rel": max(tan_rel)}
+        if bound is not None:
+            out.update({"bound": bound, "pass": max(fd_rel) <= bound})
+        return out
+
+    def close(self):
+        self.sol.close()
+
+
+def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=20,
+                    fd_N=64, fd_steps=30):
+    """Orszag-Tang MHD N x N, HLLD + minmod, `nsteps` steps with checkpoints every `every`;
+    loss = 1/2 |rho_n - rho_target|^2, the target being the final density of its own run
+    from a seeded 1 % per-cell perturbation of the initial velocity.  Reports
+
+    * the cost of one gradient (checkpointed forward + backward) against the plain forward
+      run of the same steps;
+    * the gradient against the hand-written tangent kernel (forward mode) on the measured
+      problem itself, on `ntan` seeded random directions: both differentiate the branch the
+      values take, so they agree to rounding even on the kinks below;
+    * the gradient against FP64 central differences on `ndir` seeded random unit
+      directions.  The map is piecewise smooth: minmod switches (|l| against |r|, signs),
+      the Orszag-Tang initial state itself (rho and p uniform: minmod(0, 0)) and, from step
+      59 on the 512 grid, the clamp p <= 0 -> 1e-6.  A difference quotient whose +-eps
+      straddles a switch is not the derivative; in a smooth field the |l| / |r| comparison
+      sits within ~1e-5 of switching in many cells, so on the 512 grid a unit direction
+      crosses switches at every eps that rounding allows.  The bounded check (1e-6) runs on
+      the same problem at `fd_N` (state after `pre` steps, `fd_steps` steps), where the
+      quotient resolves; the 512 windows are reported beside it."""
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z)
+
+    H = AdjointHarness(g, torch, N)
+    sol, U_ic = H.sol, H.U_ic
+    res = {"workload": f"Orszag-Tang MHD {N}x{N}, HLLD + minmod, FP64, {nsteps} steps, "
+                       f"checkpoints every {every}", "nsteps": nsteps, "ckpt_every": every}
+
+    # --- cost: plain forward run vs gradient (checkpointed forward + backward) ---------------
+    H.start(U_ic)
+    sol.advance(3)
+    H.start(U_ic)
+    ms_fwd = timed(lambda: sol.advance(nsteps))
+    grad, G, _ = H.gradient(U_ic, nsteps, every)      # also warms the backward kernels
+    l0 = sol.launch_count()
+    H.start(U_ic)
+    ms_rec = timed(lambda: sol.adj_forward(nsteps, every))
+    ms_bwd = timed(lambda: sol.adj_backward(*G, *grad))
+    res.update({"forward_ms": ms_fwd, "forward_ms_per_step": ms_fwd / nsteps,
+                "record_ms": ms_rec, "backward_ms": ms_bwd,
+                "gradient_ms": ms_rec + ms_bwd,
+                "gradient_cost_vs_forward": (ms_rec + ms_bwd) / ms_fwd,
+                "backward_cost_vs_forward": ms_bwd / ms_fwd,
+                "gpu_launches": sol.launch_count() - l0})
+
+    # --- tangent vs adjoint on the measured problem ------------------------------------------
+    rng = np.random.default_rng(7)
+    rel = []
+    for _ in range(ntan):
+        d = [H.dev(rng.standard_normal(tuple(x.shape))) for x in U_ic]
+        ad = sum(float((x * y).sum()) for x, y in zip(grad, d))
+        tn = float((G[0][:, 0] * H.jvp(d)[0][:, 0]).sum())
+        rel.append(abs(ad - tn) / max(abs(ad), abs(tn)))
+    res["tangent_vs_adjoint"] = {"directions": ntan, "max_rel": max(rel)}
+
+    # --- central differences -------------------------------------------------------------------
+    label = f"Orszag-Tang state after {pre} steps"
+    Hs = AdjointHarness(g, torch, fd_N)
+    Hs.start(Hs.U_ic, pre)
+    res["central_differences"] = Hs.fd_window(Hs.state(), fd_steps, every, ndir, label,
+                                              bound=1e-6)
+    Hs.close()
+    H.start(U_ic, pre)
+    U0 = H.state()
+    res["central_differences_512"] = [H.fd_window(U0, n, every, ndir // 4, label)
+                                      for n in (fd_steps, nsteps)]
+    H.close()
     return res
 
 
@@ -485,6 +676,11 @@ def run_gb300(args):
             line["batched"] = measure_batched(g, torch, min(args.steps, 100))
         except Exception as e:
             line["batched"] = {"unavailable": str(e)}
+    if args.adjoint:
+        try:
+            line["adjoint"] = measure_adjoint(g, torch)
+        except Exception as e:
+            line["adjoint"] = {"unavailable": str(e)}
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args.workload, cfg, s, u, b)
     print(json.dumps(line), flush=True)
@@ -503,6 +699,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--secondary", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--adjoint", type=int, default=1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -4,8 +4,9 @@
 // Checkpointing: the forward run stores the state every `ckpt_every` steps and the dt of
 // every step.  The backward sweep walks the segments from last to first; each segment is
 // recomputed once from its checkpoint (storing each step's input state and the flux
-// differences / Powell term the update used), then stepped back in reverse.  Memory is
-// O(nsteps / every + every) states instead of O(nsteps).
+// differences / Powell term the update used), then stepped back in reverse.  The last
+// segment is recorded that way during the forward run itself, so it is not recomputed.
+// Memory is O(nsteps / every + every) states instead of O(nsteps).
 #include <cstring>
 #include <new>
 
@@ -65,35 +66,63 @@ extern "C" {
 gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stream) {
     if (!ctx || nsteps < 1 || ckpt_every < 1) return GD_ERR_INVALID_ARG;
     if (!adj_supported(ctx)) return GD_ERR_UNSUPPORTED;
-    gd::adj_free(ctx);
-    gd::AdjStore* a = new (std::nothrow) gd::AdjStore();
-    if (!a) return GD_ERR_INVALID_ARG;
-    ctx->adj = a;
     const long long K = ctx->K;
     const int nf = ctx->nf;
     const int every = ckpt_every < nsteps ? ckpt_every : nsteps;
-    a->nsteps = nsteps;
-    a->every = every;
-    a->nckpt = (nsteps + every - 1) / every;
     const size_t state = sizeof(double) * (size_t)nf * K;
-    GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
-    GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
-    GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
-    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
-    GD_TRY(cudaMalloc(&a->lam, 2 * state));
-    GD_TRY(cudaMalloc(&a->scratch, sizeof(double) * 15 * (size_t)K));
-    GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
-    GD_TRY(gd::prepare_adjoint());
+    gd::AdjStore* a = ctx->adj;
+    if (!a || a->nsteps != nsteps || a->every != every) {
+        // (re)allocate only when the recording's shape changes; a repeated recording of the
+        // same length reuses the store, so a gradient loop allocates once
+        gd::adj_free(ctx);
+        a = new (std::nothrow) gd::AdjStore();
+        if (!a) return GD_ERR_INVALID_ARG;
+        ctx->adj = a;
+        a->nsteps = nsteps;
+        a->every = every;
+        a->nckpt = (nsteps + every - 1) / every;
+        GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
+        GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
+        GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
+        GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
+        GD_TRY(cudaMalloc(&a->lam, 2 * state));
+        GD_TRY(cudaMalloc(&a->scratch,
+                          sizeof(double) * (size_t)gd::adjoint_scratch_planes() * (size_t)K));
+        GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
+        GD_TRY(gd::prepare_adjoint());
+    }
     cudaStream_t st = (cudaStream_t)stream;
+    // The last segment is stepped out of `seg` with the update terms stored, so the backward
+    // sweep starts reversing at once instead of recomputing it.
+    const int k_last = (a->nckpt - 1) * every;
+    a->seg_holds = -1;
     for (int s = 0; s < nsteps; ++s) {
         if (s % every == 0)
             GD_TRY(cudaMemcpyAsync(a->ckpt + (size_t)(s / every) * nf * K, ctx->state[ctx->cur],
                                    state, cudaMemcpyDeviceToDevice, st));
         GD_TRY(cudaMemcpyAsync(a->dts + s, &ctx->sc->T_do, sizeof(double),
                                cudaMemcpyDeviceToDevice, st));
-        const gd_status r = gd_advance(ctx, 1, 0, stream);
-        if (r != GD_OK) return r;
+        if (s < k_last) {
+            const gd_status r = gd_advance(ctx, 1, 0, stream);
+            if (r != GD_OK) return r;
+            continue;
+        }
+        // the same step as gd_advance (dt rotation and counters included), reading its input
+        // from seg[j] and writing its output to seg[j + 1]
+        const int j = s - k_last;
+        if (j == 0)
+            GD_TRY(cudaMemcpyAsync(a->seg, ctx->state[ctx->cur], state, cudaMemcpyDeviceToDevice,
+                                   st));
+        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
+                                       planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
+                                       &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc, ctx->sc,
+                                       a->aux + (size_t)j * 8 * K, st));
+        ctx->launches += 1;
     }
+    // the final state back into the context
+    GD_TRY(cudaMemcpyAsync(ctx->state[ctx->cur], a->seg + (size_t)(nsteps - k_last) * nf * K,
+                           state, cudaMemcpyDeviceToDevice, st));
+    a->seg_holds = a->nckpt - 1;
     return GD_OK;
 }
 
@@ -113,15 +142,19 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
         const int k0 = sg * a->every;
         const int k1 = k0 + a->every < a->nsteps ? k0 + a->every : a->nsteps;
         const int len = k1 - k0;
-        // recompute the segment: input states and update terms of every step
-        GD_TRY(cudaMemcpyAsync(a->seg, a->ckpt + (size_t)sg * nf * K, state,
-                               cudaMemcpyDeviceToDevice, st));
-        for (int j = 0; j < len; ++j) {
-            GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
-                                           planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
-                                           a->dts + k0 + j, (unsigned long long*)a->tbits,
-                                           a->aux + (size_t)j * 8 * K, st));
-            ctx->launches += 1;
+        // recompute the segment (input states and update terms of every step) unless seg/aux
+        // already hold it
+        if (a->seg_holds != sg) {
+            GD_TRY(cudaMemcpyAsync(a->seg, a->ckpt + (size_t)sg * nf * K, state,
+                                   cudaMemcpyDeviceToDevice, st));
+            for (int j = 0; j < len; ++j) {
+                GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
+                                               planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
+                                               a->dts + k0 + j, (unsigned long long*)a->tbits,
+                                               nullptr, nullptr, a->aux + (size_t)j * 8 * K, st));
+                ctx->launches += 1;
+            }
+            a->seg_holds = sg;
         }
         // reverse through the segment
         for (int j = len - 1; j >= 0; --j) {
@@ -129,7 +162,7 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
                                            a->aux + (size_t)j * 8 * K, cplanes_at(lam[c], nf, K),
                                            planes_at(lam[c ^ 1], nf, K), a->scratch,
                                            a->dts + k0 + j, st));
-            ctx->launches += 2;
+            ctx->launches += 3;
             c ^= 1;
         }
     }
@@ -147,6 +180,7 @@ gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const doub
     const size_t state = sizeof(double) * (size_t)nf * K;
     double* t[2] = {a->lam, a->lam + (size_t)nf * K};
     double* u[2] = {a->seg, a->seg + (size_t)nf * K};
+    a->seg_holds = -1;  // seg is the work space of this sweep
     GD_TRY(gd::launch_aos_to_soa(vs, vu, vb, planes_at(t[0], nf, K), K, nf, st));
     GD_TRY(cudaMemcpyAsync(u[0], a->ckpt, state, cudaMemcpyDeviceToDevice, st));
     int c = 0;
@@ -169,11 +203,13 @@ gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const dou
     const int nf = ctx->nf;
     cudaStream_t st = (cudaStream_t)stream;
     double* w[2] = {a->seg, a->seg + (size_t)nf * K};
+    a->seg_holds = -1;  // seg is the work space of this sweep
     GD_TRY(gd::launch_aos_to_soa(s, u, b, planes_at(w[0], nf, K), K, nf, st));
     int c = 0;
     for (int k = 0; k < a->nsteps; ++k) {
         GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(w[c], nf, K), planes_at(w[c ^ 1], nf, K),
-                                       a->dts + k, (unsigned long long*)a->tbits, nullptr, st));
+                                       a->dts + k, (unsigned long long*)a->tbits, nullptr,
+                                       nullptr, nullptr, st));
         ctx->launches += 1;
         c ^= 1;
     }

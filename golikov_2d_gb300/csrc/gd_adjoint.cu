@@ -10,8 +10,8 @@
 //      forward flux differences d[7] and the Powell term divb of that cell (stored by the
 //      recompute pass), lambda'.  Outputs: the direct adjoint of the cell state, the adjoint
 //      of d[7] and of divb.
-//   B  per tile (adj_faces_kernel): every face touching the tile's stencil recomputes its
-//      forward states and HLLD flux and runs the flux's reverse sweep on
+//   B  per face, then per cell (adj_face_kernel, adj_gather_kernel): every face recomputes
+//      its forward states and HLLD flux once and runs the flux's reverse sweep on
 //      Fbar = k (dbar_low - dbar_high); the adjoints of the two face states are gathered
 //      into the cells through the reconstruction (c +- slope/2, minmod choice, rho/p
 //      fallback) and the Powell central difference, in a fixed order (deterministic).
@@ -40,8 +40,9 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
          k += (long long)gridDim.x * blockDim.x) {
         const double r = U.f[0][k], p = U.f[1][k], u = U.f[2][k], v = U.f[3][k];
-        const double bx = U.f[4][k] * kInvSpi4, by = U.f[5][k] * kInvSpi4;
-        const double bz = U.f[6][k] * kInvSpi4;
+        // rounded products, as the forward update has them (see ld_b)
+        const double bx = __dmul_rn(U.f[4][k], kInvSpi4), by = __dmul_rn(U.f[5][k], kInvSpi4);
+        const double bz = __dmul_rn(U.f[6][k], kInvSpi4);
         double d[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) d[f] = aux[(size_t)f * K + k];
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
 // ---------------------------------------------------------------------------------------
 struct SideV {
     double r, p, un, ut, bn, bt, bz;
-    double bn2, bb, pT, kin, E, gp, a, disc, sq, X, rs, cf;
+    double bn2, bb, pT, kin, E, gp, a, disc, rq, X, rs, cf;  // rq = 1 / sqrt(disc)
     double F0, F1, F2, F4, F6, F7;
     bool disc0;
 };
@@ -161,8 +162,10 @@ __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params
     double disc = fma(S.a, S.a, -4.0 * S.gp * S.bn2);
     S.disc0 = le_zero(disc);
     S.disc = S.disc0 ? 0.0 : disc;
-    S.sq = sqrt_fast(S.disc);
-    S.X = 0.5 * (S.a + S.sq);
+    // sqrt_fast(disc) = disc * rsqrt_fast(disc), kept apart so the reverse reuses 1/sqrt
+    S.rq = rsqrt_fast(S.disc);
+    const double sq = S.disc == 0.0 ? 0.0 : S.disc * S.rq;
+    S.X = 0.5 * (S.a + sq);
     S.rs = rsqrt_fast(S.X * S.r);
     S.cf = S.X * S.rs;
     S.F0 = S.r * S.un;
@@ -225,8 +228,8 @@ __device__ __forceinline__ void side_rev(const SideV& S, SideB& b, const Params&
     double ab = 0.5 * Xb, sqb = 0.5 * Xb;
     // sq = sqrt(disc), disc = a^2 - 4 gp bn^2 (clamped at 0)
     double gpb = 0.0, bn2b = 0.0;
-    if (!S.disc0 && S.sq > 0.0) {
-        const double discb = sqb * 0.5 / S.sq;
+    if (!S.disc0 && S.disc != 0.0) {
+        const double discb = sqb * 0.5 * S.rq;
         ab += discb * 2.0 * S.a;
         gpb -= discb * 4.0 * S.bn2;
         bn2b -= discb * 4.0 * S.gp;
@@ -706,28 +709,46 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
 }
 
 // ---------------------------------------------------------------------------------------
-// Pass B: face adjoints and the gather into cells.
+// Pass B: face adjoints (each face once), then the gather into cells.
+//
+// B1 adj_face_kernel: one thread per face.  It reconstructs the face's two states from the
+// four cells along its normal, recomputes the HLLD flux and runs its reverse sweep on
+// Fbar = k (dbar_low - dbar_high).  The adjoint of the low-side state (the upper face state
+// of the low cell) goes to that cell's "up" plane, the adjoint of the high-side state (the
+// lower face state of the high cell) to that cell's "dn" plane: every entry has exactly one
+// writer.  The face thread also records, before its reverse sweep, the reconstruction
+// choices of its two cells in bytes: for the low cell the minmod choice of its slope and
+// whether its upper face state fell back to the cell value (rho, p), for the high cell
+// whether its lower face state fell back (a fallback face state does not depend on the slope).
+// Scratch layout after the 15 pass-A planes:
+//   kFaceAdj + (dir * 2 + side) * 7 + f         face-state adjoints, side 0 = up, 1 = dn
+//   kSel bytes, (dir * 7 + f) * K + cell        (choice + 1) | upper fallback << 2,
+//                                               choice -1 left, +1 right, 0 none
+//   kSel bytes, 14 K + (dir * 2 + f) * K + cell lower fallback (f < 2)
+// dir 0 = x, 1 = y.
+// B2 adj_gather_kernel: one thread per cell.  The cell's state adjoint collects the value
+// parts of its two face states per direction, its own slope adjoint through its minmod
+// choice, its neighbours' slope adjoints where their minmod choice used it, and the Powell
+// terms of its neighbours, in a fixed order (deterministic).
 // ---------------------------------------------------------------------------------------
-constexpr int HU = 3;  // halo of the state tile (cells needed by the slopes of halo faces)
-constexpr int HD = 2;  // halo of the dbar tile
-constexpr int USX = ATX + 2 * HU, USY = ATY + 2 * HU;
-constexpr int DSX = ATX + 2 * HD, DSY = ATY + 2 * HD;
-constexpr int NXF = ATX + 3;  // x-faces per row: between cells x0-2 | x0-1 ... x0+TX | x0+TX+1
-constexpr int NYF = ATY + 3;
+constexpr int kFaceAdj = 15;
+constexpr int kSel = kFaceAdj + 4 * NF;
+constexpr int kScratchPlanes = kSel + 3;  // 18 bytes per cell fit in three planes of doubles
+constexpr int FBX = 32, FBY = 4;  // 128-thread blocks of both kernels
 
-struct AdjSmem {
-    double U[NF][USY][USX];       // state (b units), cross-shaped halo 3
-    double Db[NF][DSY][DSX];      // dbar, cross-shaped halo 2
-    double qax[NF][ATY][NXF];     // adjoint of the low-side face state, x-faces
-    double qbx[NF][ATY][NXF];     // adjoint of the high-side face state, x-faces
-    double qay[NF][NYF][ATX];
-    double qby[NF][NYF][ATX];
-};
-
-// periodic index for any i (tiles past the last cell of a grid read their periodic images)
+// periodic index for any i
 __device__ __forceinline__ int wrap(int i, int n) {
     const int r = i % n;
     return r < 0 ? r + n : r;
+}
+
+// state value in b units (the field is stored in Gaussian units).  The product is rounded
+// on its own (__dmul_rn: never fused into a later add), as the forward kernel rounds it when
+// it stages the tile: equal neighbours then give an exact zero difference, and the minmod
+// choices here are the forward's.
+__device__ __forceinline__ double ld_b(const CPlanes& U, int f, long long k) {
+    const double v = __ldg(U.f[f] + k);
+    return f >= 4 ? __dmul_rn(v, kInvSpi4) : v;
 }
 
 // minmod slope and which difference it took: +1 right (c_{+1} - c), -1 left (c - c_{-1}), 0
@@ -738,179 +759,145 @@ __device__ __forceinline__ double slope_sel(double cm, double c, double cp, int&
     return s;
 }
 
-__global__ void __launch_bounds__(NT) adj_faces_kernel(Params P, CPlanes U, const double* scratch,
-                                                       Planes lam_in,
-                                                       const double* __restrict__ T_do_ptr) {
-    extern __shared__ __align__(16) double smem_raw[];
-    AdjSmem& sm = *reinterpret_cast<AdjSmem*>(smem_raw);
-    const int tid = threadIdx.x;
+__global__ void __launch_bounds__(FBX * FBY) adj_face_kernel(Params P, CPlanes U, double* scratch,
+                                                             const double* __restrict__ T_do_ptr) {
     const int N = P.N, M = P.M;
     const long long K = (long long)N * M;
-    const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
+    const bool isx = blockIdx.z == 0;
+    const int ix = blockIdx.x * FBX + threadIdx.x;  // x-face index (x) or column (y)
+    const int iy = blockIdx.y * FBY + threadIdx.y;  // row (x) or y-face index (y)
+    if (ix >= N || iy >= M) return;
+    const double T_do = *T_do_ptr;
+    const double kk = isx ? T_do / P.dx : T_do / P.dy;
+    // the face lies between cells a-1 and a along its normal; cells a-2 .. a+1
+    long long kc[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+        kc[t] = isx ? (long long)iy * N + wrap(ix - 2 + t, N)
+                    : (long long)wrap(iy - 2 + t, M) * N + ix;
+    double c[4][NF];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) c[t][f] = ld_b(U, f, kc[t]);
+    // face states: low cell (t=1) + its slope / 2, high cell (t=2) - its slope / 2
+    double qa[NF], qb[NF];
+    unsigned char* rec = reinterpret_cast<unsigned char*>(scratch + (size_t)kSel * K);
+    unsigned char* sel = rec + (size_t)(isx ? 0 : NF) * K;
+    unsigned char* fbl = rec + (size_t)(2 * NF + (isx ? 0 : 2)) * K;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        int sa, sb_;
+        const double da = slope_sel(c[0][f], c[1][f], c[2][f], sa);
+        const double db = slope_sel(c[1][f], c[2][f], c[3][f], sb_);
+        const double va = fma(0.5, da, c[1][f]), vb = fma(-0.5, db, c[2][f]);
+        const bool fu = f < 2 && le_zero(va), fd = f < 2 && le_zero(vb);
+        qa[f] = fu ? c[1][f] : va;
+        qb[f] = fd ? c[2][f] : vb;
+        sel[(size_t)f * K + kc[1]] = (unsigned char)((sa + 1) | (fu ? 4 : 0));  // low cell
+        if (f < 2) fbl[(size_t)f * K + kc[2]] = fd ? 1 : 0;                   // high cell
+    }
+    // flux adjoint: d_low += k F, d_high -= k F
+    double Fslot[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+        Fslot[f] = kk * (scratch[(size_t)(7 + f) * K + kc[1]] - scratch[(size_t)(7 + f) * K + kc[2]]);
+    // slots: 0 m, 1 e, 2 mx, 3 my, 4 bx, 5 by, 6 bz -> local (m, mn, mt, e, bn, bt, bz)
+    const double Fb[7] = {Fslot[0], isx ? Fslot[2] : Fslot[3], isx ? Fslot[3] : Fslot[2],
+                          Fslot[1], isx ? Fslot[4] : Fslot[5], isx ? Fslot[5] : Fslot[4],
+                          Fslot[6]};
+    const double la[7] = {qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
+                          isx ? qa[4] : qa[5], isx ? qa[5] : qa[4], qa[6]};
+    const double lb[7] = {qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2],
+                          isx ? qb[4] : qb[5], isx ? qb[5] : qb[4], qb[6]};
+    double lab[7] = {0, 0, 0, 0, 0, 0, 0}, lbb[7] = {0, 0, 0, 0, 0, 0, 0};
+    hlld_vjp(la, lb, Fb, P, lab, lbb);
+    // back to field order (rho, p, vx, vy, bx, by, bz)
+    const double gab[7] = {lab[0], lab[1], isx ? lab[2] : lab[3], isx ? lab[3] : lab[2],
+                           isx ? lab[4] : lab[5], isx ? lab[5] : lab[4], lab[6]};
+    const double gbb[7] = {lbb[0], lbb[1], isx ? lbb[2] : lbb[3], isx ? lbb[3] : lbb[2],
+                           isx ? lbb[4] : lbb[5], isx ? lbb[5] : lbb[4], lbb[6]};
+    double* up = scratch + (size_t)(kFaceAdj + (isx ? 0 : 2) * NF) * K;
+    double* dn = up + (size_t)NF * K;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        up[(size_t)f * K + kc[1]] = gab[f];
+        dn[(size_t)f * K + kc[2]] = gbb[f];
+    }
+}
+
+__global__ void __launch_bounds__(FBX * FBY) adj_gather_kernel(Params P,
+                                                               const double* __restrict__ scratch,
+                                                               Planes lam_in,
+                                                               const double* __restrict__ T_do_ptr) {
+    const int N = P.N, M = P.M;
+    const long long K = (long long)N * M;
+    const int gx = blockIdx.x * FBX + threadIdx.x, gy = blockIdx.y * FBY + threadIdx.y;
+    if (gx >= N || gy >= M) return;
+    const long long k = (long long)gy * N + gx;
     const double T_do = *T_do_ptr;
     const double kx = T_do / P.dx, ky = T_do / P.dy;
-
-    // ---- load U (cross halo HU) and dbar (cross halo HD), periodic wrap ---------------------
-    for (int i = tid; i < USY * USX; i += NT) {
-        const int ly = i / USX, lx = i - ly * USX;
-        const bool xh = lx < HU || lx >= ATX + HU, yh = ly < HU || ly >= ATY + HU;
-        if (xh && yh) continue;
-        const int gx = wrap(x0 + lx - HU, N), gy = wrap(y0 + ly - HU, M);
-        const long long k = (long long)gy * N + gx;
+    double lam[NF];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) sm.U[f][ly][lx] = U.f[f][k] * (f >= 4 ? kInvSpi4 : 1.0);
-    }
-    for (int i = tid; i < DSY * DSX; i += NT) {
-        const int ly = i / DSX, lx = i - ly * DSX;
-        const bool xh = lx < HD || lx >= ATX + HD, yh = ly < HD || ly >= ATY + HD;
-        if (xh && yh) continue;
-        const int gx = wrap(x0 + lx - HD, N), gy = wrap(y0 + ly - HD, M);
-        const long long k = (long long)gy * N + gx;
+    for (int f = 0; f < NF; ++f) lam[f] = scratch[(size_t)f * K + k];
+    const unsigned char* rec = reinterpret_cast<const unsigned char*>(scratch + (size_t)kSel * K);
 #pragma unroll
-        for (int f = 0; f < NF; ++f) sm.Db[f][ly][lx] = scratch[(size_t)(7 + f) * K + k];
-    }
-    __syncthreads();
-
-    // ---- faces: recompute states and flux, reverse sweep ------------------------------------
-    for (int i = tid; i < NXF * ATY + NYF * ATX; i += NT) {
-        const bool isx = i < NXF * ATY;
-        int a, row;  // a: face index along the normal (face between a-1 and a, tile-local)
-        if (isx) {
-            row = i / NXF;
-            a = i - row * NXF - 1;  // x-face index in [-1, ATX+1]
-        } else {
-            const int j = i - NXF * ATY;
-            row = j / NYF;          // here: column
-            a = j - row * NYF - 1;
-        }
-        // cell values along the normal at positions a-2 .. a+1: the face's low cell a-1 and
-        // high cell a, each with the neighbour its slope needs
-        double c[4][NF];
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool isx = dir == 0;
+        // the cells at positions -1, 0, +1 along the direction
+        long long kc[3];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int pos = a - 2 + t;  // tile-local cell index along the normal, >= -3
-#pragma unroll
-            for (int f = 0; f < NF; ++f)
-                c[t][f] = isx ? sm.U[f][row + HU][pos + HU] : sm.U[f][pos + HU][row + HU];
-        }
-        // face states: low cell = pos a-1 (t=1), high cell = pos a (t=2)
-        double qa[NF], qb[NF];
+        for (int t = 0; t < 3; ++t)
+            kc[t] = isx ? (long long)gy * N + wrap(gx - 1 + t, N)
+                        : (long long)wrap(gy - 1 + t, M) * N + gx;
+        const double* up = scratch + (size_t)(kFaceAdj + 2 * dir * NF) * K;
+        const double* dn = up + (size_t)NF * K;
+        const unsigned char* sel = rec + (size_t)dir * NF * K;
+        const unsigned char* fbl = rec + (size_t)(2 * NF + 2 * dir) * K;
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            int sa, sb_;
-            const double da = slope_sel(c[0][f], c[1][f], c[2][f], sa);
-            const double db = slope_sel(c[1][f], c[2][f], c[3][f], sb_);
-            const double va = fma(0.5, da, c[1][f]), vb = fma(-0.5, db, c[2][f]);
-            qa[f] = (f < 2 && le_zero(va)) ? c[1][f] : va;
-            qb[f] = (f < 2 && le_zero(vb)) ? c[2][f] : vb;
-        }
-        // flux adjoint: d_low += k F, d_high -= k F
-        const double kk = isx ? kx : ky;
-        double Fslot[NF];
+            const double* upf = up + (size_t)f * K;
+            const double* dnf = dn + (size_t)f * K;
+            // twice the slope adjoint of cell t: up - dn of that cell, a fallback face state
+            // dropping its term; 0.5 a - 0.5 b rounds as 0.5 (a - b) (scaling by 2^-1 is
+            // exact), so the factor goes last
+            double sb2[3];
+            int s[3];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-            const double dlo = isx ? sm.Db[f][row + HD][a - 1 + HD] : sm.Db[f][a - 1 + HD][row + HD];
-            const double dhi = isx ? sm.Db[f][row + HD][a + HD] : sm.Db[f][a + HD][row + HD];
-            Fslot[f] = kk * (dlo - dhi);
-        }
-        // slots: 0 m, 1 e, 2 mx, 3 my, 4 bx, 5 by, 6 bz -> local (m, mn, mt, e, bn, bt, bz)
-        const double Fb[7] = {Fslot[0], isx ? Fslot[2] : Fslot[3], isx ? Fslot[3] : Fslot[2],
-                              Fslot[1], isx ? Fslot[4] : Fslot[5], isx ? Fslot[5] : Fslot[4],
-                              Fslot[6]};
-        const double la[7] = {qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
-                              isx ? qa[4] : qa[5], isx ? qa[5] : qa[4], qa[6]};
-        const double lb[7] = {qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2],
-                              isx ? qb[4] : qb[5], isx ? qb[5] : qb[4], qb[6]};
-        double lab[7] = {0, 0, 0, 0, 0, 0, 0}, lbb[7] = {0, 0, 0, 0, 0, 0, 0};
-        hlld_vjp(la, lb, Fb, P, lab, lbb);
-        // back to field order (rho, p, vx, vy, bx, by, bz)
-        const double gab[7] = {lab[0], lab[1], isx ? lab[2] : lab[3], isx ? lab[3] : lab[2],
-                               isx ? lab[4] : lab[5], isx ? lab[5] : lab[4], lab[6]};
-        const double gbb[7] = {lbb[0], lbb[1], isx ? lbb[2] : lbb[3], isx ? lbb[3] : lbb[2],
-                               isx ? lbb[4] : lbb[5], isx ? lbb[5] : lbb[4], lbb[6]};
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-            if (isx) {
-                sm.qax[f][row][a + 1] = gab[f];
-                sm.qbx[f][row][a + 1] = gbb[f];
-            } else {
-                sm.qay[f][a + 1][row] = gab[f];
-                sm.qby[f][a + 1][row] = gbb[f];
+            for (int t = 0; t < 3; ++t) {
+                const int b = sel[(size_t)f * K + kc[t]];
+                s[t] = (b & 3) - 1;
+                const bool fu = (b & 4) != 0;
+                const bool fd = f < 2 && fbl[(size_t)f * K + kc[t]] != 0;
+                sb2[t] = (fu ? 0.0 : upf[kc[t]]) - (fd ? 0.0 : dnf[kc[t]]);
             }
+            // value parts of the cell's two face states
+            double acc = upf[k] + dnf[k];
+            // own slope: left difference (c - c_{-1}) -> +1, right (c_{+1} - c) -> -1
+            if (s[1] != 0) acc = fma(s[1] == -1 ? 0.5 : -0.5, sb2[1], acc);
+            // neighbour -1 took its right difference (c - c_{-1})
+            if (s[0] == 1) acc = fma(0.5, sb2[0], acc);
+            // neighbour +1 took its left difference (c_{+1} - c)
+            if (s[2] == -1) acc = fma(-0.5, sb2[2], acc);
+            lam[f] += acc;
         }
     }
-    __syncthreads();
-
-    // ---- gather into the tile's cells ----------------------------------------------------------
-    // Cell c gets: the direct adjoint of its update; the face-state adjoints of its two faces
-    // (value part), its own slope adjoint through its minmod choice, and its neighbours'
-    // slope adjoints where their minmod choice used c; the Powell terms of its neighbours.
-    for (int i = tid; i < ATX * ATY; i += NT) {
-        const int ly = i / ATX, lx = i - ly * ATX;
-        const int gx = x0 + lx, gy = y0 + ly;
-        if (gx >= N || gy >= M) continue;
-        const long long k = (long long)gy * N + gx;
-        double lam[NF];
-#pragma unroll
-        for (int f = 0; f < NF; ++f) lam[f] = scratch[(size_t)f * K + k];
-        // two directions
-#pragma unroll
-        for (int dir = 0; dir < 2; ++dir) {
-            const bool isx = dir == 0;
-            const int a = isx ? lx : ly;      // position along the normal
-            const int o = isx ? ly : lx;      // row (x) or column (y)
-#pragma unroll
-            for (int f = 0; f < NF; ++f) {
-                // cell values at positions a-2 .. a+2
-                double cv[5];
-#pragma unroll
-                for (int t = 0; t < 5; ++t)
-                    cv[t] = isx ? sm.U[f][o + HU][a - 2 + t + HU] : sm.U[f][a - 2 + t + HU][o + HU];
-                // slope adjoint of the cells at positions a-1, a, a+1 (face j between j-1 and
-                // j is stored at index j+1)
-                double sb[3];
-                int sel[3];
-#pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    const int pc = a - 1 + t;
-                    const double qa_up = isx ? sm.qax[f][o][pc + 2] : sm.qay[f][pc + 2][o];
-                    const double qb_dn = isx ? sm.qbx[f][o][pc + 1] : sm.qby[f][pc + 1][o];
-                    double s = slope_sel(cv[t], cv[t + 1], cv[t + 2], sel[t]);
-                    // face states of cell pc: low side of face pc+1 (c + s/2), high side of
-                    // face pc (c - s/2); a fallback removes the slope term
-                    const bool fbu = f < 2 && le_zero(fma(0.5, s, cv[t + 1]));
-                    const bool fbd = f < 2 && le_zero(fma(-0.5, s, cv[t + 1]));
-                    sb[t] = (fbu ? 0.0 : 0.5 * qa_up) - (fbd ? 0.0 : 0.5 * qb_dn);
-                }
-                // value parts: cell a is the low side of face a+1 and the high side of face a
-                double acc = (isx ? sm.qax[f][o][a + 2] : sm.qay[f][a + 2][o]) +
-                             (isx ? sm.qbx[f][o][a + 1] : sm.qby[f][a + 1][o]);
-                // own slope: left difference (c - c_{-1}) -> +1, right (c_{+1} - c) -> -1
-                acc += sel[1] == -1 ? sb[1] : (sel[1] == 1 ? -sb[1] : 0.0);
-                // neighbour a-1 took its right difference (c_a - c_{a-1})
-                acc += sel[0] == 1 ? sb[0] : 0.0;
-                // neighbour a+1 took its left difference (c_{a+1} - c_a)
-                acc -= sel[2] == -1 ? sb[2] : 0.0;
-                lam[f] += acc;
-            }
-        }
-        // Powell: divb_c' = 0.5 kx (bx_{c'+1} - bx_{c'-1}) + 0.5 ky (by_{c'+N} - by_{c'-N})
-        {
-            const long long kW = (long long)gy * N + wrap(gx - 1, N);
-            const long long kE = (long long)gy * N + wrap(gx + 1, N);
-            const long long kS = (long long)wrap(gy - 1, M) * N + gx;
-            const long long kN = (long long)wrap(gy + 1, M) * N + gx;
-            const double* dvb = scratch + (size_t)14 * K;
-            lam[4] += 0.5 * kx * (dvb[kW] - dvb[kE]);
-            lam[5] += 0.5 * ky * (dvb[kS] - dvb[kN]);
-        }
-        // field adjoint back to the stored Gaussian units: b = B / sqrt(4 pi)
-        lam[4] *= kInvSpi4;
-        lam[5] *= kInvSpi4;
-        lam[6] *= kInvSpi4;
-#pragma unroll
-        for (int f = 0; f < NF; ++f) lam_in.f[f][k] = lam[f];
+    // Powell: divb_c' = 0.5 kx (bx_{c'+1} - bx_{c'-1}) + 0.5 ky (by_{c'+N} - by_{c'-N})
+    {
+        const long long kW = (long long)gy * N + wrap(gx - 1, N);
+        const long long kE = (long long)gy * N + wrap(gx + 1, N);
+        const long long kS = (long long)wrap(gy - 1, M) * N + gx;
+        const long long kN = (long long)wrap(gy + 1, M) * N + gx;
+        const double* dvb = scratch + (size_t)14 * K;
+        lam[4] += 0.5 * kx * (dvb[kW] - dvb[kE]);
+        lam[5] += 0.5 * ky * (dvb[kS] - dvb[kN]);
     }
+    // field adjoint back to the stored Gaussian units: b = B / sqrt(4 pi)
+    lam[4] *= kInvSpi4;
+    lam[5] *= kInvSpi4;
+    lam[6] *= kInvSpi4;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) lam_in.f[f][k] = lam[f];
 }
 
 int grid_cells(long long K) {
@@ -920,22 +907,24 @@ int grid_cells(long long K) {
 
 }  // namespace
 
-size_t adj_faces_smem_bytes() { return sizeof(AdjSmem); }
+int adjoint_scratch_planes() { return kScratchPlanes; }
 
-cudaError_t prepare_adjoint() {
-    return cudaFuncSetAttribute(adj_faces_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(AdjSmem));
-}
+cudaError_t prepare_adjoint() { return cudaSuccess; }
 
 cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
                                 const CPlanes& lam_out, const Planes& lam_in, double* scratch,
                                 const double* T_do, cudaStream_t st) {
     const long long K = (long long)P.N * P.M;
+    const dim3 blk(FBX, FBY);
+    const unsigned gxb = (unsigned)((P.N + FBX - 1) / FBX), gyb = (unsigned)((P.M + FBY - 1) / FBY);
+    if (gyb > 65535u) return cudaErrorInvalidConfiguration;
     adj_update_kernel<<<grid_cells(K), NT, 0, st>>>(P, U, aux, lam_out, scratch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    dim3 grid((P.N + ATX - 1) / ATX, (P.M + ATY - 1) / ATY);
-    adj_faces_kernel<<<grid, NT, sizeof(AdjSmem), st>>>(P, U, scratch, lam_in, T_do);
+    adj_face_kernel<<<dim3(gxb, gyb, 2), blk, 0, st>>>(P, U, scratch, T_do);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    adj_gather_kernel<<<dim3(gxb, gyb, 1), blk, 0, st>>>(P, scratch, lam_in, T_do);
     return cudaGetLastError();
 }
 

@@ -18,8 +18,9 @@ struct AdjStore {
     double* seg = nullptr;       // (every + 1) * nf * K: states of one segment
     double* aux = nullptr;       // every * 8 * K: flux differences and Powell term per step
     double* lam = nullptr;       // 2 * nf * K
-    double* scratch = nullptr;   // 15 * K
+    double* scratch = nullptr;   // adjoint_scratch_planes() * K
     double* tbits = nullptr;     // dt accumulator the recompute pass writes (unused value)
+    int seg_holds = -1;          // segment whose input states and update terms seg/aux hold
 };
 
 }  // namespace gd

@@ -620,10 +620,10 @@ cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& ou
 }
 
 cudaError_t launch_mhd_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
-                                const double* T_do, unsigned long long* T_bits, double* aux,
-                                cudaStream_t st) {
-    if (P.order == 1) return launch_t<1>(P, in, out, T_do, T_bits, nullptr, nullptr, 0, st, aux);
-    return launch_t<2>(P, in, out, T_do, T_bits, nullptr, nullptr, 0, st, aux);
+                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                Scalars* ctr, double* aux, cudaStream_t st) {
+    if (P.order == 1) return launch_t<1>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
+    return launch_t<2>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
 }
 
 cudaError_t launch_mhd_tangent(const Params& P, const CPlanes& in, const CPlanes& din,

@@ -49,13 +49,15 @@ cudaError_t launch_mhd_tangent(const Params& P, const CPlanes& in, const CPlanes
                                cudaStream_t st);
 
 // Fast MHD step that also stores, per cell, the flux differences and the Powell term the
-// update used (8 planes of N*M in `aux`), for the adjoint.  No dt rotation.
+// update used (8 planes of N*M in `aux`), for the adjoint.  `rot` / `ctr` as in
+// launch_mhd_fast (null: no dt rotation, no counters).
 cudaError_t launch_mhd_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
-                                const double* T_do, unsigned long long* T_bits, double* aux,
-                                cudaStream_t st);
+                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                Scalars* ctr, double* aux, cudaStream_t st);
 // One reverse step of the fast MHD step (HLLD, order 2, Cartesian, periodic):
 // lam_in = S'(U)^T lam_out, with U, aux of the forward step and the dt *T_do.
-// `scratch` holds 15 planes of N*M.
+// `scratch` holds adjoint_scratch_planes() planes of N*M.
+int adjoint_scratch_planes();
 cudaError_t prepare_adjoint();
 cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
                                 const CPlanes& lam_out, const Planes& lam_in, double* scratch,
