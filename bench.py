@@ -253,6 +253,25 @@ def measure_batched(g, torch, steps, ngrids=512):
     return res
 
 
+def adjoint_step_case(g, torch, N=512):
+    """A short differentiation run for kernel profiles: Orszag-Tang N x N, 20 plain steps,
+    a 10-step recording, one backward sweep and one tangent sweep."""
+    H = AdjointHarness(g, torch, N)
+    H.start(H.U_ic, 20)
+    U0 = H.state()
+    H.sol.adj_forward(10, 10)
+    rng = np.random.default_rng(1)
+    lam = [H.dev(rng.standard_normal(tuple(x.shape))) for x in U0]
+    out = H.zeros(U0)
+    H.sol.adj_backward(*lam, *out)
+    tan = H.jvp(lam)
+    torch.cuda.synchronize()
+    ok = all(bool(torch.isfinite(x).all()) for x in out + tan)
+    H.close()
+    print(json.dumps({"case": "adjoint-step", "grid": f"{N}x{N}", "finite": ok}), flush=True)
+    return 0 if ok else 1
+
+
 class AdjointHarness:
     """One Orszag-Tang grid with its solver and the device-side helpers of the gradient
     checks (device tensors in the reference AoS layout)."""
@@ -366,7 +385,7 @@ class AdjointHarness:
 
 
 def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=20,
-                    fd_N=64, fd_steps=30):
+                    fd_N=32, fd_pre=40, fd_steps=30):
     """Orszag-Tang MHD N x N, HLLD + minmod, `nsteps` steps with checkpoints every `every`;
     loss = 1/2 |rho_n - rho_target|^2, the target being the final density of its own run
     from a seeded 1 % per-cell perturbation of the initial velocity.  Reports
@@ -383,8 +402,9 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
       straddles a switch is not the derivative; in a smooth field the |l| / |r| comparison
       sits within ~1e-5 of switching in many cells, so on the 512 grid a unit direction
       crosses switches at every eps that rounding allows.  The bounded check (1e-6) runs on
-      the same problem at `fd_N` (state after `pre` steps, `fd_steps` steps), where the
-      quotient resolves; the 512 windows are reported beside it."""
+      the same problem at `fd_N` (state after `fd_pre` steps, `fd_steps` steps), where the
+      quotient resolves; windows of the 512 grid from the state after `pre` steps are
+      reported beside it."""
     stream = torch.cuda.current_stream()
 
     def timed(fn):
@@ -429,16 +449,17 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
     res["tangent_vs_adjoint"] = {"directions": ntan, "max_rel": max(rel)}
 
     # --- central differences -------------------------------------------------------------------
-    label = f"Orszag-Tang state after {pre} steps"
     Hs = AdjointHarness(g, torch, fd_N)
-    Hs.start(Hs.U_ic, pre)
-    res["central_differences"] = Hs.fd_window(Hs.state(), fd_steps, every, ndir, label,
+    Hs.start(Hs.U_ic, fd_pre)
+    res["central_differences"] = Hs.fd_window(Hs.state(), fd_steps, every, ndir,
+                                              f"Orszag-Tang state after {fd_pre} steps",
                                               bound=1e-6)
     Hs.close()
     H.start(U_ic, pre)
     U0 = H.state()
-    res["central_differences_512"] = [H.fd_window(U0, n, every, ndir // 4, label)
-                                      for n in (fd_steps, nsteps)]
+    res["central_differences_512"] = [
+        H.fd_window(U0, n, every, ndir // 4, f"Orszag-Tang state after {pre} steps")
+        for n in (fd_steps, nsteps)]
     H.close()
     return res
 
@@ -700,11 +721,17 @@ def main():
     ap.add_argument("--secondary", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--adjoint", type=int, default=1)
+    ap.add_argument("--case", default="bench", choices=["bench", "adjoint-step"],
+                    help="adjoint-step: a short differentiation run for kernel profiles")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.case == "adjoint-step":
+        import torch
+        import golikov_2d_gb300 as g
+        return adjoint_step_case(g, torch)
     return run_gb300(args)
 
 
