@@ -42,6 +42,8 @@ EXPORTS = (
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
     "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
+    "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text", "gd_write_binary",
+    "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot",
 )
 BATCH_PERSISTENT, BATCH_LOOPED = 0, 1
 
@@ -80,6 +82,12 @@ class gd_stats(ctypes.Structure):
         ("steps", ctypes.c_longlong), ("rho_floor_hits", ctypes.c_longlong),
         ("p_floor_hits", ctypes.c_longlong), ("nonfinite", ctypes.c_longlong),
     ]
+
+
+class gd_tecplot_opts(ctypes.Structure):
+    _fields_ = [("nmin", ctypes.c_int), ("x_min", ctypes.c_double), ("x_max", ctypes.c_double),
+                ("y_min", ctypes.c_double), ("y_max", ctypes.c_double),
+                ("with_time", ctypes.c_int), ("time", ctypes.c_double)]
 
 
 _lib = None
@@ -121,6 +129,16 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    sz = ctypes.c_size_t
+    tecp = ctypes.POINTER(gd_tecplot_opts)
+    L.gd_format_text.argtypes = [vp, vp, sz, ctypes.POINTER(sz), vp]
+    L.gd_write_text.argtypes = [vp, ctypes.c_char_p, vp]
+    L.gd_parse_text.argtypes = [vp, ctypes.c_char_p, sz, vp]
+    L.gd_read_text.argtypes = [vp, ctypes.c_char_p, vp]
+    L.gd_write_binary.argtypes = [vp, ctypes.c_char_p, vp]
+    L.gd_read_binary.argtypes = [vp, ctypes.c_char_p, vp]
+    L.gd_format_tecplot.argtypes = [vp, tecp, vp, sz, ctypes.POINTER(sz), vp]
+    L.gd_write_tecplot.argtypes = [vp, ctypes.c_char_p, tecp, vp]
     L.gd_batch_create.argtypes = [cfgp, i, ctypes.POINTER(vp)]
     L.gd_batch_destroy.argtypes = [vp]
     L.gd_batch_import.argtypes = [vp, i, vp, vp, vp, i, vp]
@@ -139,7 +157,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
-                 "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay"):
+                 "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
+                 "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text",
+                 "gd_write_binary", "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -293,6 +313,56 @@ class Solver:
 
     def launch_count(self) -> int:
         return int(self.lib.gd_launch_count(self.handle))
+
+    # -- state files (the reference's formats, made on the GPU) --------------------------------
+    def _fetch(self, fn, what, *args, stream=None) -> bytes:
+        n = ctypes.c_size_t(0)
+        _check(fn(self.handle, *args, None, 0, ctypes.byref(n), _stream_handle(stream)), what)
+        buf = ctypes.create_string_buffer(n.value)
+        _check(fn(self.handle, *args, buf, n.value, ctypes.byref(n), _stream_handle(stream)),
+               what)
+        return buf.raw[:n.value]
+
+    def format_text(self, stream=None) -> bytes:
+        """The restart text of the resident state ("x y rho p vx vy Bx By Bz" per cell)."""
+        return self._fetch(self.lib.gd_format_text, "gd_format_text", stream=stream)
+
+    def write_text(self, path: str, stream=None) -> None:
+        _check(self.lib.gd_write_text(self.handle, os.fsencode(path), _stream_handle(stream)),
+               "gd_write_text")
+
+    def parse_text(self, text: bytes, stream=None) -> None:
+        _check(self.lib.gd_parse_text(self.handle, text, len(text), _stream_handle(stream)),
+               "gd_parse_text")
+
+    def read_text(self, path: str, stream=None) -> None:
+        _check(self.lib.gd_read_text(self.handle, os.fsencode(path), _stream_handle(stream)),
+               "gd_read_text")
+
+    def write_binary(self, path: str, stream=None) -> None:
+        _check(self.lib.gd_write_binary(self.handle, os.fsencode(path), _stream_handle(stream)),
+               "gd_write_binary")
+
+    def read_binary(self, path: str, stream=None) -> None:
+        _check(self.lib.gd_read_binary(self.handle, os.fsencode(path), _stream_handle(stream)),
+               "gd_read_binary")
+
+    @staticmethod
+    def tecplot_opts(nmin, x_min, x_max, y_min, y_max, time=None) -> gd_tecplot_opts:
+        return gd_tecplot_opts(int(nmin), float(x_min), float(x_max), float(y_min),
+                               float(y_max), 0 if time is None else 1,
+                               0.0 if time is None else float(time))
+
+    def format_tecplot(self, nmin, x_min, x_max, y_min, y_max, time=None, stream=None) -> bytes:
+        o = self.tecplot_opts(nmin, x_min, x_max, y_min, y_max, time)
+        return self._fetch(self.lib.gd_format_tecplot, "gd_format_tecplot", ctypes.byref(o),
+                           stream=stream)
+
+    def write_tecplot(self, path, nmin, x_min, x_max, y_min, y_max, time=None,
+                      stream=None) -> None:
+        o = self.tecplot_opts(nmin, x_min, x_max, y_min, y_max, time)
+        _check(self.lib.gd_write_tecplot(self.handle, os.fsencode(path), ctypes.byref(o),
+                                         _stream_handle(stream)), "gd_write_tecplot")
 
 
 class Batch:

@@ -180,6 +180,7 @@ gd_status gd_destroy(gd_ctx* ctx) {
     cudaFree(ctx->ref_planes);
     cudaFree(ctx->aos);
     gd::adj_free(ctx);
+    gd::io_free(ctx);
     delete ctx;
     return GD_OK;
 }

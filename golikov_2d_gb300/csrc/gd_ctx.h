@@ -23,6 +23,14 @@ struct AdjStore {
     int seg_holds = -1;          // segment whose input states and update terms seg/aux hold
 };
 
+// Work buffers of the state I/O entry points (gd_io.cu), grown on demand.
+struct IoScratch {
+    char* dev = nullptr;   // device: line slots, lengths, offsets, scan partials, output
+    size_t dev_cap = 0;
+    char* host = nullptr;  // pinned staging for file reads and writes
+    size_t host_cap = 0;
+};
+
 }  // namespace gd
 
 using gd::CPlanes;
@@ -44,6 +52,7 @@ struct gd_ctx {
     long long launches = 0;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
     gd::AdjStore* adj = nullptr;            // differentiation record (gd_adj_forward)
+    gd::IoScratch* io = nullptr;            // state I/O work buffers (gd_io.cu)
 
     Planes planes(int which) const {
         Planes p{};
@@ -66,4 +75,5 @@ struct gd_ctx {
 
 namespace gd {
 void adj_free(gd_ctx* ctx);
+void io_free(gd_ctx* ctx);
 }  // namespace gd

@@ -237,6 +237,50 @@ gd_status gd_step_ref_static(const gd_config* cfg, const double* s, const double
                              const double* b, double* s2, double* u2, double* b2, double* T,
                              const double* T_do, int method, gd_stream stream);
 
+/* ---- state I/O -------------------------------------------------------------------------
+ * The reference's file formats, produced and parsed on the GPU (formatting into per-line
+ * slots, a prefix sum of line lengths, compaction, one copy to the host).  Numbers are
+ * written as `ostream << double` writes them at its default format (printf "%.6g",
+ * correctly rounded) and read as `istream >> double` reads them (correctly rounded);
+ * files are byte-identical to the reference's writers.  Cells are in the reference order
+ * k = m*N + n.  The gd_format_* / gd_parse_* forms work on host memory: with buf == NULL
+ * (or cap too small) they only report the length in *len (GD_ERR_INVALID_ARG if buf was
+ * given but too small).  All are blocking (they synchronise `stream`).
+ *
+ * Text restart file (kernel.cu:4245-4254 writer, kernel.cu:3944-3996 reader): one line
+ * per cell, "x y rho p vx vy Bx By Bz", x = x0 + n*dx, y = y0 + m*dy (the config's cell
+ * centres, the reference's x_min + n*dx), B in the stored Gaussian units; Euler contexts
+ * write 0 for B.  The reader takes whitespace-separated numbers in order as the
+ * reference's `fin >> c1 >> c2 >> a1 ... >> a7` does, ignores x and y, and fails on a
+ * malformed or missing number or an overflowing value. */
+gd_status gd_format_text(gd_ctx* ctx, char* buf, size_t cap, size_t* len, gd_stream stream);
+gd_status gd_write_text(gd_ctx* ctx, const char* path, gd_stream stream);
+gd_status gd_parse_text(gd_ctx* ctx, const char* text, size_t len, gd_stream stream);
+gd_status gd_read_text(gd_ctx* ctx, const char* path, gd_stream stream);
+
+/* Binary dump save_b3.dat (kernel.cu:4233-4261): per cell the raw doubles x, y, rho, p, vx,
+ * vy, Bz (host byte order).  The reference writes no reader; gd_read_binary restores rho,
+ * p, vx, vy and Bz from such a file and sets Bx = By = 0 (the file has no Bx, By). */
+gd_status gd_write_binary(gd_ctx* ctx, const char* path, gd_stream stream);
+gd_status gd_read_binary(gd_ctx* ctx, const char* path, gd_stream stream);
+
+/* Tecplot FEPOINT snapshot (print_file_mini kernel.cu:3682-3722 for Euler,
+ * print_file_mini2 kernel.cu:3724-3808 for MHD; with_time adds SOLUTIONTIME as the
+ * second print_file_mini2 does): every nmin-th point in x and y (the reference's Nmin),
+ * x = x_min + n (x_max - x_min) / (N - 1) with the reference's x_min / x_max (and y),
+ * columns X Y Ro P Vx Vy [Bx By Bz] Max T with Max = |v| / sqrt(gamma p / rho) and
+ * T = p / rho (0 where rho <= 0), then the quadrilateral connectivity (1-based). */
+typedef struct {
+    int nmin;
+    double x_min, x_max, y_min, y_max;
+    int with_time;
+    double time;
+} gd_tecplot_opts;
+gd_status gd_format_tecplot(gd_ctx* ctx, const gd_tecplot_opts* opts, char* buf, size_t cap,
+                            size_t* len, gd_stream stream);
+gd_status gd_write_tecplot(gd_ctx* ctx, const char* path, const gd_tecplot_opts* opts,
+                           gd_stream stream);
+
 /* ---- measurement helpers -------------------------------------------------------------- */
 
 /* Number of kernel launches the library issued on behalf of this context so far. */

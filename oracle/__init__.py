@@ -117,10 +117,41 @@ class Oracle:
         L.gdo_step.argtypes = [ctypes.POINTER(OracleConfig), _pd, _pd, _pd, _pd, _pd, _pd, _d, _d, _i]
         L.gdo_set_threads.restype = _i
         L.gdo_set_threads.argtypes = [_i]
+        cp = ctypes.POINTER(OracleConfig)
+        for name in ("gdo_write_restart", "gdo_write_binary"):
+            getattr(L, name).restype = _i
+            getattr(L, name).argtypes = [cp, _pd, _pd, _pd, ctypes.c_char_p]
+        L.gdo_write_tecplot.restype = _i
+        L.gdo_write_tecplot.argtypes = [cp, _pd, _pd, _pd, _i, _d, _d, _d, _d, _i, _d,
+                                        ctypes.c_char_p]
         self.lib = L
 
     def set_threads(self, n: int) -> int:
         return self.lib.gdo_set_threads(n)
+
+    # state files (the reference's writers restated with C stdio)
+    def write_restart(self, g: Grid, s, u, b, path) -> None:
+        c = g.cstruct()
+        args = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (s, u, b)]
+        if self.lib.gdo_write_restart(ctypes.byref(c), *[_ptr(a) for a in args],
+                                      os.fsencode(path)):
+            raise OSError(path)
+
+    def write_binary(self, g: Grid, s, u, b, path) -> None:
+        c = g.cstruct()
+        args = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (s, u, b)]
+        if self.lib.gdo_write_binary(ctypes.byref(c), *[_ptr(a) for a in args],
+                                     os.fsencode(path)):
+            raise OSError(path)
+
+    def write_tecplot(self, g: Grid, s, u, b, nmin, x_min, x_max, y_min, y_max, path,
+                      time=None) -> None:
+        c = g.cstruct()
+        args = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (s, u, b)]
+        if self.lib.gdo_write_tecplot(ctypes.byref(c), *[_ptr(a) for a in args], int(nmin),
+                                      x_min, x_max, y_min, y_max, 0 if time is None else 1,
+                                      0.0 if time is None else float(time), os.fsencode(path)):
+            raise OSError(path)
 
     def minmod(self, a, b):
         return self.lib.gdo_minmod(a, b)
@@ -202,6 +233,8 @@ class Reference:
             getattr(L, name).argtypes = [_pd, _pd, _pd, _pd, _pd, _pd, _pd, _d, _i, _i]
         for name in ("gdref_ker_dekard", "gdref_kernel_tvd_old"):
             getattr(L, name).argtypes = [_pd, _pd, _pd, _pd, _pd, _d, _i]
+        L.gdref_print_tecplot.argtypes = [_pd, _pd, _pd, _i, _d, ctypes.c_char_p]
+        L.gdref_write_restart.argtypes = [_pd, _pd, _pd, ctypes.c_char_p]
         self.lib = L
 
     @staticmethod
@@ -239,6 +272,22 @@ class Reference:
 
     def add2(self, s, u, b, T_do, i=0, method=2, out=None):
         return self._mhd_kernel(self.lib.gdref_add2, s, u, b, T_do, i, method, out)
+
+    def print_tecplot(self, s, u, b, with_b, ttt, path):
+        """The reference's print_file_mini (with_b 0) / print_file_mini2 (1; 2 = with
+        SOLUTIONTIME ttt) for the grid set by set_params."""
+        s = np.ascontiguousarray(s, np.float64)
+        u = np.ascontiguousarray(u, np.float64)
+        b = None if b is None else np.ascontiguousarray(b, np.float64)
+        self.lib.gdref_print_tecplot(_ptr(s), _ptr(u), _ptr(b), int(with_b), float(ttt),
+                                     os.fsencode(path))
+
+    def write_restart(self, s, u, b, path):
+        """The restart dump of the reference's main loop (kernel.cu:4245-4254)."""
+        s = np.ascontiguousarray(s, np.float64)
+        u = np.ascontiguousarray(u, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        self.lib.gdref_write_restart(_ptr(s), _ptr(u), _ptr(b), os.fsencode(path))
 
     def ker_dekard(self, s, u, T_do, method=1, out=None):
         s = np.ascontiguousarray(s, np.float64)

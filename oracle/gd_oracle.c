@@ -20,6 +20,7 @@
 #include "gd_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -715,4 +716,89 @@ void gdo_funk_time(double* T, double* T_do, double* TT, int* i) {
     *TT = *TT + *T_do;
     *T = 10000000;
     *i = *i + 1;
+}
+
+/* ---- state files ------------------------------------------------------------------------
+ * Restart text: the stream of kernel.cu:4245-4254, one line per cell, x = x_min + n dx,
+ * y = y_min + m dy; an Euler state (b == NULL) writes 0 for B. */
+int gdo_write_restart(const gdo_config* c, const double* s, const double* u, const double* b,
+                      const char* path) {
+    FILE* f = fopen(path, "w");
+    if (!f) return 1;
+    const long K = (long)c->N * c->M;
+    for (long k = 0; k < K; ++k) {
+        const int n = (int)(k % c->N), m = (int)(k / c->N);
+        const double y = c->y0 + m * c->dy;
+        const double x = c->x0 + n * c->dx;
+        fprintf(f, "%g %g %g %g %g %g %g %g %g\n", x, y, s[2 * k], s[2 * k + 1], u[2 * k],
+                u[2 * k + 1], b ? b[3 * k] : 0.0, b ? b[3 * k + 1] : 0.0, b ? b[3 * k + 2] : 0.0);
+    }
+    return fclose(f) != 0;
+}
+
+/* save_b3.dat (kernel.cu:4255-4261): x, y, rho, p, vx, vy, Bz as raw doubles. */
+int gdo_write_binary(const gdo_config* c, const double* s, const double* u, const double* b,
+                     const char* path) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return 1;
+    const long K = (long)c->N * c->M;
+    for (long k = 0; k < K; ++k) {
+        const int n = (int)(k % c->N), m = (int)(k / c->N);
+        const double rec[7] = {c->x0 + n * c->dx, c->y0 + m * c->dy, s[2 * k], s[2 * k + 1],
+                               u[2 * k], u[2 * k + 1], b ? b[3 * k + 2] : 0.0};
+        if (fwrite(rec, sizeof(double), 7, f) != 7) {
+            fclose(f);
+            return 1;
+        }
+    }
+    return fclose(f) != 0;
+}
+
+/* print_file_mini (b == NULL, kernel.cu:3682-3722) and print_file_mini2 (kernel.cu:3724-3808,
+ * with_time adds SOLUTIONTIME): every nmin-th point, Max and T per point, then the
+ * quadrilateral connectivity. */
+int gdo_write_tecplot(const gdo_config* c, const double* s, const double* u, const double* b,
+                      int nmin, double x_min, double x_max, double y_min, double y_max,
+                      int with_time, double time, const char* path) {
+    FILE* f = fopen(path, "w");
+    if (!f) return 1;
+    const int N = c->N, M = c->M;
+    const int nn = (N + nmin - 1) / nmin, mm = (M + nmin - 1) / nmin;
+    if (b)
+        fprintf(f, "TITLE = \"HP\"  VARIABLES = \"X\", \"Y\", \"Ro\", \"P\", \"Vx\", "
+                   "\"Vy\", \"Bx\", \"By\", \"Bz\", \"Max\", \"T\", ZONE T = \"HP\", N = %d , "
+                   "E = %d, F = FEPOINT, ET = quadrilateral",
+                nn * mm, (nn - 1) * (mm - 1));
+    else
+        fprintf(f, "TITLE = \"HP\"  VARIABLES = \"X\", \"Y\", \"Ro\", \"P\", \"Vx\", "
+                   "\"Vy\", \"Max\", \"T\", ZONE T = \"HP\", N = %d , E = %d, F = FEPOINT, "
+                   "ET = quadrilateral",
+                nn * mm, (nn - 1) * (mm - 1));
+    if (with_time) fprintf(f, ", SOLUTIONTIME = %g", time);
+    fprintf(f, "\n");
+    const long K = (long)N * M;
+    for (long k = 0; k < K; ++k) {
+        const int n = (int)(k % N), m = (int)((k - n) / N);
+        if (n % nmin != 0 || m % nmin != 0) continue;
+        const double y = y_min + m * (y_max - y_min) / (M - 1);
+        const double x = x_min + n * (x_max - x_min) / (N - 1);
+        double Max = 0.0, Temp = 0.0;
+        const double r = s[2 * k], p = s[2 * k + 1], vx = u[2 * k], vy = u[2 * k + 1];
+        if (r > 0.0) {
+            Max = sqrt((vx * vx + vy * vy) / (c->gamma * p / r));
+            Temp = p / r;
+        }
+        if (b)
+            fprintf(f, "%g %g %g %g %g %g %g %g %g %g %g\n", x, y, r, p, vx, vy, b[3 * k],
+                    b[3 * k + 1], b[3 * k + 2], Max, Temp);
+        else
+            fprintf(f, "%g %g %g %g %g %g %g %g\n", x, y, r, p, vx, vy, Max, Temp);
+    }
+    for (long k = 0; k < (long)nn * mm; ++k) {
+        const int n = (int)(k % nn), m = (int)((k - n) / nn);
+        if (m < mm - 1 && n < nn - 1)
+            fprintf(f, "%d %d %d %d\n", m * nn + n + 1, m * nn + n + 2, (m + 1) * nn + n + 2,
+                    (m + 1) * nn + n + 1);
+    }
+    return fclose(f) != 0;
 }

@@ -75,6 +75,17 @@ int gdo_set_threads(int n);
 /* Reference funk_time, kernel.cu:1722-1733 (without its progress print). */
 void gdo_funk_time(double* T, double* T_do, double* TT, int* i);
 
+/* State files (kernel.cu:3682-3808, 4233-4261): the reference's writers restated with C
+ * stdio.  `os << double` at the stream's default format is printf "%g" (precision 6) and
+ * `os << int` is "%d", so the bytes are the reference's.  Return 0 on success. */
+int gdo_write_restart(const gdo_config* cfg, const double* s, const double* u, const double* b,
+                      const char* path);
+int gdo_write_binary(const gdo_config* cfg, const double* s, const double* u, const double* b,
+                     const char* path);
+int gdo_write_tecplot(const gdo_config* cfg, const double* s, const double* u, const double* b,
+                      int nmin, double x_min, double x_max, double y_min, double y_max,
+                      int with_time, double time, const char* path);
+
 #ifdef __cplusplus
 }
 #endif

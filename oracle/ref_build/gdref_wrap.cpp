@@ -13,6 +13,8 @@
  */
 #include "gdref_prelude.h"
 #include <cstring>
+#include <fstream>
+#include <string>
 #include <vector>
 #include <omp.h>
 
@@ -47,6 +49,10 @@ void Kernel_TVD(double2* s, double2* u, double3* b, double2* s2, double2* u2,
                 double3* b2, double* T, double* T_do, int i, int method);       /* kernel.cu:2198 */
 void Kernel_TVD_old(double2* s, double2* u, double2* s2, double2* u2, double* T,
                     double* T_do, int method);                                  /* kernel.cu:3286 */
+void print_file_mini(double2* s, double2* u, std::string name);                 /* kernel.cu:3682 */
+void print_file_mini2(double2* s, double2* u, double3* b, std::string name);    /* kernel.cu:3724 */
+void print_file_mini2(double2* s, double2* u, double3* b, std::string name,
+                      double TTT);                                              /* kernel.cu:3767 */
 
 namespace {
 
@@ -196,6 +202,43 @@ void gdref_kernel_tvd_old(const double* s, const double* u, double* s2, double* 
     for_each_cell(T, [&](double* t) {
         Kernel_TVD_old(ps.data(), pu.data(), (double2*)s2, (double2*)u2, t, &tdo, method);
     });
+}
+
+/* Tecplot snapshots through the reference's own writers (Nmin, x_min = x_max / (2 N) and
+ * y_min are the reference's compile-time values; x_max, y_max, N, M, gamma are the ones set
+ * by gdref_set_params).  with_b = 0: print_file_mini (s, u); with_b = 1: print_file_mini2;
+ * with_b = 2: print_file_mini2 with SOLUTIONTIME = ttt. */
+void gdref_print_tecplot(const double* s, const double* u, const double* b, int with_b,
+                         double ttt, const char* path) {
+    const long K = (long)gdref_N * gdref_M;
+    auto ps = padded<double2>(s, K);
+    auto pu = padded<double2>(u, K);
+    if (with_b == 0) {
+        print_file_mini(ps.data(), pu.data(), std::string(path));
+        return;
+    }
+    auto pb = padded<double3>(b, K);
+    if (with_b == 1) print_file_mini2(ps.data(), pu.data(), pb.data(), std::string(path));
+    else print_file_mini2(ps.data(), pu.data(), pb.data(), std::string(path), ttt);
+}
+
+/* The restart dump of the reference's main loop (kernel.cu:4245-4254, the
+ * "instable_for_inner_b3.txt" stream): the same stream statements over every cell, at the
+ * reference's x_min + n dx, y_min + m dy. */
+void gdref_write_restart(const double* s, const double* u, const double* b, const char* path) {
+    const long K = (long)gdref_N * gdref_M;
+    const double xmin = gdref_xmax / (2.0 * gdref_N), ymin = gdref_ymax / (2.0 * gdref_M);
+    const double dxr = gdref_xmax / gdref_N, dyr = gdref_ymax / gdref_M;
+    std::ofstream fout(path);
+    for (long k = 0; k < K; k++) {
+        const int n = (int)(k % gdref_N);
+        const int m = (int)((k - n) / gdref_N);
+        const double y = ymin + m * dyr;
+        const double x = xmin + n * dxr;
+        fout << x << " " << y << " " << s[2 * k] << " " << s[2 * k + 1] << " " << u[2 * k] << " "
+             << u[2 * k + 1] << " " << b[3 * k] << " " << b[3 * k + 1] << " " << b[3 * k + 2]
+             << std::endl;
+    }
 }
 
 }  // extern "C"

@@ -15,6 +15,12 @@ Fixtures:
                    small random grids with the reference's own boundary conditions
   run_native.npz   20 steps of the reference protocol (Kernel_TVD + funk_time) from the
                    reference's wind initial condition on a reduced axisymmetric grid
+  io_files.npz     the reference's state files for one random state with hard-to-print
+                   values: print_file_mini / print_file_mini2 (both overloads) Tecplot
+                   snapshots (kernel.cu:3682-3808) and the restart dump of its main loop
+                   (kernel.cu:4245-4254), as bytes
+
+    python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
 from __future__ import annotations
 
@@ -176,14 +182,55 @@ def run_native(ref, nsteps=20):
                         nsteps=nsteps, s0=s0, u0=u0, b0=b0, s=s, u=u, b=b, T_do=T_do, TT=TT)
 
 
+def io_state(rng, K):
+    """A state whose numbers exercise every branch of %g: magnitudes 1e-8..1e3, negative
+    and zero densities (the Tecplot writer's rho > 0 branch), signed zeros, exact decimal
+    ties, powers of ten and their neighbours, subnormals and extremes."""
+    s = np.stack([10 ** rng.uniform(-8, 3, K) * np.where(rng.random(K) < 0.05, -1, 1),
+                  10 ** rng.uniform(-8, 3, K)], 1)
+    u = rng.standard_normal((K, 2)) * 10 ** rng.uniform(-5, 2, (K, 2))
+    b = rng.standard_normal((K, 3)) * 10 ** rng.uniform(-5, 2, (K, 3))
+    special = [0.0, -0.0, 1234565.0, 1234575.0, 0.5, 2.5e-5, 99999.95, 999999.5, 9.9999995,
+               1e-5, 1e-4, 1e5, 1e6, 1e-300, 5e-324, 2.2250738585072014e-308,
+               1.7976931348623157e308, -123456.5, 0.1, 1.0 / 3.0, 1e21, 1e22, 1e23,
+               np.nextafter(1e-4, 0), np.nextafter(1e6, 2e6), 100000.5]
+    flat = np.concatenate([s.ravel(), u.ravel(), b.ravel()])
+    idx = rng.choice(flat.size, len(special), replace=False)
+    flat[idx] = special
+    s = flat[:2 * K].reshape(K, 2)
+    u = flat[2 * K:4 * K].reshape(K, 2)
+    b = flat[4 * K:].reshape(K, 3)
+    s[3, 0] = 0.0
+    return s, u, b
+
+
+def io_files(ref):
+    N, M, xmax, ymax, gamma = 23, 17, 9.0, 5.0, 5.0 / 3.0
+    rng = np.random.default_rng(SEED + 7)
+    s, u, b = io_state(rng, N * M)
+    ref.set_params(gamma, 0.25, N, M, xmax, ymax)
+    out = {}
+    tmp = os.path.join(HERE, "_io_tmp.dat")
+    for name, call in (("tec_euler", lambda: ref.print_tecplot(s, u, None, 0, 0.0, tmp)),
+                       ("tec_mhd", lambda: ref.print_tecplot(s, u, b, 1, 0.0, tmp)),
+                       ("tec_mhd_t", lambda: ref.print_tecplot(s, u, b, 2, 0.123456789, tmp)),
+                       ("restart", lambda: ref.write_restart(s, u, b, tmp))):
+        call()
+        with open(tmp, "rb") as f:
+            out[name] = np.frombuffer(f.read(), np.uint8)
+    os.remove(tmp)
+    np.savez_compressed(os.path.join(HERE, "io_files.npz"), N=N, M=M, xmax=xmax, ymax=ymax,
+                        gamma=gamma, nmin=3, ttt=0.123456789, s=s, u=u, b=b, **out)
+
+
 def main():
     oracle.build(ref=True)
     ref = oracle.Reference()
     ref.lib.gdref_set_threads(1)
-    faces(ref)
-    recon(ref)
-    step_native(ref)
-    run_native(ref)
+    jobs = {"faces": faces, "recon": recon, "step_native": step_native,
+            "run_native": run_native, "io_files": io_files}
+    for name in (sys.argv[1:] or list(jobs)):
+        jobs[name](ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

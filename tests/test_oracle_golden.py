@@ -99,3 +99,27 @@ def test_native_run_20_steps(oracle_lib):
     s, u, b, T_do, TT = oracle_lib.run(grid, g["s0"], g["u0"], g["b0"], int(g["nsteps"]), 1e-8)
     assert T_do == g["T_do"] and TT == g["TT"]
     assert np.array_equal(s, g["s"]) and np.array_equal(u, g["u"]) and np.array_equal(b, g["b"])
+
+
+def io_grid(g):
+    N, M = int(g["N"]), int(g["M"])
+    xmax, ymax = float(g["xmax"]), float(g["ymax"])
+    return oracle.Grid(N, M, xmax / N, ymax / M, xmax / (2.0 * N), ymax / (2.0 * M),
+                       float(g["gamma"]), 0.25, physics=oracle.MHD)
+
+
+def test_state_file_writers(oracle_lib, tmp_path):
+    """The oracle's stdio writers produce the reference's files byte for byte: the restart
+    dump of its main loop and the three Tecplot writers (golden bytes from the reference)."""
+    g = golden("io_files.npz")
+    grid = io_grid(g)
+    s, u, b = g["s"], g["u"], g["b"]
+    xmax, ymax = float(g["xmax"]), float(g["ymax"])
+    xmin, ymin = xmax / (2.0 * grid.N), ymax / (2.0 * grid.M)
+    p = str(tmp_path / "f")
+    oracle_lib.write_restart(grid, s, u, b, p)
+    assert open(p, "rb").read() == g["restart"].tobytes()
+    for key, bb, t in (("tec_euler", None, None), ("tec_mhd", b, None),
+                       ("tec_mhd_t", b, float(g["ttt"]))):
+        oracle_lib.write_tecplot(grid, s, u, bb, int(g["nmin"]), xmin, xmax, ymin, ymax, p, t)
+        assert open(p, "rb").read() == g[key].tobytes(), key

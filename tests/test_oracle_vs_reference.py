@@ -60,3 +60,24 @@ def test_hlld_random_faces(oracle_lib, reference):
         t1, F1 = oracle_lib.hlld(L, R, n1, n2, 0.0, 0.003, meth, 5.0 / 3.0, 0.4)
         t2, F2 = reference.hlld(L, R, n1, n2, 0.0, 0.003, meth)
         assert t1 == t2 and np.array_equal(F1, F2, equal_nan=True)
+
+
+@pytest.mark.parametrize("seed,N,M", [(31, 40, 23), (32, 7, 5), (33, 16, 16)])
+def test_state_file_writers_random(oracle_lib, reference, tmp_path, seed, N, M):
+    """Writers on fresh states and grid shapes (the reference's Tecplot writers take
+    Nmin = 3 from its header)."""
+    from golden.make_golden import io_state
+    rng = np.random.default_rng(seed)
+    s, u, b = io_state(rng, N * M)
+    xmax, ymax, gamma = 9.0, 5.0, 1.4
+    reference.set_params(gamma, 0.25, N, M, xmax, ymax)
+    grid = oracle.Grid(N, M, xmax / N, ymax / M, xmax / (2.0 * N), ymax / (2.0 * M), gamma, 0.25)
+    pr, po = str(tmp_path / "r"), str(tmp_path / "o")
+    reference.write_restart(s, u, b, pr)
+    oracle_lib.write_restart(grid, s, u, b, po)
+    assert open(pr, "rb").read() == open(po, "rb").read()
+    for wb, bb, t in ((0, None, None), (1, b, None), (2, b, 2.5e-3)):
+        reference.print_tecplot(s, u, bb, wb, 0.0 if t is None else t, pr)
+        oracle_lib.write_tecplot(grid, s, u, bb, 3, xmax / (2.0 * N), xmax, ymax / (2.0 * M),
+                                 ymax, po, t)
+        assert open(pr, "rb").read() == open(po, "rb").read(), wb
