@@ -253,6 +253,129 @@ def measure_batched(g, torch, steps, ngrids=512):
     return res
 
 
+def measure_io(g, torch, N=1024, reps=5, cpu_N=256):
+    """State files of Orszag-Tang N x N after 5 steps, made and read on the GPU through the C
+    ABI: the restart text (9 numbers per cell, the reference's dump format), the Tecplot
+    snapshot at every point and at the reference's Nmin = 3, the binary dump.  Device time =
+    formatting, scan and compaction with the image left on the device (gd_format_text with no
+    buffer); e2e = the same into host memory (pageable, copy included); parse = host text ->
+    device -> state.  CPU baseline: the oracle's stdio writer and reader (one thread, the
+    reference writes and reads with one thread) on an N = cpu_N grid of the same problem."""
+    import ctypes
+    import tempfile
+    from golikov_2d_gb300 import problems
+
+    def state_after(n, steps=5):
+        cfg, s, u, b = problems.orszag_tang(n, n)
+        sol = g.Solver(cfg)
+        sol.import_state(s, u, b)
+        sol.set_time(0.0, 0.0)
+        sol.init_dt()
+        sol.advance(steps)
+        return cfg, sol
+
+    def best(fn):
+        fn()  # warm-up (scratch allocation)
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts), statistics.median(ts)
+
+    cfg, sol = state_after(N)
+    K = cfg.N * cfg.M
+    lib, h = sol.lib, sol.handle
+    n = ctypes.c_size_t(0)
+
+    def fmt_device():
+        if lib.gd_format_text(h, None, 0, ctypes.byref(n), None):
+            raise RuntimeError("gd_format_text")
+
+    fmt_device()
+    nbytes = n.value
+    buf = ctypes.create_string_buffer(nbytes)
+
+    def fmt_host():
+        if lib.gd_format_text(h, buf, nbytes, ctypes.byref(n), None):
+            raise RuntimeError("gd_format_text")
+
+    l0 = sol.launch_count()
+    t_dev, t_dev_med = best(fmt_device)
+    launches = (sol.launch_count() - l0) // (reps + 1)
+    t_e2e, _ = best(fmt_host)
+    text = buf.raw[:nbytes]
+    sol2 = g.Solver(cfg)
+    t_parse, _ = best(lambda: sol2.parse_text(text))
+    ok = sol2.format_text() == text
+    peak, _ = measured_peaks()
+    state_bytes = K * 7 * 8
+    res = {"workload": f"Orszag-Tang {N}x{N} MHD state after 5 steps", "cells": K,
+           "restart_text": {
+               "bytes": nbytes, "bytes_per_cell": nbytes / K,
+               "format_device_s": t_dev, "format_device_median_s": t_dev_med,
+               "format_cells_per_s": K / t_dev, "format_text_GBps": nbytes / t_dev / 1e9,
+               "format_e2e_s": t_e2e, "format_e2e_cells_per_s": K / t_e2e,
+               "parse_e2e_s": t_parse, "parse_cells_per_s": K / t_parse,
+               "parse_text_GBps": nbytes / t_parse / 1e9, "round_trip_identical": ok,
+               "launches_per_format": launches,
+               "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak,
+                            "algorithmic_bytes": state_bytes + nbytes,
+                            "achieved": (state_bytes + nbytes) / t_dev / 1e9,
+                            "frac": (state_bytes + nbytes) / t_dev / 1e9 / peak,
+                            "note": "state read once + text written once; the formatter is "
+                                    "integer-issue bound (digit generation)"}}}
+    for nmin in (1, 3):
+        o = sol.tecplot_opts(nmin, cfg.x0, cfg.x0 + cfg.N * cfg.dx, cfg.y0,
+                             cfg.y0 + cfg.M * cfg.dy)
+
+        def tec():
+            if lib.gd_format_tecplot(h, ctypes.byref(o), None, 0, ctypes.byref(n), None):
+                raise RuntimeError("gd_format_tecplot")
+
+        t_tec, _ = best(tec)
+        res[f"tecplot_nmin{nmin}"] = {"bytes": n.value, "format_device_s": t_tec,
+                                      "points_per_s": ((cfg.N + nmin - 1) // nmin) ** 2 / t_tec}
+    with tempfile.TemporaryDirectory() as d:
+        pb = os.path.join(d, "save_b3.dat")
+        t_bin, _ = best(lambda: sol.write_binary(pb))
+        res["binary"] = {"bytes": os.path.getsize(pb), "write_file_s": t_bin}
+        pt = os.path.join(d, "restart.txt")
+        t_wf, _ = best(lambda: sol.write_text(pt))
+        res["restart_text"]["write_file_s"] = t_wf
+        t_rf, _ = best(lambda: sol2.read_text(pt))
+        res["restart_text"]["read_file_s"] = t_rf
+        # CPU baseline: the oracle's writer and reader, one thread
+        import oracle
+        oracle.build(ref=False)
+        o = oracle.Oracle()
+        cfg_c, sol_c = state_after(cpu_N)
+        Kc = cfg_c.N * cfg_c.M
+        sc, uc, bc = np.zeros((Kc, 2)), np.zeros((Kc, 2)), np.zeros((Kc, 3))
+        sol_c.export_state(sc, uc, bc)
+        grid = oracle.Grid(cfg_c.N, cfg_c.M, cfg_c.dx, cfg_c.dy, cfg_c.x0, cfg_c.y0, cfg_c.gamma,
+                           cfg_c.krit, physics=oracle.MHD)
+        pc = os.path.join(d, "cpu.txt")
+        t0 = time.perf_counter()
+        o.write_restart(grid, sc, uc, bc, pc)
+        t_cw = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.read_restart(grid, pc)
+        t_cr = time.perf_counter() - t0
+        same = open(pc, "rb").read() == sol_c.format_text()
+        sol_c.close()
+    res["cpu_baseline"] = {"kind": "port", "cores": 1,
+                           "sample": f"Orszag-Tang {cpu_N}x{cpu_N} restart text, oracle "
+                                     f"gdo_write_restart / gdo_read_restart (C stdio)",
+                           "write_cells_per_s": Kc / t_cw, "read_cells_per_s": Kc / t_cr,
+                           "gpu_text_identical": same}
+    sol.close()
+    sol2.close()
+    return res
+
+
 def adjoint_step_case(g, torch, N=512):
     """A short differentiation run for kernel profiles: Orszag-Tang N x N, 20 plain steps,
     a 10-step recording, one backward sweep and one tangent sweep."""
@@ -702,6 +825,11 @@ def run_gb300(args):
             line["adjoint"] = measure_adjoint(g, torch)
         except Exception as e:
             line["adjoint"] = {"unavailable": str(e)}
+    if args.io:
+        try:
+            line["io"] = measure_io(g, torch)
+        except Exception as e:
+            line["io"] = {"unavailable": str(e)}
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args.workload, cfg, s, u, b)
     print(json.dumps(line), flush=True)
@@ -721,8 +849,10 @@ def main():
     ap.add_argument("--secondary", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--adjoint", type=int, default=1)
-    ap.add_argument("--case", default="bench", choices=["bench", "adjoint-step"],
-                    help="adjoint-step: a short differentiation run for kernel profiles")
+    ap.add_argument("--io", type=int, default=1)
+    ap.add_argument("--case", default="bench", choices=["bench", "adjoint-step", "io"],
+                    help="adjoint-step: a short differentiation run for kernel profiles; "
+                         "io: the state-file measurement alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -732,6 +862,11 @@ def main():
         import torch
         import golikov_2d_gb300 as g
         return adjoint_step_case(g, torch)
+    if args.case == "io":
+        import torch
+        import golikov_2d_gb300 as g
+        print(json.dumps({"case": "io", "io": measure_io(g, torch)}), flush=True)
+        return 0
     return run_gb300(args)
 
 

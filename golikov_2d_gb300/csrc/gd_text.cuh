@@ -16,6 +16,8 @@
 #include <cmath>
 #include <cstdint>
 
+#include "gd_pow10.h"
+
 #ifdef __CUDACC__
 #define GD_HD __host__ __device__ __forceinline__
 #else
@@ -179,8 +181,8 @@ constexpr int kPrec = 6;
 constexpr uint32_t kLow = 100000u, kHigh = 1000000u;  // 10^(P-1), 10^P
 
 // Digits D (kLow <= D < kHigh) and exponent X with |x| = D 10^(X-P+1) rounded half-even on
-// the exact value.  ax finite, positive.
-GD_HD bool round_sig(double ax, int& X, uint32_t& D) {
+// the exact value, decided on integers where FP64 cannot decide.  ax finite, positive.
+GD_HD bool round_sig_exact(double ax, int& X, uint32_t& D) {
     uint64_t m;
     int e;
     decompose(ax, m, e);
@@ -257,6 +259,73 @@ exact:
     D = c;
 done:
     if (D >= kHigh) {  // rounded up to 10^P
+        D = kLow;
+        ++X;
+    }
+    return true;
+}
+
+// ---- the fast path ---------------------------------------------------------------------
+
+#ifdef __CUDACC__
+__device__ const double d_pow10[] = {GD_POW10_TABLE};
+#endif
+static const double h_pow10[] = {GD_POW10_TABLE};
+
+// binary64 nearest to 10^k, GD_POW10_LO <= k <= GD_POW10_HI
+GD_HD double pow10_near(int k) {
+#ifdef __CUDA_ARCH__
+    return d_pow10[k - GD_POW10_LO];
+#else
+    return h_pow10[k - GD_POW10_LO];
+#endif
+}
+
+GD_HD int clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+
+// floor(e log10 2) for |e| <= 1650: (e 78913) >> 18, the approximation published with the
+// Ryu conversion (Adams 2018) for e >= 0, mirrored for e < 0
+GD_HD int floor_log10_pow2(int e) {
+    return e >= 0 ? (int)(((uint32_t)e * 78913u) >> 18) : -(int)(((uint32_t)(-e) * 78913u) >> 18) - 1;
+}
+
+// round_sig with four FP64 operations on the common path: the decimal exponent from the
+// binary one and one integer comparison with the nearest double to a power of ten, the
+// scaled value t = ax 10^-s from one (rarely two) multiplications by table values, and
+// its nearest integer and remainder by the 2^52 addition.  t carries at most three
+// roundings, i.e. it is within 4e-10 of the exact ax / 10^s (t < 10^6); outside that
+// margin around a half-integer the nearest integer of t is the exact rounding.  The
+// remaining cases (a half-integer within the margin, ax within one ulp of a power of ten
+// whose double is inexact) go to round_sig_exact.
+GD_HD bool round_sig(double ax, int& X, uint32_t& D) {
+    const uint64_t b = dbits(ax);
+    const int be = (int)(b >> 52);
+    const int e2 = be ? be - 1023 : -1011 - clz64(b);  // floor(log2 ax); subnormal: top bit
+    const int X0 = floor_log10_pow2(e2);                // X is X0 or X0 + 1
+    const int k = X0 + 1;
+    const uint64_t tb = dbits(pow10_near(k));
+    if (k >= 0 && k <= 22) {  // exact power of ten
+        X = b >= tb ? k : X0;
+    } else {
+        if (b + 1 >= tb && b <= tb + 1) return round_sig_exact(ax, X, D);
+        X = b > tb ? k : X0;
+    }
+    const int ms = kPrec - 1 - X;  // -s
+    const double t = ms > 300 ? (ax * 1e30) * pow10_near(ms - 30) : ax * pow10_near(ms);
+    const double y = t + 4503599627370496.0;  // 2^52: y - 2^52 is t rounded to an integer
+    const uint32_t r = (uint32_t)(dbits(y) - 0x4330000000000000ULL);
+    const double f = t - (y - 4503599627370496.0);
+    if ((dbits(f) & 0x7fffffffffffffffULL) >= 0x3FDFFFFFFEED1F41ULL /* 0.5 - 1e-9 */ ||
+        r < kLow || r > kHigh)
+        return round_sig_exact(ax, X, D);
+    D = r;
+    if (D == kHigh) {  // rounded up to 10^P
         D = kLow;
         ++X;
     }

@@ -121,6 +121,8 @@ class Oracle:
         for name in ("gdo_write_restart", "gdo_write_binary"):
             getattr(L, name).restype = _i
             getattr(L, name).argtypes = [cp, _pd, _pd, _pd, ctypes.c_char_p]
+        L.gdo_read_restart.restype = _i
+        L.gdo_read_restart.argtypes = [cp, ctypes.c_char_p, _pd, _pd, _pd]
         L.gdo_write_tecplot.restype = _i
         L.gdo_write_tecplot.argtypes = [cp, _pd, _pd, _pd, _i, _d, _d, _d, _d, _i, _d,
                                         ctypes.c_char_p]
@@ -136,6 +138,17 @@ class Oracle:
         if self.lib.gdo_write_restart(ctypes.byref(c), *[_ptr(a) for a in args],
                                       os.fsencode(path)):
             raise OSError(path)
+
+    def read_restart(self, g: Grid, path, mhd=True):
+        """Returns (s, u, b) read from a restart text (b None unless mhd)."""
+        c = g.cstruct()
+        K = g.N * g.M
+        s, u = np.zeros((K, 2)), np.zeros((K, 2))
+        b = np.zeros((K, 3)) if mhd else None
+        if self.lib.gdo_read_restart(ctypes.byref(c), os.fsencode(path), _ptr(s), _ptr(u),
+                                     _ptr(b)):
+            raise OSError(path)
+        return s, u, b
 
     def write_binary(self, g: Grid, s, u, b, path) -> None:
         c = g.cstruct()

@@ -736,6 +736,33 @@ int gdo_write_restart(const gdo_config* c, const double* s, const double* u, con
     return fclose(f) != 0;
 }
 
+/* Restart reader: `fin >> c1 >> c2 >> a1 ... >> a7` per cell, restated with fscanf("%lf")
+ * (both are correctly rounded decimal conversions). */
+int gdo_read_restart(const gdo_config* c, const char* path, double* s, double* u, double* b) {
+    FILE* f = fopen(path, "r");
+    if (!f) return 1;
+    const long K = (long)c->N * c->M;
+    for (long k = 0; k < K; ++k) {
+        double v[9];
+        for (int i = 0; i < 9; ++i)
+            if (fscanf(f, "%lf", &v[i]) != 1) {
+                fclose(f);
+                return 1;
+            }
+        s[2 * k] = v[2];
+        s[2 * k + 1] = v[3];
+        u[2 * k] = v[4];
+        u[2 * k + 1] = v[5];
+        if (b) {
+            b[3 * k] = v[6];
+            b[3 * k + 1] = v[7];
+            b[3 * k + 2] = v[8];
+        }
+    }
+    fclose(f);
+    return 0;
+}
+
 /* save_b3.dat (kernel.cu:4255-4261): x, y, rho, p, vx, vy, Bz as raw doubles. */
 int gdo_write_binary(const gdo_config* c, const double* s, const double* u, const double* b,
                      const char* path) {

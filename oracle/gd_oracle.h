@@ -82,6 +82,9 @@ int gdo_write_restart(const gdo_config* cfg, const double* s, const double* u, c
                       const char* path);
 int gdo_write_binary(const gdo_config* cfg, const double* s, const double* u, const double* b,
                      const char* path);
+/* The restart reader (kernel.cu:3944-3996): nine numbers per cell read in order, x and y
+ * dropped; b may be NULL (Euler).  Returns 0 on success, 1 if a number is missing. */
+int gdo_read_restart(const gdo_config* cfg, const char* path, double* s, double* u, double* b);
 int gdo_write_tecplot(const gdo_config* cfg, const double* s, const double* u, const double* b,
                       int nmin, double x_min, double x_max, double y_min, double y_max,
                       int with_time, double time, const char* path);
