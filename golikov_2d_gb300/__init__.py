@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(PKG, "libgd2d.so")
 
 EULER, MHD = 0, 1
 CARTESIAN, AXISYM = 0, 1
-METHOD_HLLC, METHOD_HLLC_MHD, METHOD_HLLD = 1, 2, 3
+METHOD_HLL, METHOD_HLLC, METHOD_HLLC_MHD, METHOD_HLLD = 0, 1, 2, 3
+METHOD_CONFIG = -1  # per-call method argument: the context's configured method
 (BC_PERIODIC, BC_TRANSMISSIVE, BC_MIRROR_X, BC_AXIS, BC_AMBIENT, BC_OUTFLOW,
  BC_AMBIENT_KEEPB) = range(7)
 MODE_FAST, MODE_PARITY = 0, 1
@@ -234,8 +235,10 @@ class Solver:
             pass
 
     # -- the reference's launch protocol (device pointers, AoS layout) ------------------------
-    def kernel_step(self, s, u, b, s2, u2, b2, T, T_do, i=0, method=0, stream=None) -> None:
-        """gd_step_ref: Kernel_TVD / add2 / Ker_Dekard on CUDA tensors."""
+    def kernel_step(self, s, u, b, s2, u2, b2, T, T_do, i=0, method=METHOD_CONFIG,
+                    stream=None) -> None:
+        """gd_step_ref: Kernel_TVD / add2 / Ker_Dekard on CUDA tensors; `method` is the
+        reference's code (METHOD_*) or METHOD_CONFIG."""
         p = lambda t: None if t is None else t.data_ptr()
         _check(self.lib.gd_step_ref(self.handle, p(s), p(u), p(b), p(s2), p(u2), p(b2), p(T),
                                     p(T_do), int(i), int(method), _stream_handle(stream)),

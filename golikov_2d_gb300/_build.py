@@ -22,6 +22,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "--expt-relaxed-constexpr", "-I", INCLUDE]
+# gd_parity.cu: the reference's operations, unfused
 PER_FILE = {"gd_parity.cu": ["--fmad=false"]}
 
 

@@ -54,7 +54,8 @@ gd_status validate(const gd_config* c) {
     if (c->geometry != GD_CARTESIAN && c->geometry != GD_AXISYM) return GD_ERR_INVALID_ARG;
     if (c->order != 1 && c->order != 2) return GD_ERR_INVALID_ARG;
     if (c->mode != GD_MODE_FAST && c->mode != GD_MODE_PARITY) return GD_ERR_INVALID_ARG;
-    if (c->physics == GD_EULER && c->method != GD_METHOD_HLLC) return GD_ERR_INVALID_ARG;
+    if (c->physics == GD_EULER && c->method != GD_METHOD_HLLC && c->method != GD_METHOD_HLL)
+        return GD_ERR_INVALID_ARG;
     if (c->physics == GD_MHD && c->method != GD_METHOD_HLLC_MHD && c->method != GD_METHOD_HLLD)
         return GD_ERR_INVALID_ARG;
     for (int s = 0; s < 4; ++s)
@@ -198,8 +199,9 @@ gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const doubl
     if (!ctx || !s || !u || !s2 || !u2 || !T || !T_do) return GD_ERR_INVALID_ARG;
     if (ctx->nf == 7 && (!b || !b2)) return GD_ERR_INVALID_ARG;
     Params P = ctx->P;
-    if (method > 0) {
-        if (ctx->cfg.physics == GD_EULER && method != GD_METHOD_HLLC) return GD_ERR_INVALID_ARG;
+    if (method != GD_METHOD_CONFIG) {
+        if (ctx->cfg.physics == GD_EULER && method != GD_METHOD_HLLC && method != GD_METHOD_HLL)
+            return GD_ERR_INVALID_ARG;
         if (ctx->cfg.physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
             return GD_ERR_INVALID_ARG;
         P.method = method;

@@ -1,14 +1,19 @@
-// gd_fast_euler.cu -- fused minmod-TVD + HLLC + update step for 2-D Euler, face-once tiles.
+// gd_fast_euler.cu -- fused minmod-TVD + HLLC/HLL + update step for 2-D Euler, face-once tiles.
 //
 // One CTA owns a TX x TY tile.  Phases, separated by __syncthreads():
 //   L  load the tile plus a 2-cell cross-shaped halo (boundary ghosts applied) into smem;
 //   S  per-cell minmod slopes along x and y (integer-pipe minmod, one FP64 sub per edge);
-//   F  every face of the tile once: left/right face states from the slopes, the HLLC flux
-//      in the face's local (normal, tangent) frame, and the face's wave-speed maximum;
+//   F  every face of the tile once: left/right face states from the slopes, the HLLC (or,
+//      for method 0, HLL) flux in the face's local (normal, tangent) frame, and the face's
+//      wave-speed maximum;
 //   U  conservative update of each cell from its four face fluxes, positivity floors,
 //      primitive recovery; store; block dt minimum and the fused funk_time rotation.
 // The reference computes every face twice, once from each neighbour (kernel.cu:3560-3586);
 // here each face is computed once and used with opposite signs by its two cells.
+//
+// Each tile shape is a separate template instantiation; the compiler may fuse multiply-adds
+// differently in each, so shapes agree to rounding (~1e-14 relative per step), not bit for
+// bit.  A given shape is deterministic.
 //
 // Two kernels share the tile body: euler_fast_kernel (one grid, one CTA per tile) and
 // euler_batch_kernel (a persistent launch that walks the tiles of many independent grids,
@@ -17,7 +22,8 @@
 //
 // Reference semantics kept: primitive reconstruction of (rho, p, vx, vy) with the rho/p
 // face fallback to the cell value (kernel.cu:3436-3544), Davis wave speeds and the HLLC
-// star states of HLLC_Aleksashov (kernel.cu:853-1165), the Ker_Dekard update and floors
+// star states of HLLC_Aleksashov (kernel.cu:853-1165), the HLL flux (kernel.cu:1485-1609)
+// for method 0, the Ker_Dekard update and floors
 // rho <= 0 -> 1e-4, p <= 0 -> 1e-6 (kernel.cu:1849-1874), dt = min over faces of
 // krit*rad/max(|SL|,|SR|) with rad = dy on x-faces (kernel.cu:1811).
 #include "gd_internal.cuh"
@@ -73,13 +79,53 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
         const double inv = rcp_fast(S - SM);
         const double rz = r * (su * inv);
         const double pst = fma(mm, SM - un, p);
-        const double ez = (fma(E, su, pst * SM) - p * un) * inv;
+        const double ez = fma(-p, un, fma(E, su, pst * SM)) * inv;
         const double drz = rz - r;
         F.mn = fma(S, fma(rz, SM, -F.m), F.mn);
         F.m = fma(S, drz, F.m);
         F.mt = fma(S, ut * drz, F.mt);
         F.e = fma(S, ez - E, F.e);
     }
+    return F;
+}
+
+// HLL flux of kernel.cu:1485-1609 in a local frame (same arguments and results as
+// hllc_local): sound speed 0 where rho <= 0, D_L = min(un) - max(c), D_R = max(un) + max(c),
+// the upwind physical flux when the fan lies on one side of the face (strict tests against
+// Omega = 0, kernel.cu:11), else (D_R F_L - D_L F_R + D_L D_R (U_R - U_L)) / (D_R - D_L).
+__device__ __forceinline__ FluxE hll_local(double rL, double pL, double unL, double utL,
+                                           double rR, double pR, double unR, double utR,
+                                           const Params& P, double& UU) {
+    const double g = P.gamma;
+    const double gpL = g * pL, gpR = g * pR;
+    const double cL = le_zero(rL) ? 0.0 : gpL * rsqrt_fast(gpL * rL);  // sqrt(g p / rho)
+    const double cR = le_zero(rR) ? 0.0 : gpR * rsqrt_fast(gpR * rR);
+    const double cm = max_nonneg(cL, cR);
+    const double DL = dmin(unL, unR) - cm;
+    const double DR = dmax(unL, unR) + cm;
+    UU = max_nonneg(dabs(DL), dabs(DR));
+    const bool left = gt_zero(DL), right = !left && lt_zero(DR);
+    FluxE F;
+    if (left || right) {  // one side's physical flux
+        const double r = left ? rL : rR, p = left ? pL : pR;
+        const double un = left ? unL : unR, ut = left ? utL : utR;
+        F.m = r * un;
+        F.mn = fma(F.m, un, p);
+        F.mt = F.m * ut;
+        const double E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
+        F.e = (E + p) * un;
+        return F;
+    }
+    const double mL = rL * unL, mR = rR * unR;
+    const double EL = fma(pL, P.inv_gm1, 0.5 * rL * fma(unL, unL, utL * utL));
+    const double ER = fma(pR, P.inv_gm1, 0.5 * rR * fma(unR, unR, utR * utR));
+    const double inv = rcp_fast(DR - DL);
+    const double dd = DL * DR;
+    // (D_R F_L - D_L F_R + D_L D_R dU) / (D_R - D_L), component by component
+    F.m = fma(dd, rR - rL, fma(DR, mL, -DL * mR)) * inv;
+    F.mn = fma(dd, mR - mL, fma(DR, fma(mL, unL, pL), -DL * fma(mR, unR, pR))) * inv;
+    F.mt = fma(dd, fma(rR, utR, -rL * utL), fma(DR, mL * utL, -DL * (mR * utR))) * inv;
+    F.e = fma(dd, ER - EL, fma(DR, (EL + pL) * unL, -DL * ((ER + pR) * unR))) * inv;
     return F;
 }
 
@@ -210,8 +256,12 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
             }
         }
         double UU;
-        const FluxE F = hllc_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
-                                   qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU);
+        const FluxE F =
+            P.method == GD_METHOD_HLL
+                ? hll_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], qb[0], qb[1],
+                            isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU)
+                : hllc_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], qb[0], qb[1],
+                             isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU);
         if (isx) {
             double* fo = fx + ly * (TX + 1) + lx;
             fo[0 * TY * (TX + 1)] = F.m;
@@ -241,14 +291,11 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
         const double* c = prim + (ly + H) * SX + (lx + H);
         const double r = c[0], p = c[SY * SX], u = c[2 * SY * SX], v = c[3 * SY * SX];
         const long long k = (long long)gy * N + gx;
-        if (P.frozen_radius > 0.0) {
-            const double x = P.x0 + gx * P.dx, y = P.y0 + gy * P.dy;
-            if (sqrt(x * x + y * y) < P.frozen_radius) {
-                if (!dt_only) {
-                    out.f[0][k] = r; out.f[1][k] = p; out.f[2][k] = u; out.f[3][k] = v;
-                }
-                continue;
+        if (P.frozen_radius > 0.0 && !cell_active(P, gx, gy)) {  // the faces' own test
+            if (!dt_only) {
+                out.f[0][k] = r; out.f[1][k] = p; out.f[2][k] = u; out.f[3][k] = v;
             }
+            continue;
         }
         any_active = true;
         if (dt_only) continue;
@@ -267,7 +314,7 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
         const double inv = rcp_fast(r2);
         const double u2 = fma(r, u, -d[2]) * inv;
         const double v2 = fma(r, v, -d[3]) * inv;
-        double p2 = ((E - d[1]) - 0.5 * r2 * fma(u2, u2, v2 * v2)) * P.gm1;
+        double p2 = fma(-0.5 * r2, fma(u2, u2, v2 * v2), E - d[1]) * P.gm1;
         if (le_zero(p2)) { p2 = 0.000001; ++nfl_p; }
         if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2)) ++nbad;
         out.f[0][k] = r2;

@@ -36,6 +36,64 @@ __device__ __forceinline__ void lin2(double x1, double t1, double x2, double t2,
 
 // Euler HLLC of kernel.cu:853-1165 for B = 0: basis (n, e_z, (-n2, n1, 0)).
 // L, R = {rho, p, vx, vy}; out = {F_rho, F_E, F_mx, F_my}; returns krit*rad/UU.
+// the reference's my_min / my_max (kernel.cu:102-124), which HLL uses
+__device__ __forceinline__ double my_min(double a, double b) { return a <= b ? a : b; }
+__device__ __forceinline__ double my_max(double a, double b) { return a >= b ? a : b; }
+
+// Euler HLL of kernel.cu:1485-1609, term by term in the reference's order: sound speeds 0
+// for rho <= 0, speeds min/max of the normal velocities -+ the larger sound speed, the
+// upwind flux when the fan does not straddle the face (Omega = 0, kernel.cu:11), else the
+// HLL average.  out = {F_rho, F_E, F_mx, F_my}; returns krit rad / max(|D_L|, |D_R|).
+__device__ double hll_ref(const double* L, const double* R, double n1, double n2, double rad,
+                          const Params& P, double* out) {
+    const double g = P.gamma;
+    const double ro_L = L[0], p_L = L[1], v1_L = L[2], v2_L = L[3];
+    const double ro_R = R[0], p_R = R[1], v1_R = R[2], v2_R = R[3];
+    const double Vkv_L = v1_L * v1_L + v2_L * v2_L;
+    const double Vkv_R = v1_R * v1_R + v2_R * v2_R;
+    const double c_L = ro_L <= 0 ? 0.0 : sqrt(g * p_L / ro_L);
+    const double c_R = ro_R <= 0 ? 0.0 : sqrt(g * p_R / ro_R);
+    const double e_L = p_L / (g - 1.0) + ro_L * Vkv_L / 2.0;
+    const double e_R = p_R / (g - 1.0) + ro_R * Vkv_R / 2.0;
+    const double Vn_L = v1_L * n1 + v2_L * n2;
+    const double Vn_R = v1_R * n1 + v2_R * n2;
+    const double D_L = my_min(Vn_L, Vn_R) - my_max(c_L, c_R);
+    const double D_R = my_max(Vn_L, Vn_R) + my_max(c_L, c_R);
+    double t = 10000000;
+    t = my_min(t, P.krit * rad / my_max(fabs(D_L), fabs(D_R)));
+    const double fl_1 = (ro_L * v1_L) * n1 + (ro_L * v2_L) * n2;
+    const double fl_2 = (ro_L * v1_L * v1_L + p_L) * n1 + (ro_L * v1_L * v2_L) * n2;
+    const double fl_3 = (ro_L * v1_L * v2_L) * n1 + (ro_L * v2_L * v2_L + p_L) * n2;
+    const double fl_5 = ((e_L + p_L) * v1_L) * n1 + ((e_L + p_L) * v2_L) * n2;
+    if (D_L > 0.0) {
+        out[0] = fl_1;
+        out[1] = fl_5;
+        out[2] = fl_2;
+        out[3] = fl_3;
+        return t;
+    }
+    const double fr_1 = (ro_R * v1_R) * n1 + (ro_R * v2_R) * n2;
+    const double fr_2 = (ro_R * v1_R * v1_R + p_R) * n1 + (ro_R * v1_R * v2_R) * n2;
+    const double fr_3 = (ro_R * v1_R * v2_R) * n1 + (ro_R * v2_R * v2_R + p_R) * n2;
+    const double fr_5 = ((e_R + p_R) * v1_R) * n1 + ((e_R + p_R) * v2_R) * n2;
+    if (D_R < 0.0) {
+        out[0] = fr_1;
+        out[1] = fr_5;
+        out[2] = fr_2;
+        out[3] = fr_3;
+        return t;
+    }
+    const double dq1 = ro_R - ro_L;
+    const double dq2 = ro_R * v1_R - ro_L * v1_L;
+    const double dq3 = ro_R * v2_R - ro_L * v2_L;
+    const double dq5 = e_R - e_L;
+    out[0] = (D_R * fl_1 - D_L * fr_1 + D_L * D_R * dq1) / (D_R - D_L);
+    out[2] = (D_R * fl_2 - D_L * fr_2 + D_L * D_R * dq2) / (D_R - D_L);
+    out[3] = (D_R * fl_3 - D_L * fr_3 + D_L * D_R * dq3) / (D_R - D_L);
+    out[1] = (D_R * fl_5 - D_L * fr_5 + D_L * D_R * dq5) / (D_R - D_L);
+    return t;
+}
+
 __device__ double hllc_ref(const double* L, const double* R, double n1, double n2, double rad,
                            const Params& P, double* out) {
     const double g = P.gamma, g1 = P.gamma - 1.0;
@@ -351,7 +409,10 @@ __global__ void __launch_bounds__(PNT) parity_kernel(Params P, CPlanes in, Plane
                 for (int fc = 0; fc < 4; ++fc) {
                     const double rad = (fc == 0 || fc == 2) ? dy : dx;
                     double o[4];
-                    const double tf = hllc_ref(own[fc], nbr[fc], kFaceN1[fc], kFaceN2[fc], rad, P, o);
+                    const double tf =
+                        P.method == GD_METHOD_HLL
+                            ? hll_ref(own[fc], nbr[fc], kFaceN1[fc], kFaceN2[fc], rad, P, o)
+                            : hllc_ref(own[fc], nbr[fc], kFaceN1[fc], kFaceN2[fc], rad, P, o);
                     tmin = ref_min(tmin, tf);
                     Ps[fc][0] = o[0]; Ps[fc][1] = o[1]; Pu[fc][0] = o[2]; Pu[fc][1] = o[3];
                 }

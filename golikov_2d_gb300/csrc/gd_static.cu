@@ -67,8 +67,9 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
     const long long K = (long long)cfg->N * cfg->M;
     if (K > GD_STATIC_MAX_CELLS) return GD_ERR_INVALID_ARG;  // beyond the fixed scratch
     gd::Params P = gd::params_from_config(*cfg);
-    if (method > 0) {
-        if (cfg->physics == GD_EULER && method != GD_METHOD_HLLC) return GD_ERR_INVALID_ARG;
+    if (method != GD_METHOD_CONFIG) {
+        if (cfg->physics == GD_EULER && method != GD_METHOD_HLLC && method != GD_METHOD_HLL)
+            return GD_ERR_INVALID_ARG;
         if (cfg->physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
             return GD_ERR_INVALID_ARG;
         P.method = method;

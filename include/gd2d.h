@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GD_ABI_VERSION 1
+#define GD_ABI_VERSION 2
 
 typedef void* gd_stream; /* cudaStream_t */
 
@@ -38,10 +38,15 @@ typedef enum {
 enum { GD_EULER = 0, GD_MHD = 1 };
 /* geometry: Cartesian, or axisymmetric with y the radius (kernel.cu:2615, 2619-2648) */
 enum { GD_CARTESIAN = 0, GD_AXISYM = 1 };
-/* flux method codes are the reference's `method` argument (kernel.cu:1795, Kernel_TVD's
- * HLLDQ_Korolkov metod): 1 = HLLC (Euler, HLLC_Aleksashov kernel.cu:853),
- * 2 = HLLC-MHD (Gas_Dinamic.cu:1137), 3 = HLLD (Gas_Dinamic.cu:1303). */
-enum { GD_METHOD_HLLC = 1, GD_METHOD_HLLC_MHD = 2, GD_METHOD_HLLD = 3 };
+/* flux method codes are the reference's `method` argument (Ker_Dekard kernel.cu:1795 and
+ * Kernel_TVD_old kernel.cu:3547 for Euler, Kernel_TVD's HLLDQ_Korolkov metod for MHD):
+ * 0 = HLL (Euler, kernel.cu:1485), 1 = HLLC (Euler, HLLC_Aleksashov kernel.cu:853; the
+ * reference's method 1 switches to HLL only on faces below hx = -3288, hy = 0, kernel.cu:26-27,
+ * i.e. nowhere on its domains), 2 = HLLC-MHD (Gas_Dinamic.cu:1137), 3 = HLLD
+ * (Gas_Dinamic.cu:1303).  GD_METHOD_CONFIG (-1) in a per-call argument means the context's
+ * configured method. */
+enum { GD_METHOD_HLL = 0, GD_METHOD_HLLC = 1, GD_METHOD_HLLC_MHD = 2, GD_METHOD_HLLD = 3 };
+#define GD_METHOD_CONFIG (-1)
 /* boundary conditions, one per side (left, right, bottom, top); two ghost layers each */
 enum {
     GD_BC_PERIODIC = 0,      /* wrap; both sides of an axis must be periodic              */
@@ -111,7 +116,8 @@ int gd_abi_version(void);
  *   Kernel_TVD<<<K/256,256>>>(s,u,b,s2,u2,b2,T,T_do,i,method)  (kernel.cu:2198, 4113)
  *   add2<<<...>>>(...)            when cfg.order == 1, physics MHD (kernel.cu:1877, 4042)
  *   Ker_Dekard<<<...>>>(...)      when cfg.order == 1, physics Euler (kernel.cu:1736)
- * method <= 0 uses cfg.method.  `i` is the reference's step counter (unused, as there).
+ * method is the reference's code (GD_METHOD_*), GD_METHOD_CONFIG (-1) uses cfg.method.  `i`
+ * is the reference's step counter (unused, as there).
  * All pointers are device pointers; s/s2 etc. must not alias.  Unlike the reference, the
  * dt minimum is exact and deterministic (no racy read-compare-write, kernel.cu:2607-2611),
  * and the launch needs no K % 256 == 0. */

@@ -109,8 +109,9 @@ class Oracle:
         L.gdo_linear.argtypes = [_d] * 7
         L.gdo_linear2.restype = None
         L.gdo_linear2.argtypes = [_d] * 8 + [_pd, _pd]
-        L.gdo_hllc.restype = _d
-        L.gdo_hllc.argtypes = [_pd, _pd, _d, _d, _d, _d, _d, _pd]
+        for name in ("gdo_hllc", "gdo_hll"):
+            getattr(L, name).restype = _d
+            getattr(L, name).argtypes = [_pd, _pd, _d, _d, _d, _d, _d, _pd]
         L.gdo_hlld.restype = _d
         L.gdo_hlld.argtypes = [_pd, _pd, _d, _d, _d, _d, _i, _d, _d, _pd]
         L.gdo_step.restype = _d
@@ -174,6 +175,13 @@ class Oracle:
         R = np.ascontiguousarray(R, np.float64)
         out = np.zeros(4)
         t = self.lib.gdo_hllc(_ptr(L), _ptr(R), n1, n2, rad, gamma, krit, _ptr(out))
+        return t, out
+
+    def hll(self, L, R, n1, n2, rad, gamma, krit):
+        L = np.ascontiguousarray(L, np.float64)
+        R = np.ascontiguousarray(R, np.float64)
+        out = np.zeros(4)
+        t = self.lib.gdo_hll(_ptr(L), _ptr(R), n1, n2, rad, gamma, krit, _ptr(out))
         return t, out
 
     def hlld(self, L, R, n1, n2, n3, rad, method, gamma, krit):
@@ -262,6 +270,13 @@ class Reference:
         R = np.ascontiguousarray(R, np.float64)
         out = np.zeros(4)
         t = self.lib.gdref_hllc(_ptr(L), _ptr(R), n1, n2, rad, _ptr(out))
+        return t, out
+
+    def hll(self, L, R, n1, n2, rad):
+        L = np.ascontiguousarray(L, np.float64)
+        R = np.ascontiguousarray(R, np.float64)
+        out = np.zeros(4)
+        t = self.lib.gdref_hll(_ptr(L), _ptr(R), n1, n2, rad, _ptr(out))
         return t, out
 
     def hlld(self, L, R, n1, n2, n3, rad, method):

@@ -60,6 +60,57 @@ void gdo_linear2(double x1, double t1, double x2, double t2, double x3, double t
 }
 
 /* ------------------------------------------------------------------------------------- */
+/* Euler HLL: kernel.cu:1485-1609.  my_min / my_max as kernel.cu:102-124; Omega = 0          */
+/* (kernel.cu:11).  out = {F_rho, F_E, F_mx, F_my}.                                         */
+/* ------------------------------------------------------------------------------------- */
+
+static double my_min(double a, double b) { return a <= b ? a : b; }
+static double my_max(double a, double b) { return a >= b ? a : b; }
+
+double gdo_hll(const double* L, const double* R, double n1, double n2, double rad,
+               double gamma, double krit, double* out) {
+    const double ro_L = L[0], p_L = L[1], v1_L = L[2], v2_L = L[3];
+    const double ro_R = R[0], p_R = R[1], v1_R = R[2], v2_R = R[3];
+    const double Vkv_L = v1_L * v1_L + v2_L * v2_L;
+    const double Vkv_R = v1_R * v1_R + v2_R * v2_R;
+    const double c_L = ro_L <= 0 ? 0.0 : sqrt(gamma * p_L / ro_L);
+    const double c_R = ro_R <= 0 ? 0.0 : sqrt(gamma * p_R / ro_R);
+    const double e_L = p_L / (gamma - 1.0) + ro_L * Vkv_L / 2.0;
+    const double e_R = p_R / (gamma - 1.0) + ro_R * Vkv_R / 2.0;
+    const double Vn_L = v1_L * n1 + v2_L * n2;
+    const double Vn_R = v1_R * n1 + v2_R * n2;
+    const double D_L = my_min(Vn_L, Vn_R) - my_max(c_L, c_R);
+    const double D_R = my_max(Vn_L, Vn_R) + my_max(c_L, c_R);
+    double t = 10000000;
+    t = my_min(t, krit * rad / my_max(fabs(D_L), fabs(D_R)));
+    const double fl_1 = (ro_L * v1_L) * n1 + (ro_L * v2_L) * n2;
+    const double fl_2 = (ro_L * v1_L * v1_L + p_L) * n1 + (ro_L * v1_L * v2_L) * n2;
+    const double fl_3 = (ro_L * v1_L * v2_L) * n1 + (ro_L * v2_L * v2_L + p_L) * n2;
+    const double fl_5 = ((e_L + p_L) * v1_L) * n1 + ((e_L + p_L) * v2_L) * n2;
+    if (D_L > 0.0) {
+        out[0] = fl_1; out[1] = fl_5; out[2] = fl_2; out[3] = fl_3;
+        return t;
+    }
+    const double fr_1 = (ro_R * v1_R) * n1 + (ro_R * v2_R) * n2;
+    const double fr_2 = (ro_R * v1_R * v1_R + p_R) * n1 + (ro_R * v1_R * v2_R) * n2;
+    const double fr_3 = (ro_R * v1_R * v2_R) * n1 + (ro_R * v2_R * v2_R + p_R) * n2;
+    const double fr_5 = ((e_R + p_R) * v1_R) * n1 + ((e_R + p_R) * v2_R) * n2;
+    if (D_R < 0.0) {
+        out[0] = fr_1; out[1] = fr_5; out[2] = fr_2; out[3] = fr_3;
+        return t;
+    }
+    const double dq1 = ro_R - ro_L;
+    const double dq2 = ro_R * v1_R - ro_L * v1_L;
+    const double dq3 = ro_R * v2_R - ro_L * v2_L;
+    const double dq5 = e_R - e_L;
+    out[0] = (D_R * fl_1 - D_L * fr_1 + D_L * D_R * dq1) / (D_R - D_L);
+    out[2] = (D_R * fl_2 - D_L * fr_2 + D_L * D_R * dq2) / (D_R - D_L);
+    out[3] = (D_R * fl_3 - D_L * fr_3 + D_L * D_R * dq3) / (D_R - D_L);
+    out[1] = (D_R * fl_5 - D_L * fr_5 + D_L * D_R * dq5) / (D_R - D_L);
+    return t;
+}
+
+/* ------------------------------------------------------------------------------------- */
 /* Euler HLLC: HLLC_Aleksashov, kernel.cu:853-1165, with B = 0 and v_z = 0.               */
 /* ------------------------------------------------------------------------------------- */
 
@@ -548,7 +599,10 @@ static double euler_cell(const gdo_config* c, const cell_faces* F, double y, dou
         const double R[4] = {z->r, z->p, z->u, z->v};
         const double rad = (f == 0 || f == 2) ? dy : dx; /* kernel.cu:3562-3586 */
         double o[4];
-        tmin = mn(tmin, gdo_hllc(L, R, FACE_N1[f], FACE_N2[f], rad, gamma, c->krit, o));
+        /* method 0 = HLL everywhere (Ker_Dekard / Kernel_TVD_old, kernel.cu:1796, 3547) */
+        tmin = mn(tmin, c->method == 0
+                            ? gdo_hll(L, R, FACE_N1[f], FACE_N2[f], rad, gamma, c->krit, o)
+                            : gdo_hllc(L, R, FACE_N1[f], FACE_N2[f], rad, gamma, c->krit, o));
         Ps[f][0] = o[0]; Ps[f][1] = o[1]; Pu[f][0] = o[2]; Pu[f][1] = o[3];
     }
     const double PSx = Ps[0][0] * dy + Ps[1][0] * dx + Ps[2][0] * dy + Ps[3][0] * dx;

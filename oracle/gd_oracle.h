@@ -54,6 +54,8 @@ void gdo_linear2(double x1, double t1, double x2, double t2, double x3, double t
 
 /* Euler HLLC, kernel.cu:853-1165.  L, R = {rho, p, vx, vy}; normal (n1, n2) axis-aligned.
  * out = {F_rho, F_E, F_mx, F_my}.  Returns krit*rad/max(|SL|,|SR|). */
+double gdo_hll(const double* L, const double* R, double n1, double n2, double rad,
+               double gamma, double krit, double* out);
 double gdo_hllc(const double* L, const double* R, double n1, double n2, double rad,
                 double gamma, double krit, double* out);
 

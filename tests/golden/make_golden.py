@@ -15,6 +15,8 @@ Fixtures:
                    small random grids with the reference's own boundary conditions
   run_native.npz   20 steps of the reference protocol (Kernel_TVD + funk_time) from the
                    reference's wind initial condition on a reduced axisymmetric grid
+  faces_hll.npz    Euler HLL (kernel.cu:1485) on random and branch-targeted faces, and one
+                   Ker_Dekard step with method 0 (HLL everywhere)
   io_files.npz     the reference's state files for one random state with hard-to-print
                    values: print_file_mini / print_file_mini2 (both overloads) Tecplot
                    snapshots (kernel.cu:3682-3808) and the restart dump of its main loop
@@ -182,6 +184,33 @@ def run_native(ref, nsteps=20):
                         nsteps=nsteps, s0=s0, u0=u0, b0=b0, s=s, u=u, b=b, T_do=T_do, TT=TT)
 
 
+def hll_golden(ref):
+    """HLL (kernel.cu:1485-1609) on random and branch-targeted faces, plus one Ker_Dekard step
+    with method 0 (HLL everywhere, kernel.cu:1796-1802)."""
+    rng = np.random.default_rng(SEED + 11)
+    n = 1600
+    L, R = euler_states(rng, n)
+    k = n // 8
+    L[6 * k:6 * k + k // 2, 0] = 0.0                  # rho <= 0: sound speed 0
+    R[6 * k + k // 2:7 * k, 0] = -rng.uniform(0, 1, k - k // 2)
+    L[7 * k:, 2] = R[7 * k:, 2]                       # equal normal speeds (ties in min/max)
+    nrm = NORMALS[rng.integers(0, 4, n)]
+    gam = np.where(rng.uniform(size=n) < 0.5, 1.4, 5.0 / 3.0)
+    T = np.zeros(n)
+    F = np.zeros((n, 4))
+    for i in range(n):
+        ref.set_params(gam[i], 0.4, 64, 64, 1.0, 1.0)
+        T[i], F[i] = ref.hll(L[i], R[i], nrm[i, 0], nrm[i, 1], 1.0 / 128)
+    N, M, xmax, ymax = 40, 24, 9.0, 5.0
+    s, u, _ = random_state(rng, N * M)
+    T_do = 2e-3
+    ref.set_params(1.4, 0.4, N, M, xmax, ymax)
+    s2, u2, T1 = ref.ker_dekard(s, u, T_do, method=0)
+    np.savez_compressed(os.path.join(HERE, "faces_hll.npz"), L=L, R=R, normal=nrm, gamma=gam,
+                        krit=0.4, rad=1.0 / 128, t=T, flux=F, N=N, M=M, xmax=xmax, ymax=ymax,
+                        s=s, u=u, T_do=T_do, dek_s=s2, dek_u=u2, dek_T=T1)
+
+
 def io_state(rng, K):
     """A state whose numbers exercise every branch of %g: magnitudes 1e-8..1e3, negative
     and zero densities (the Tecplot writer's rho > 0 branch), signed zeros, exact decimal
@@ -228,7 +257,7 @@ def main():
     ref = oracle.Reference()
     ref.lib.gdref_set_threads(1)
     jobs = {"faces": faces, "recon": recon, "step_native": step_native,
-            "run_native": run_native, "io_files": io_files}
+            "run_native": run_native, "io_files": io_files, "hll": hll_golden}
     for name in (sys.argv[1:] or list(jobs)):
         jobs[name](ref)
     for f in sorted(os.listdir(HERE)):

@@ -18,7 +18,7 @@ def to_dev(a):
     return None if a is None else torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def gpu_step_ref(cfg, s, u, b, T_do, method=0):
+def gpu_step_ref(cfg, s, u, b, T_do, method=g.METHOD_CONFIG):
     """One step through gd_step_ref (device pointers, reference layout)."""
     import torch
     sol = g.Solver(cfg)

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(gdlib):
 
 
 def test_abi_version_and_status_strings(gdlib):
-    assert gdlib.gd_abi_version() == 1
+    assert gdlib.gd_abi_version() == 2
     assert gdlib.gd_status_string(0) == b"ok"
     assert gdlib.gd_status_string(1) == b"invalid argument"
 

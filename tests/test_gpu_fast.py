@@ -20,7 +20,17 @@ pytestmark = pytest.mark.gpu
 PER_STEP_TOL = 1e-12
 NSTEP_TOL = 1e-9
 
+def hll(case):
+    cfg, s, u, b = case
+    cfg.method = g.METHOD_HLL
+    return cfg, s, u, b
+
+
 EULER_CASES = {
+    "sod256_hll": lambda: hll(problems.sod(256, 256)),
+    "kh128_hll": lambda: hll(problems.kelvin_helmholtz(128, 128)),
+    "quad97_hll": lambda: hll(problems.four_quadrant(97, np.random.default_rng(7))),
+    "sod_o1_hll": lambda: (lambda c: (setattr(c[0], "order", 1), c)[1])(hll(problems.sod(80, 40))),
     "sod256": lambda: problems.sod(256, 256),
     "kh128": lambda: problems.kelvin_helmholtz(128, 128),
     "quad97": lambda: problems.four_quadrant(97, np.random.default_rng(7)),
@@ -57,6 +67,16 @@ def test_fast_sod_200_steps(cuda, oracle_lib):
     r = sg[:, 0].reshape(cfg.M, cfg.N)
     assert np.array_equal(r, np.broadcast_to(r[0], r.shape))
     assert st.rho_floor_hits == 0 and st.nonfinite == 0
+
+
+def test_fast_sod_hll_200_steps(cuda, oracle_lib):
+    """Sod 256^2 with the HLL flux (method 0), 200 steps of the full protocol."""
+    cfg, s, u, b = hll(problems.sod(256, 256))
+    so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 200)
+    sg, ug, bg, st = gpu_run(cfg, s, u, b, 200)
+    err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
+    assert err <= NSTEP_TOL, err
+    assert abs(st.t - TT) <= 1e-10 * TT
 
 
 def test_fast_periodic_conservation(cuda):

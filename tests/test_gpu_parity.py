@@ -64,7 +64,34 @@ def test_native_run_matches_reference(cuda, use_graph):
     assert np.array_equal(s, gz["s"]) and np.array_equal(u, gz["u"]) and np.array_equal(b, gz["b"])
 
 
+def test_native_euler_first_order_hll_matches_reference(cuda):
+    """Ker_Dekard with method 0 (HLL everywhere, kernel.cu:1796-1802), golden from the
+    reference; the method passed per call as the reference passes it."""
+    gz = golden("faces_hll.npz")
+    cfg = native_cfg(gz, 1, 1, physics=g.EULER)
+    s2, u2, _, T = gpu_step_ref(cfg, gz["s"], gz["u"], None, float(gz["T_do"]),
+                                method=g.METHOD_HLL)
+    N, M = cfg.N, cfg.M
+    mask = np.zeros((M, N), bool)
+    mask[: M - 1, : N - 1] = True
+    mask = mask.ravel()
+    assert np.array_equal(s2[mask], gz["dek_s"][mask])
+    assert np.array_equal(u2[mask], gz["dek_u"][mask])
+
+
+def hll(case):
+    cfg, s, u, b = case
+    cfg.method = g.METHOD_HLL
+    return cfg, s, u, b
+
+
 CASES = {
+    "sod64_hll": lambda: hll(problems.sod(64, 48, mode=g.MODE_PARITY)),
+    "kh64_hll": lambda: hll(problems.kelvin_helmholtz(64, 64, mode=g.MODE_PARITY)),
+    "quad50_hll": lambda: hll(problems.four_quadrant(50, np.random.default_rng(5),
+                                                     mode=g.MODE_PARITY)),
+    "sod_o1_hll": lambda: (lambda c: (setattr(c[0], "order", 1), c)[1])(
+        hll(problems.sod(48, 32, mode=g.MODE_PARITY))),
     "sod64": lambda: problems.sod(64, 48, mode=g.MODE_PARITY),
     "kh64": lambda: problems.kelvin_helmholtz(64, 64, mode=g.MODE_PARITY),
     "ot48_hlld": lambda: problems.orszag_tang(48, 48, method=g.METHOD_HLLD, mode=g.MODE_PARITY),

@@ -123,3 +123,22 @@ def test_state_file_writers(oracle_lib, tmp_path):
                        ("tec_mhd_t", b, float(g["ttt"]))):
         oracle_lib.write_tecplot(grid, s, u, bb, int(g["nmin"]), xmin, xmax, ymin, ymax, p, t)
         assert open(p, "rb").read() == g[key].tobytes(), key
+
+
+def test_hll_faces_and_first_order_step(oracle_lib):
+    """HLL (kernel.cu:1485) on golden faces, and Ker_Dekard with method 0 (kernel.cu:1796)."""
+    g = golden("faces_hll.npz")
+    for i in range(len(g["t"])):
+        t, F = oracle_lib.hll(g["L"][i], g["R"][i], g["normal"][i, 0], g["normal"][i, 1],
+                              float(g["rad"]), float(g["gamma"][i]), float(g["krit"]))
+        assert t == g["t"][i]
+        assert np.array_equal(F, g["flux"][i], equal_nan=True), (i, F, g["flux"][i])
+    grid = native_grid(g, 1, 0, physics=oracle.EULER)
+    grid.method = 0
+    s2, u2, _, T = oracle_lib.step(grid, g["s"], g["u"], None, float(g["T_do"]))
+    N, M = grid.N, grid.M
+    mask = np.zeros((M, N), bool)
+    mask[: M - 1, : N - 1] = True  # Ker_Dekard leaves the last column and row unwritten
+    mask = mask.ravel()
+    assert np.array_equal(s2[mask], g["dek_s"][mask])
+    assert np.array_equal(u2[mask], g["dek_u"][mask])

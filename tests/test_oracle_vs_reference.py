@@ -81,3 +81,18 @@ def test_state_file_writers_random(oracle_lib, reference, tmp_path, seed, N, M):
         oracle_lib.write_tecplot(grid, s, u, bb, 3, xmax / (2.0 * N), xmax, ymax / (2.0 * M),
                                  ymax, po, t)
         assert open(pr, "rb").read() == open(po, "rb").read(), wb
+
+
+@pytest.mark.parametrize("gamma", [1.4, 5.0 / 3.0])
+def test_hll_random_faces(oracle_lib, reference, gamma):
+    rng = np.random.default_rng(44)
+    reference.set_params(gamma, 0.4, 64, 64, 1.0, 1.0)
+    for _ in range(400):
+        L = np.array([rng.uniform(-0.1, 3), rng.uniform(0.01, 3), rng.uniform(-8, 8),
+                      rng.uniform(-8, 8)])
+        R = np.array([rng.uniform(-0.1, 3), rng.uniform(0.01, 3), rng.uniform(-8, 8),
+                      rng.uniform(-8, 8)])
+        n1, n2 = [(1.0, 0.0), (0.0, -1.0), (-1.0, 0.0), (0.0, 1.0)][rng.integers(0, 4)]
+        t0, F0 = reference.hll(L, R, n1, n2, 0.01)
+        t1, F1 = oracle_lib.hll(L, R, n1, n2, 0.01, gamma, 0.4)
+        assert t0 == t1 and np.array_equal(F0, F1, equal_nan=True)

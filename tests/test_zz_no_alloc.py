@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 PER_STEP_TOL = 1e-12
 
 
-def static_step(cfg, s, u, b, T_do, method=0):
+def static_step(cfg, s, u, b, T_do, method=g.METHOD_CONFIG):
     """One call of gd_step_ref_static on device copies of (s, u, b)."""
     import torch
     L = g.load()
@@ -73,7 +73,7 @@ def test_static_step_rejects_grids_beyond_its_scratch(cuda):
     Tdo = torch.tensor([1e-5], dtype=torch.float64, device="cuda")
     st = L.gd_step_ref_static(ctypes.byref(cfg.cstruct()), ds.data_ptr(), du.data_ptr(), None,
                               s2.data_ptr(), u2.data_ptr(), None, T.data_ptr(), Tdo.data_ptr(),
-                              0, None)
+                              g.METHOD_CONFIG, None)
     torch.cuda.synchronize()
     assert st == 1
     assert bool((s2 == 7.0).all()) and float(T.cpu()[0]) == 1e7
