@@ -28,6 +28,12 @@ METHOD_HLL, METHOD_HLLC, METHOD_HLLC_MHD, METHOD_HLLD = 0, 1, 2, 3
 METHOD_CONFIG = -1  # per-call method argument: the context's configured method
 (BC_PERIODIC, BC_TRANSMISSIVE, BC_MIRROR_X, BC_AXIS, BC_AMBIENT, BC_OUTFLOW,
  BC_AMBIENT_KEEPB) = range(7)
+# spatial scheme: minmod TVD / first order (Kernel_TVD, add2, Ker_Dekard), or the
+# MUSCL-Hancock predictor-corrector of Kernel_GKR as written (v_y slopes from the
+# pressures) or with v_y slopes from v_y
+SCHEME_TVD, SCHEME_HANCOCK_REF, SCHEME_HANCOCK = 0, 1, 2
+# the only setting Kernel_GKR is written for: left, right, bottom, top
+HANCOCK_BC = (BC_MIRROR_X, BC_OUTFLOW, BC_AXIS, BC_AMBIENT_KEEPB)
 MODE_FAST, MODE_PARITY = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "non-finite state",
@@ -66,6 +72,8 @@ class gd_config(ctypes.Structure):
         ("bc", ctypes.c_int * 4),
         ("frozen_radius", ctypes.c_double),
         ("mode", ctypes.c_int),
+        ("scheme", ctypes.c_int),
+        ("x_max", ctypes.c_double), ("y_max", ctypes.c_double),
     ]
 
 
@@ -196,6 +204,9 @@ class Config:
     bc: tuple = (BC_TRANSMISSIVE,) * 4
     frozen_radius: float = 0.0
     mode: int = MODE_FAST
+    scheme: int = SCHEME_TVD
+    x_max: float = 0.0  # domain extents used by the Hancock schemes' cell coordinates
+    y_max: float = 0.0
 
     def cstruct(self) -> gd_config:
         c = gd_config()

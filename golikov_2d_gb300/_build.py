@@ -1,9 +1,9 @@
 """Compiles the CUDA library ``libgd2d.so`` for sm_103a with nvcc.
 
 Each ``csrc/*.cu`` is compiled to an object in ``_build/`` (in parallel, skipped when
-up to date), then linked into ``golikov_2d_gb300/libgd2d.so``.  ``gd_parity.cu`` is built
-with ``--fmad=false``: the parity kernels must not contract multiply-adds, so that their
-results match the reference's arithmetic bit for bit.
+up to date), then linked into ``golikov_2d_gb300/libgd2d.so``.  ``gd_parity.cu`` and
+``gd_hancock.cu`` are built with ``--fmad=false``: the parity kernels must not contract
+multiply-adds, so that their results match the reference's arithmetic bit for bit.
 """
 from __future__ import annotations
 
@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "--expt-relaxed-constexpr", "-I", INCLUDE]
 # gd_parity.cu: the reference's operations, unfused
-PER_FILE = {"gd_parity.cu": ["--fmad=false"]}
+PER_FILE = {"gd_parity.cu": ["--fmad=false"], "gd_hancock.cu": ["--fmad=false"]}
 
 
 def nvcc() -> str:

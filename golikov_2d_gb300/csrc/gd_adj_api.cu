@@ -43,7 +43,8 @@ bool adj_supported(const gd_ctx* ctx) {
     const gd_config& c = ctx->cfg;
     for (int s = 0; s < 4; ++s)
         if (c.bc[s] != GD_BC_PERIODIC) return false;
-    return c.physics == GD_MHD && c.method == GD_METHOD_HLLD && c.order == 2 &&
+    return c.scheme == GD_SCHEME_TVD && c.physics == GD_MHD && c.method == GD_METHOD_HLLD &&
+           c.order == 2 &&
            c.geometry == GD_CARTESIAN && c.mode == GD_MODE_FAST && c.frozen_radius == 0.0;
 }
 

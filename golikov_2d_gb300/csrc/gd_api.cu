@@ -65,6 +65,17 @@ gd_status validate(const gd_config* c) {
     // the axisymmetric sources divide by the radius y of every cell centre
     if (c->geometry == GD_AXISYM && !(c->y0 > 0.0)) return GD_ERR_INVALID_ARG;
     if (!(std::isfinite(c->frozen_radius) && c->frozen_radius >= 0.0)) return GD_ERR_INVALID_ARG;
+    if (c->scheme < GD_SCHEME_TVD || c->scheme > GD_SCHEME_HANCOCK) return GD_ERR_INVALID_ARG;
+    if (c->scheme != GD_SCHEME_TVD) {
+        if (!finite_pos(c->x_max) || !finite_pos(c->y_max)) return GD_ERR_INVALID_ARG;
+        // Kernel_GKR is written for one setting: axisymmetric MHD, HLLD faces (its metod 3,
+        // kernel.cu:3123-3233) and its own ghost cells on the four sides (kernel.cu:2701-2960)
+        const int want[4] = {GD_BC_MIRROR_X, GD_BC_OUTFLOW, GD_BC_AXIS, GD_BC_AMBIENT_KEEPB};
+        if (c->physics != GD_MHD || c->geometry != GD_AXISYM || c->method != GD_METHOD_HLLD)
+            return GD_ERR_UNSUPPORTED;
+        for (int s = 0; s < 4; ++s)
+            if (c->bc[s] != want[s]) return GD_ERR_UNSUPPORTED;
+    }
     return GD_OK;
 }
 
@@ -84,6 +95,9 @@ Params make_params(const gd_config& c) {
     P.gamma = c.gamma;
     P.krit = c.krit;
     P.frozen_radius = c.frozen_radius;
+    P.scheme = c.scheme;
+    P.x_max = c.x_max;
+    P.y_max = c.y_max;
     P.gm1 = c.gamma - 1.0;
     P.inv_gm1 = 1.0 / (c.gamma - 1.0);
     P.ambient_p = 1.0 / c.gamma;
@@ -102,7 +116,11 @@ Params make_params(const gd_config& c) {
 cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const Planes& out,
                         const double* T_do, unsigned long long* T_bits, Scalars* rot,
                         Scalars* ctr, int dt_only, cudaStream_t st) {
-    ctx->launches += 1;
+    ctx->launches += ctx->step_launches;
+    if (P.scheme != GD_SCHEME_TVD)
+        return ctx->cfg.mode == GD_MODE_PARITY
+                   ? gd::launch_hancock_parity(P, in, out, T_do, T_bits, rot, ctr, dt_only, st)
+                   : gd::launch_hancock_fast(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
     if (ctx->cfg.mode == GD_MODE_PARITY)
         return gd::launch_parity(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
     if (P.physics == GD_EULER)
@@ -160,8 +178,14 @@ gd_status gd_create(const gd_config* cfg, gd_ctx** out) {
         std::memcpy(&h.T_bits, &reset, sizeof(double));
         e = cudaMemcpy(ctx->sc, &h, sizeof(Scalars), cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess && cfg->mode == GD_MODE_FAST)
-        e = cfg->physics == GD_EULER ? gd::prepare_euler_fast() : gd::prepare_mhd_fast();
+    if (e == cudaSuccess && cfg->mode == GD_MODE_FAST) {
+        if (cfg->scheme != GD_SCHEME_TVD) {
+            e = gd::prepare_hancock_fast();
+            ctx->step_launches = 2;  // edge band, then the interior tiles
+        } else {
+            e = cfg->physics == GD_EULER ? gd::prepare_euler_fast() : gd::prepare_mhd_fast();
+        }
+    }
     if (e == cudaSuccess) e = cudaMemset(ctx->state[0], 0, plane_bytes);
     if (e == cudaSuccess) e = cudaMemset(ctx->state[1], 0, plane_bytes);
     if (e != cudaSuccess) {
@@ -204,6 +228,8 @@ gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const doubl
             return GD_ERR_INVALID_ARG;
         if (ctx->cfg.physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
             return GD_ERR_INVALID_ARG;
+        if (ctx->cfg.scheme != GD_SCHEME_TVD && method != GD_METHOD_HLLD)
+            return GD_ERR_UNSUPPORTED;
         P.method = method;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -339,7 +365,7 @@ gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream) {
         it = ctx->graphs.emplace(key, ge).first;
     }
     GD_CUDA(cudaGraphLaunch(it->second, st));
-    ctx->launches += nsteps;
+    ctx->launches += (long long)nsteps * ctx->step_launches;
     if (nsteps & 1) ctx->cur ^= 1;
     return GD_OK;
 }

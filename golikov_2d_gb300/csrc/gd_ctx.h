@@ -50,6 +50,7 @@ struct gd_ctx {
     double* ref_planes = nullptr;           // 2 * nf * K: SoA in/out for gd_step_ref
     double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
     long long launches = 0;
+    int step_launches = 1;                  // kernel launches of one step (fast Hancock: 2)
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
     gd::AdjStore* adj = nullptr;            // differentiation record (gd_adj_forward)
     gd::IoScratch* io = nullptr;            // state I/O work buffers (gd_io.cu)

@@ -1,0 +1,444 @@
+// gd_fast_hancock.cu -- fast MUSCL-Hancock step (Kernel_GKR, kernel.cu:2663-3284): the
+// predictor-corrector with HLLD faces, face-once on tiles, FMA contraction, field in
+// Heaviside-Lorentz units (b = B / sqrt(4 pi)).
+//
+// The reference evaluates, for every cell, the half-step predictions of itself and of its
+// four neighbours, so each prediction is computed five times and each face twice.  Away
+// from the edges a cell's view of a neighbour's prediction is the neighbour's own (same
+// stencil points), so here every prediction is computed once per tile and every face once.
+// That holds for the cells with 2 <= n < N-2 and 2 <= m < M-2 (the "interior"); along the
+// edges the reference's substitutes depend on the asking cell (see gd_hancock_cell.cuh), and
+// the two-cell band is computed cell by cell exactly as the reference does.  Two launches:
+//   hancock_band_kernel   the band cells, per cell (hancock_cell of gd_hancock_cell.cuh)
+//   hancock_tile_kernel   32 x 8 interior tiles:
+//     L  state of the tile + 2 halo (cross-shaped), B -> b
+//     P  per cell of the tile + 1 halo: minmod slopes, the predictor's four physical fluxes
+//        (POTOK_Korolkov, Gas_Dinamic.cu:70-180, written in x / y components) and
+//        sources, the half-step mean A = (Q + QQ)/2
+//     F  each face once: HLLD between A_L + D_L/2 and A_R - D_R/2 (gd_mhd_flux.cuh)
+//     U  the corrector of kernel.cu:3256-3281 (Pdiv = 0) from A and the four faces
+// The tile kernel runs second and performs the funk_time rotation.
+//
+// Differences from the parity step are rounding only: contraction, reciprocals instead of
+// divisions, slopes minmod(a - b, b - c) instead of h minmod((a - b)/h, (b - c)/h), the
+// neighbour's prediction at its own radius y_{m+-1} instead of y -+ dy, and the face solved
+// once (its two sides see the same flux up to rounding of the solver's symmetry).
+#include "gd_hancock_cell.cuh"
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+#include "gd_mhd_flux.cuh"
+
+namespace gd {
+namespace {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;  // one interior cell per thread in U
+constexpr int NF = 7;                          // rho, p, vx, vy, bx, by, bz
+constexpr int RX = TX + 4, RY = TY + 4;        // state: tile + 2
+constexpr int PX = TX + 2, PY = TY + 2;        // predictions: tile + 1
+constexpr int kRaw = NF * RY * RX;
+constexpr int kPred = NF * PY * PX;            // one array each of A, DX, DY
+constexpr int NFX = (TX + 1) * TY, NFY = TX * (TY + 1);
+constexpr int kFx = NF * NFX, kFy = NF * NFY;
+constexpr int kUnion = kRaw > kFx + kFy ? kRaw : kFx + kFy;  // state, later the fluxes
+constexpr size_t kSmemBytes = sizeof(double) * (kUnion + 3 * kPred + 2 * PY) + TX * TY;
+
+constexpr int BNT = 128;  // band kernel
+
+// physical flux of state s = {r, p, u, v, bx, by, bz} (b units) through an x face and a
+// y face, components {mass, energy, mom x, mom y, bx, by, bz}
+__device__ __forceinline__ void flux_x(const double* s, double ig, double* F) {
+    const double r = s[0], p = s[1], u = s[2], v = s[3], bx = s[4], by = s[5], bz = s[6];
+    const double bb = fma(bz, bz, fma(by, by, bx * bx));
+    const double pT = fma(0.5, bb, p);
+    const double E = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
+    const double ru = r * u;
+    F[0] = ru;
+    F[1] = fma(E + pT, u, -bx * fma(u, bx, v * by));
+    F[2] = fma(ru, u, pT - bx * bx);
+    F[3] = fma(ru, v, -bx * by);
+    F[4] = 0.0;
+    F[5] = fma(u, by, -v * bx);
+    F[6] = u * bz;
+}
+__device__ __forceinline__ void flux_y(const double* s, double ig, double* F) {
+    const double r = s[0], p = s[1], u = s[2], v = s[3], bx = s[4], by = s[5], bz = s[6];
+    const double bb = fma(bz, bz, fma(by, by, bx * bx));
+    const double pT = fma(0.5, bb, p);
+    const double E = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
+    const double rv = r * v;
+    F[0] = rv;
+    F[1] = fma(E + pT, v, -by * fma(u, bx, v * by));
+    F[2] = fma(rv, u, -bx * by);
+    F[3] = fma(rv, v, pT - by * by);
+    F[4] = fma(v, bx, -u * by);
+    F[5] = 0.0;
+    F[6] = v * bz;
+}
+
+// Q + sgn D/2 with the reference's fallback of rho and p to Q when <= 0 (kernel.cu:1640-1680)
+__device__ __forceinline__ void half_state(const double* Q, const double* D, double sgn,
+                                           double* S) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) S[f] = fma(0.5 * sgn, D[f], Q[f]);
+    S[0] = le_zero(S[0]) ? Q[0] : S[0];
+    S[1] = le_zero(S[1]) ? Q[1] : S[1];
+}
+
+template <bool VYP>
+__global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, Planes out,
+                                                          const double* __restrict__ T_do_ptr,
+                                                          unsigned long long* T_bits,
+                                                          Scalars* rot, Scalars* ctr,
+                                                          int dt_only) {
+    extern __shared__ __align__(16) double smem[];
+    double* raw = smem;            // [NF][RY][RX], then fx [NF][TY][TX+1], fy [NF][TY+1][TX]
+    double* fx = smem;
+    double* fy = smem + kFx;
+    double* pA = smem + kUnion;    // [NF][PY][PX]
+    double* pDX = pA + kPred;
+    double* pDY = pDX + kPred;
+    double* rowy = pDY + kPred;    // radius of prediction rows
+    double* rowiy = rowy + PY;     // its reciprocal
+    unsigned char* flag = reinterpret_cast<unsigned char*>(rowiy + PY);  // [TY][TX]
+
+    const int tid = threadIdx.x;
+    const int N = P.N, M = P.M;
+    const int tx0 = 2 + blockIdx.x * TX, ty0 = 2 + blockIdx.y * TY;
+    const double ig = P.inv_gm1;
+
+    // ---- L: state of the tile + 2 halo; corner blocks the stencils never reach are skipped
+    for (int i = tid; i < RY * RX; i += NT) {
+        const int ly = i / RX, lx = i - ly * RX;
+        if ((lx == 0 || lx == RX - 1) && (ly < 2 || ly >= TY + 2)) continue;
+        if ((ly == 0 || ly == RY - 1) && (lx < 2 || lx >= TX + 2)) continue;
+        const int gx = tx0 + lx - 2, gy = ty0 + ly - 2;
+        double v[NF];
+        if (gx >= 0 && gx < N && gy >= 0 && gy < M) {
+            const long long k = (long long)gy * N + gx;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) v[f] = in.f[f][k];
+            v[4] *= kInvSpi4;
+            v[5] *= kInvSpi4;
+            v[6] *= kInvSpi4;
+        } else {
+            // outside the grid: only predictions that no interior face uses read these
+#pragma unroll
+            for (int f = 0; f < NF; ++f) v[f] = f < 2 ? 1.0 : 0.0;
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f) raw[(f * RY + ly) * RX + lx] = v[f];
+    }
+    if (tid < PY) {
+        const double y = hancock_y(P, ty0 + tid - 1);
+        rowy[tid] = y;
+        rowiy[tid] = 1.0 / y;
+    }
+    // this thread's cell: 0 outside the interior, 1 interior and frozen, 2 interior, updated
+    const int cx = tid % TX, cy = tid / TX;
+    const int gx = tx0 + cx, gy = ty0 + cy;
+    int my_flag = 0;
+    if (gx < N - 2 && gy < M - 2) my_flag = hancock_frozen(P, gx, hancock_y(P, gy)) ? 1 : 2;
+    flag[tid] = (unsigned char)my_flag;
+    __syncthreads();
+
+    // ---- P: predictions of the tile + 1 halo (not its corners) ---------------------------
+    const double T_do = *T_do_ptr;
+    const double st = 0.5 * T_do;
+    const double sx = st / P.dx, sy = st / P.dy;
+    for (int i = tid; i < PY * PX; i += NT) {
+        const int py = i / PX, px = i - py * PX;
+        if ((px == 0 || px == PX - 1) && (py == 0 || py == PY - 1)) continue;
+        const double* c = raw + (py + 1) * RX + (px + 1);
+        constexpr int PS = RY * RX;
+        double Q[NF], DX[NF], DY[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const double* q = c + f * PS;
+            Q[f] = q[0];
+            DX[f] = minmod(q[1] - q[0], q[0] - q[-1]);
+            DY[f] = minmod(q[RX] - q[0], q[0] - q[-RX]);
+        }
+        if (VYP) {
+            DX[3] = DX[1];
+            DY[3] = DY[1];
+        }
+        // predictor (kernel.cu:1611-1720): flux differences of the four face states
+        double d[NF];
+        {
+            double Sp[NF], Sm[NF], Fp[NF], Fm[NF];
+            half_state(Q, DX, 1.0, Sp);
+            half_state(Q, DX, -1.0, Sm);
+            flux_x(Sp, ig, Fp);
+            flux_x(Sm, ig, Fm);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) d[f] = sx * (Fp[f] - Fm[f]);
+            half_state(Q, DY, 1.0, Sp);
+            half_state(Q, DY, -1.0, Sm);
+            flux_y(Sp, ig, Fp);
+            flux_y(Sm, ig, Fm);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) d[f] = fma(sy, Fp[f] - Fm[f], d[f]);
+        }
+        const double sty = st * rowiy[py];
+        const double r = Q[0], p = Q[1], u = Q[2], v = Q[3], bx = Q[4], by = Q[5], bz = Q[6];
+        const double bb = fma(bz, bz, fma(by, by, bx * bx));
+        const double U = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
+        double r2 = fma(-sty * r, v, r - d[0]);
+        r2 = le_zero(r2) ? r : r2;
+        const double ir2 = rcp_fast(r2);
+        const double u2 = fma(-sty, fma(r * u, v, -bx * by), fma(r, u, -d[2])) * ir2;
+        const double v2 = fma(-sty, fma(r * v, v, fma(bz, bz, -by * by)), fma(r, v, -d[3])) * ir2;
+        const double bx2 = fma(-sty, fma(v, bx, -by * u), bx - d[4]);
+        const double by2 = by - d[5];
+        const double bz2 = bz - d[6];
+        const double E2 =
+            fma(-sty, fma(U + p + 0.5 * bb, v, -by * fma(u, bx, v * by)), U - d[1]);
+        double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2),
+                                    fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+        p2 = le_zero(p2) ? 0.000001 : p2;
+        const double QQ[NF] = {r2, p2, u2, v2, bx2, by2, bz2};
+        const int o = py * PX + px;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            pA[f * PY * PX + o] = 0.5 * (Q[f] + QQ[f]);
+            pDX[f * PY * PX + o] = DX[f];
+            pDY[f * PY * PX + o] = DY[f];
+        }
+    }
+    __syncthreads();
+
+    // ---- F: each face of an updated cell once -------------------------------------------
+    double umax_x = 0.0, umax_y = 0.0;
+    for (int i = tid; i < NFX + NFY; i += NT) {
+        const bool isx = i < NFX;
+        int lx, ly, pa, pb;
+        if (isx) {
+            ly = i / (TX + 1);
+            lx = i - ly * (TX + 1);
+            const bool need = (lx > 0 && flag[ly * TX + lx - 1] == 2) ||
+                              (lx < TX && flag[ly * TX + lx] == 2);
+            if (!need) continue;
+            pa = (ly + 1) * PX + lx;  // cell lx-1 of the tile
+            pb = pa + 1;
+        } else {
+            const int j = i - NFX;
+            ly = j / TX;
+            lx = j - ly * TX;
+            const bool need = (ly > 0 && flag[(ly - 1) * TX + lx] == 2) ||
+                              (ly < TY && flag[ly * TX + lx] == 2);
+            if (!need) continue;
+            pa = ly * PX + lx + 1;  // cell (lx, ly-1) of the tile
+            pb = pa + PX;
+        }
+        const double* D = isx ? pDX : pDY;
+        double qa[NF], qb[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const double Aa = pA[f * PY * PX + pa], Ab = pA[f * PY * PX + pb];
+            qa[f] = fma(0.5, D[f * PY * PX + pa], Aa);
+            qb[f] = fma(-0.5, D[f * PY * PX + pb], Ab);
+            if (f < 2) {
+                qa[f] = le_zero(qa[f]) ? Aa : qa[f];
+                qb[f] = le_zero(qb[f]) ? Ab : qb[f];
+            }
+        }
+        // local frame: x-face (n, t) = (x, y); y-face (n, t) = (y, x); z stays z
+        Side<double> A, B;
+        side(A, qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], isx ? qa[4] : qa[5],
+             isx ? qa[5] : qa[4], qa[6], P);
+        side(B, qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], isx ? qb[4] : qb[5],
+             isx ? qb[5] : qb[4], qb[6], P);
+        double UU;
+        const FluxM<double> F = hlld_local(A, B, GD_METHOD_HLLD, UU);
+        if (isx) {
+            double* fo = fx + ly * (TX + 1) + lx;
+            fo[0 * NFX] = F.m;
+            fo[1 * NFX] = F.e;
+            fo[2 * NFX] = F.mn;
+            fo[3 * NFX] = F.mt;
+            fo[4 * NFX] = F.bn;
+            fo[5 * NFX] = F.bt;
+            fo[6 * NFX] = F.bz;
+            umax_x = max_nonneg(umax_x, UU);
+        } else {
+            double* fo = fy + ly * TX + lx;
+            fo[0 * NFY] = F.m;
+            fo[1 * NFY] = F.e;
+            fo[2 * NFY] = F.mt;
+            fo[3 * NFY] = F.mn;
+            fo[4 * NFY] = F.bt;
+            fo[5 * NFY] = F.bn;
+            fo[6 * NFY] = F.bz;
+            umax_y = max_nonneg(umax_y, UU);
+        }
+    }
+    __syncthreads();
+
+    // ---- U: corrector (kernel.cu:3256-3281, Pdiv = 0) --------------------------------------
+    unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
+    if (my_flag == 1 && !dt_only) {
+        const long long k = (long long)gy * N + gx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+    } else if (my_flag == 2 && !dt_only) {
+        const double hT = 0.5 * T_do;
+        const double kx = hT / P.dx, ky = hT / P.dy;
+        const double hTy = hT * rowiy[cy + 1];
+        const int o = (cy + 1) * PX + (cx + 1);
+        double A[NF], d[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            A[f] = pA[f * PY * PX + o];
+            const double* a = fx + f * NFX + cy * (TX + 1) + cx;
+            const double* b = fy + f * NFY + cy * TX + cx;
+            d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
+        }
+        const double r = A[0], p = A[1], u = A[2], v = A[3], bx = A[4], by = A[5], bz = A[6];
+        const double bb = fma(bz, bz, fma(by, by, bx * bx));
+        const double U = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
+        double r2 = fma(-hTy * r, v, r - d[0]);
+        if (le_zero(r2)) {
+            r2 = r;
+            ++nfl_r;
+        }
+        const double ir2 = rcp_fast(r2);
+        const double u2 = fma(-hTy, fma(r * u, v, -bx * by), fma(r, u, -d[2])) * ir2;
+        const double v2 = fma(-hTy, fma(r * v, v, fma(bz, bz, -by * by)), fma(r, v, -d[3])) * ir2;
+        const double bx2 = fma(-hTy, fma(v, bx, -by * u), bx - d[4]);
+        const double by2 = by - d[5];
+        const double bz2 = bz - d[6];
+        const double E2 =
+            fma(-hTy, fma(U + p + 0.5 * bb, v, -by * fma(u, bx, v * by)), U - d[1]);
+        double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2),
+                                    fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+        if (le_zero(p2)) {
+            p2 = 0.000001;
+            ++nfl_p;
+        }
+        if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2) ||
+            !isfinite(bx2) || !isfinite(by2) || !isfinite(bz2))
+            ++nbad;
+        const long long k = (long long)gy * N + gx;
+        out.f[0][k] = r2;
+        out.f[1][k] = p2;
+        out.f[2][k] = u2;
+        out.f[3][k] = v2;
+        out.f[4][k] = bx2 * kSpi4;
+        out.f[5][k] = by2 * kSpi4;
+        out.f[6][k] = bz2 * kSpi4;
+    }
+    if (ctr != nullptr && (nfl_r | nfl_p | nbad)) {
+        if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
+        if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
+        if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
+    }
+    const bool any_active = __syncthreads_or(my_flag == 2) != 0;
+    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot);
+}
+
+// The band: rows m < 2 and m >= M-2 whole, and columns n < 2, n >= N-2 of the rows between.
+struct Band {
+    int rows_lo, rows_hi0, cols_lo, cols_hi0, nrows, ncols, mid0, nmid, total;
+};
+
+Band make_band(int N, int M) {
+    Band b;
+    b.rows_lo = M < 2 ? M : 2;              // rows [0, rows_lo)
+    b.rows_hi0 = M - 2 > 2 ? M - 2 : 2;     // rows [rows_hi0, M)
+    b.nrows = b.rows_lo + (M - b.rows_hi0);
+    b.cols_lo = N < 2 ? N : 2;
+    b.cols_hi0 = N - 2 > 2 ? N - 2 : 2;
+    b.ncols = b.cols_lo + (N - b.cols_hi0);
+    b.mid0 = 2;
+    b.nmid = M - 4 > 0 ? M - 4 : 0;          // rows [2, M-2)
+    b.total = b.nrows * N + b.nmid * b.ncols;
+    return b;
+}
+
+template <bool VYP>
+__global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in, Planes out,
+                                                           const double* __restrict__ T_do_ptr,
+                                                           unsigned long long* T_bits,
+                                                           Scalars* ctr, int dt_only, Band b) {
+    const int i = blockIdx.x * BNT + threadIdx.x;
+    double tmin = kCellTmin0;
+    bool active = false;
+    unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
+    if (i < b.total) {
+        int n, m;
+        if (i < b.nrows * P.N) {
+            const int r = i / P.N;
+            n = i - r * P.N;
+            m = r < b.rows_lo ? r : b.rows_hi0 + (r - b.rows_lo);
+        } else {
+            const int j = i - b.nrows * P.N;
+            const int r = j / b.ncols, c = j - r * b.ncols;
+            m = b.mid0 + r;
+            n = c < b.cols_lo ? c : b.cols_hi0 + (c - b.cols_lo);
+        }
+        const long long k = (long long)m * P.N + n;
+        const double y = hancock_y(P, m);
+        if (hancock_frozen(P, n, y)) {
+            if (!dt_only)
+                for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+        } else {
+            active = true;
+            double res[NF];
+            tmin = hancock_cell<VYP>(P, in, n, m, y, *T_do_ptr, res, nfl_r, nfl_p);
+            if (!dt_only) {
+                for (int f = 0; f < NF; ++f) {
+                    if (!isfinite(res[f])) {
+                        ++nbad;
+                        break;
+                    }
+                }
+                for (int f = 0; f < NF; ++f) out.f[f][k] = res[f];
+            }
+        }
+    }
+    if (ctr != nullptr && !dt_only && (nfl_r | nfl_p | nbad)) {
+        if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
+        if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
+        if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
+    }
+    block_tmin_and_rotate<BNT>(tmin, active, T_bits, nullptr);
+}
+
+template <bool VYP>
+cudaError_t launch_v(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
+                     unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
+                     cudaStream_t st) {
+    const Band b = make_band(P.N, P.M);
+    hancock_band_kernel<VYP><<<(b.total + BNT - 1) / BNT, BNT, 0, st>>>(P, in, out, T_do, T_bits,
+                                                                        ctr, dt_only, b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // interior tiles; at least one block, which performs the rotation
+    const int nx = P.N - 4 > 0 ? (P.N - 4 + TX - 1) / TX : 1;
+    const int ny = P.M - 4 > 0 ? (P.M - 4 + TY - 1) / TY : 1;
+    hancock_tile_kernel<VYP><<<dim3(nx, ny), NT, kSmemBytes, st>>>(P, in, out, T_do, T_bits, rot,
+                                                                   ctr, dt_only);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t prepare_hancock_fast() {
+    cudaError_t e = cudaFuncSetAttribute(hancock_tile_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmemBytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(hancock_tile_kernel<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    return e;
+}
+
+cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes& out,
+                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                Scalars* ctr, int dt_only, cudaStream_t st) {
+    if (P.scheme == GD_SCHEME_HANCOCK_REF)
+        return launch_v<true>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+    return launch_v<false>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+}  // namespace gd

@@ -27,6 +27,7 @@
 #include "gd_dual.cuh"
 #include "gd_internal.cuh"
 #include "gd_kernels.h"
+#include "gd_mhd_flux.cuh"
 
 namespace gd {
 namespace {
@@ -34,196 +35,6 @@ namespace {
 constexpr int TX = 32;
 constexpr int NT = 256;
 constexpr int NF = 7;  // rho, p, vx, vy, bx, by, bz
-
-template <class T>
-__device__ __forceinline__ T cst(double x);
-template <>
-__device__ __forceinline__ double cst<double>(double x) { return x; }
-template <>
-__device__ __forceinline__ Dual cst<Dual>(double x) { return Dual{x, 0.0}; }
-
-template <class T>
-struct FluxM {
-    T m, mn, mt, e, bn, bt, bz;  // mass, normal / tangential momentum, energy, field
-};
-
-// One side of the face in the local frame (un normal, ut in-plane tangential, uz = 0).
-template <class T>
-struct Side {
-    T r, p, un, ut, bn, bt, bz, bb, pT, E, cf;
-    T F0, F1, F2, F4, F6, F7;
-};
-
-template <class T>
-__device__ __forceinline__ void side(Side<T>& S, T r, T p, T un, T ut, T bn, T bt, T bz,
-                                     const Params& P) {
-    S.r = r; S.p = p; S.un = un; S.ut = ut; S.bn = bn; S.bt = bt; S.bz = bz;
-    const T bn2 = bn * bn;
-    S.bb = fma(bz, bz, fma(bt, bt, bn2));
-    S.pT = fma(0.5, S.bb, p);
-    S.E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(un, un, ut * ut), S.bb));
-    const T gp = P.gamma * p;
-    const T a = gp + S.bb;
-    T disc = fma(a, a, -4.0 * gp * bn2);
-    disc = le_zero(disc) ? cst<T>(0.0) : disc;
-    const T X = 0.5 * (a + sqrt_fast(disc));  // rho cf^2
-    S.cf = X * rsqrt_fast(X * r);              // sqrt(X / r)
-    S.F0 = r * un;
-    S.F1 = fma(S.F0, un, S.pT - bn2);
-    S.F2 = fma(S.F0, ut, -bn * bt);
-    S.F4 = fma(S.E + S.pT, un, -bn * fma(ut, bt, un * bn));
-    S.F6 = fma(un, bt, -ut * bn);
-    S.F7 = un * bz;
-}
-
-__device__ __forceinline__ double sgn_select(double v, int idbn) {
-    // idbn * v for idbn in {-1, 0, 1}, on the integer pipe (sign-bit flip, select)
-    const double w = idbn < 0 ? from_bits(bits(v) ^ (long long)0x8000000000000000ULL) : v;
-    return idbn == 0 ? 0.0 : w;
-}
-__device__ __forceinline__ Dual sgn_select(Dual v, int idbn) {
-    return idbn == 0 ? Dual{0.0, 0.0} : (idbn < 0 ? -v : v);
-}
-
-// HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = max(|SL|, |SR|).
-template <class T>
-__device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& B, int method,
-                                               T& UU) {
-    const T uminN = dmin(A.un, B.un);
-    const T umaxN = dmax(A.un, B.un);
-    const T cmax = max_nonneg(A.cf, B.cf);
-    const T SL = uminN - cmax, SR = umaxN + cmax;
-    const T suL = SL - A.un, suR = SR - B.un;
-    const T mL = A.r * suL, mR = B.r * suR;
-    const T iden = rcp_fast(mR - mL);
-    const T SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
-    const T PTT = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT)) * iden;
-    UU = max_nonneg(dabs(SL), dabs(SR));
-    const T iS = rcp_fast(SR - SL);
-    const T bn = fma(SR, B.bn, -SL * A.bn) * iS;
-    const T bt = (fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6)) * iS;
-    const T bz = (fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7)) * iS;
-    const T iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
-    const T rLL = mL * iL, rRR = mR * iR;
-
-    FluxM<T> F;
-    if (method == GD_METHOD_HLLC_MHD) {
-        const bool takeL = ge_zero(SL) || ge_zero(SM);
-        const Side<T>& K = takeL ? A : B;
-        const T S = takeL ? SL : SR;
-        const bool star = takeL ? lt_zero(SL) : gt_zero(SR);
-        F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
-        if (star) {
-            // HLL state of the fan (Gas_Dinamic.cu:1145-1149); mom_z: U = 0, F = -bn bz
-            const T UZ0 = (fma(SR, B.r, -SL * A.r) + (A.F0 - B.F0)) * iS;
-            const T UZ1 = (fma(SR, B.r * B.un, -SL * A.r * A.un) + (A.F1 - B.F1)) * iS;
-            const T UZ2 = (fma(SR, B.r * B.ut, -SL * A.r * A.ut) + (A.F2 - B.F2)) * iS;
-            const T UZ3 = (B.bn * B.bz - A.bn * A.bz) * iS;
-            const T iU0 = rcp_fast(UZ0);
-            const T vS = UZ2 * iU0;
-            const T ptz = 0.5 * (fma(mR, SM - B.un, B.pT) + fma(mL, SM - A.un, A.pT));
-            const T sbvz = fma(bn, UZ1, fma(bt, UZ2, bz * UZ3)) * iU0;
-            const T sbvK = fma(K.un, K.bn, K.ut * K.bt);
-            const T iK = takeL ? iL : iR;
-            const T suK = takeL ? suL : suR;
-            const T eK = (fma(K.E, suK, fma(ptz, SM, -K.pT * K.un)) + bn * (sbvK - sbvz)) * iK;
-            const T rK = takeL ? rLL : rRR;
-            F.m = fma(S, rK - K.r, F.m);
-            F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
-            F.mt = fma(S, fma(rK, vS, -K.r * K.ut), F.mt);
-            F.e = fma(S, eK - K.E, F.e);
-            F.bt = fma(S, bt - K.bt, F.bt);
-            F.bz = fma(S, bz - K.bz, F.bz);
-        }
-    } else {
-        const T bbn = bn * bn;
-        // star states of both sides (Gas_Dinamic.cu:1306-1350)
-        T vLL, wLL, btL, bzL, vRR, wRR, btR, bzR;
-        {
-            const T tt = fma(mL, SL - SM, -bbn);
-            if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {  // |tt| >= 1e-5
-                const T it = rcp_fast(tt);
-                const T c = bn * (SM - A.un) * it;
-                const T d = fma(mL, suL, -bbn) * it;
-                vLL = fma(-c, A.bt, A.ut);
-                wLL = -c * A.bz;
-                btL = A.bt * d;
-                bzL = A.bz * d;
-            } else {
-                vLL = A.ut; wLL = cst<T>(0.0); btL = cst<T>(0.0); bzL = cst<T>(0.0);
-            }
-        }
-        {
-            const T tt = fma(mR, SR - SM, -bbn);
-            if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {
-                const T it = rcp_fast(tt);
-                const T c = bn * (SM - B.un) * it;
-                const T d = fma(mR, suR, -bbn) * it;
-                vRR = fma(-c, B.bt, B.ut);
-                wRR = -c * B.bz;
-                btR = B.bt * d;
-                bzR = B.bz * d;
-            } else {
-                vRR = B.ut; wRR = cst<T>(0.0); btR = cst<T>(0.0); bzR = cst<T>(0.0);
-            }
-        }
-        const T SMbn = SM * bn;
-        const T sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
-        const T sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
-        const T eLL = (fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) +
-                       bn * (fma(A.un, A.bn, A.ut * A.bt) - sbLL)) * iL;
-        const T eRR = (fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) +
-                       bn * (fma(B.un, B.bn, B.ut * B.bt) - sbRR)) * iR;
-        const T isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
-        const T sLL = rLL * isLL, sRR = rRR * isRR;
-        const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;  // |bn| > 1e-6
-        const T abn = dabs(bn);
-        const T SLL = bnz ? fma(-abn, isLL, SM) : SM;
-        const T SRR = bnz ? fma(abn, isRR, SM) : SM;
-        const int idbn = bnz ? (gt_zero(bn) ? 1 : -1) : 0;
-
-        const bool takeL = ge_zero(SL) || ge_zero(SM);
-        int level;
-        if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
-        else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
-        const Side<T>& K = takeL ? A : B;
-        F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
-        if (level >= 1) {
-            const T S = takeL ? SL : SR;
-            const T rK = takeL ? rLL : rRR;
-            const T vK = takeL ? vLL : vRR;
-            const T eK = takeL ? eLL : eRR;
-            const T btK = takeL ? btL : btR;
-            const T bzK = takeL ? bzL : bzR;
-            F.m = fma(S, rK - K.r, F.m);
-            F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
-            F.mt = fma(S, fma(rK, vK, -K.r * K.ut), F.mt);
-            F.e = fma(S, eK - K.E, F.e);
-            F.bt = fma(S, btK - K.bt, F.bt);
-            F.bz = fma(S, bzK - K.bz, F.bz);
-            if (level == 2) {
-                // double-star states (Gas_Dinamic.cu:1371-1430)
-                const T is = rcp_fast(sLL + sRR);
-                const T vL3 = (fma(sLL, vLL, sRR * vRR) + sgn_select(btR - btL, idbn)) * is;
-                const T wL3 = (fma(sLL, wLL, sRR * wRR) + sgn_select(bzR - bzL, idbn)) * is;
-                const T s2 = sgn_select(sLL * sRR, idbn);
-                const T bt3 = fma(s2, vRR - vLL, fma(sLL, btR, sRR * btL)) * is;
-                const T bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
-                const T sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
-                const T sK = takeL ? -sLL : sRR;
-                const T e3 = fma(sgn_select(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
-                const T S2 = takeL ? SLL : SRR;
-                F.mt = fma(S2, rK * (vL3 - vK), F.mt);
-                F.e = fma(S2, e3 - eK, F.e);
-                F.bt = fma(S2, bt3 - btK, F.bt);
-                F.bz = fma(S2, bz3 - bzK, F.bz);
-            }
-        }
-    }
-    // normal-field flux replaced by the diffusive term (Gas_Dinamic.cu:1488-1490)
-    F.bn = -UU * (B.bn - A.bn);
-    return F;
-}
 
 // ---- state access: planes of doubles for the step, value + tangent planes for the JVP ----
 

@@ -29,6 +29,8 @@ struct Params {
     double dx, dy, x0, y0;
     double gamma, krit;
     double frozen_radius;
+    int scheme;           // GD_SCHEME_*
+    double x_max, y_max;  // domain extents of the Hancock schemes' cell coordinates
     // derived
     double gm1, inv_gm1;
     double ambient_p;   // 1/gamma
@@ -246,6 +248,25 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
     return v;
 }
 
+// Called by one thread of each block after the block's dt is combined: the last block of
+// the launch to arrive performs the funk_time rotation on `sc` (T_do <- T, TT += T_do,
+// T <- 1e7, ++step).  `nblocks` blocks report per launch; 0 means every block of the grid.
+__device__ __forceinline__ void rotate_if_last(Scalars* sc, unsigned int nblocks) {
+    __threadfence();
+    const unsigned int nb = nblocks ? nblocks : gridDim.x * gridDim.y * gridDim.z;
+    const unsigned int ticket = atomicAdd(&sc->done, 1u);
+    if (ticket == nb - 1) {
+        __threadfence();
+        const double T = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
+        sc->T_do = T;
+        sc->TT = sc->TT + T;
+        sc->T_bits = (unsigned long long)bits(kTReset);
+        sc->step = sc->step + 1;
+        sc->done = 0;
+        __threadfence();
+    }
+}
+
 // Reduces the per-thread maximum wave speeds of x and y faces over the block, turns them
 // into the block's dt (min over faces of krit*rad/UU, capped at 1000) and min-combines it
 // into *T_bits.  `any_active` says whether the block contains a non-frozen cell.  Then,
@@ -290,21 +311,39 @@ __device__ void block_dt_and_rotate(const Params& P, double umax_x, double umax_
             }
             atomicMin(T_bits, (unsigned long long)bits(t));
         }
-        if (sc != nullptr) {
-            __threadfence();
-            const unsigned int nb = nblocks ? nblocks : gridDim.x * gridDim.y * gridDim.z;
-            const unsigned int ticket = atomicAdd(&sc->done, 1u);
-            if (ticket == nb - 1) {
-                __threadfence();
-                const double T = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
-                sc->T_do = T;
-                sc->TT = sc->TT + T;
-                sc->T_bits = (unsigned long long)bits(kTReset);
-                sc->step = sc->step + 1;
-                sc->done = 0;
-                __threadfence();
-            }
+        if (sc != nullptr) rotate_if_last(sc, nblocks);
+    }
+}
+
+// Block minimum of per-thread dt values (positive doubles order like their bit patterns),
+// min-combined into *T_bits when the block holds an active cell, then the funk_time
+// rotation as in block_dt_and_rotate.  Must be called by every thread of the block.
+template <int NTHREADS>
+__device__ void block_tmin_and_rotate(double tmin, bool active, unsigned long long* T_bits,
+                                      Scalars* sc) {
+    __shared__ unsigned long long red[NTHREADS / 32];
+    __shared__ int act[NTHREADS / 32];
+    unsigned long long tb = active ? (unsigned long long)bits(tmin) : ~0ULL;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, tb, o);
+        tb = w < tb ? w : tb;
+    }
+    const int a = __any_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = tb;
+        act[threadIdx.x >> 5] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long mn = ~0ULL;
+        int any = 0;
+        for (int w = 0; w < NTHREADS / 32; ++w) {
+            mn = red[w] < mn ? red[w] : mn;
+            any |= act[w];
         }
+        if (any) atomicMin(T_bits, mn);
+        if (sc != nullptr) rotate_if_last(sc, 0);
     }
 }
 

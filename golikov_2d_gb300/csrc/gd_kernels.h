@@ -69,6 +69,18 @@ cudaError_t launch_parity(const Params& P, const CPlanes& in, const Planes& out,
                           const double* T_do, unsigned long long* T_bits, Scalars* rot,
                           Scalars* ctr, int dt_only, cudaStream_t st);
 
+// MUSCL-Hancock step of Kernel_GKR (P.scheme GD_SCHEME_HANCOCK_REF / GD_SCHEME_HANCOCK).
+// Parity: every cell as the reference computes it (built without FMA contraction;
+// bit-identical).  Fast: face-once tiles for the cells away from the edges, the per-cell
+// evaluation for the two-cell band along the edges (two launches).
+cudaError_t launch_hancock_parity(const Params& P, const CPlanes& in, const Planes& out,
+                                  const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                  Scalars* ctr, int dt_only, cudaStream_t st);
+cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes& out,
+                                const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                Scalars* ctr, int dt_only, cudaStream_t st);
+cudaError_t prepare_hancock_fast();
+
 // Utilities (gd_util.cu).
 cudaError_t launch_aos_to_soa(const double* s, const double* u, const double* b, Planes out,
                               long long K, int nf, cudaStream_t st);

@@ -46,6 +46,7 @@ gd_status scratch_for_device(int dev, void** out) {
         if (e != cudaSuccess || p == nullptr) return GD_ERR_CUDA;
         e = gd::prepare_euler_fast();
         if (e == cudaSuccess) e = gd::prepare_mhd_fast();
+        if (e == cudaSuccess) e = gd::prepare_hancock_fast();
         if (e != cudaSuccess) return GD_ERR_CUDA;
         g_scratch_addr[dev] = p;
     }
@@ -72,6 +73,7 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
             return GD_ERR_INVALID_ARG;
         if (cfg->physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
             return GD_ERR_INVALID_ARG;
+        if (cfg->scheme != GD_SCHEME_TVD && method != GD_METHOD_HLLD) return GD_ERR_UNSUPPORTED;
         P.method = method;
     }
     int dev = 0;
@@ -96,7 +98,12 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
     if (cudaMemsetAsync(ctr, 0, sizeof(gd::Scalars), cs) != cudaSuccess) return GD_ERR_CUDA;
     if (gd::launch_aos_to_soa(s, u, b, in, K, nf, cs) != cudaSuccess) return GD_ERR_CUDA;
     cudaError_t e;
-    if (cfg->mode == GD_MODE_PARITY)
+    unsigned long long* Tb = (unsigned long long*)T;
+    if (cfg->scheme != GD_SCHEME_TVD)
+        e = cfg->mode == GD_MODE_PARITY
+                ? gd::launch_hancock_parity(P, cin, out, T_do, Tb, nullptr, ctr, 0, cs)
+                : gd::launch_hancock_fast(P, cin, out, T_do, Tb, nullptr, ctr, 0, cs);
+    else if (cfg->mode == GD_MODE_PARITY)
         e = gd::launch_parity(P, cin, out, T_do, (unsigned long long*)T, nullptr, ctr, 0, cs);
     else if (cfg->physics == GD_EULER)
         e = gd::launch_euler_fast(P, cin, out, T_do, (unsigned long long*)T, nullptr, ctr, 0, cs);

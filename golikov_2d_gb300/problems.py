@@ -11,8 +11,8 @@ import math
 import numpy as np
 
 from . import (AXISYM, BC_AMBIENT, BC_AXIS, BC_MIRROR_X, BC_OUTFLOW, BC_PERIODIC,
-               BC_TRANSMISSIVE, CARTESIAN, EULER, MHD, METHOD_HLLC, METHOD_HLLD, MODE_FAST,
-               Config)
+               BC_TRANSMISSIVE, CARTESIAN, EULER, HANCOCK_BC, MHD, METHOD_HLLC, METHOD_HLLD,
+               MODE_FAST, SCHEME_HANCOCK_REF, Config)
 
 KH_SEED = 20261203
 
@@ -111,6 +111,49 @@ def stellar_wind(N=3226, M=1792, xmax=9.0, ymax=5.0, krit=0.25, method=METHOD_HL
     P_E = ro_E * V_E * V_E / (gamma * M_0 * M_0)
     B_E = math.sqrt(4.0 * math.pi) / (M_ALF * RR_0)
     inside = dist < DDIST * 1.01
+    dsafe = np.where(inside, dist, 1.0)
+    s = np.stack([np.where(inside, ro_E / (dsafe / RR_0) ** 2, 1.0),
+                  np.where(inside, P_E * (RR_0 / dsafe) ** (2.0 * gamma), 1.0 / gamma)], 1)
+    u = np.stack([np.where(inside, V_E * X / dsafe, 0.0), np.where(inside, V_E * Y / dsafe, 0.0)], 1)
+    BE = B_E / (dsafe / RR_0)
+    bz = np.where(inside, BE * np.sin(np.arccos(np.clip(X / dsafe, -1.0, 1.0))), 0.0)
+    b = np.stack([np.zeros(K), np.zeros(K), bz], 1)
+    return cfg, np.ascontiguousarray(s), np.ascontiguousarray(u), np.ascontiguousarray(b)
+
+
+# Kernel_GKR freezes every cell with sqrt(x^2 + y^2) < 2.0 (kernel.cu:2692).
+GKR_FROZEN = 2.0
+
+
+def hancock_config(N, M, xmax=9.0, ymax=5.0, krit=0.25, gamma=5.0 / 3.0,
+                   scheme=SCHEME_HANCOCK_REF, mode=MODE_FAST) -> Config:
+    """The setting Kernel_GKR (kernel.cu:2663-3284) is written for: axisymmetric MHD, HLLD
+    faces, its own edge cells (mirror at x = 0, outflow at x = xmax, axis at y = 0, ambient
+    keeping B at y = ymax), the domain constants of kernel.cu:12-20 and its frozen sphere."""
+    return Config(N=N, M=M, dx=xmax / N, dy=ymax / M, x0=xmax / (2.0 * N), y0=ymax / (2.0 * M),
+                  gamma=gamma, krit=krit, physics=MHD, geometry=AXISYM, order=2,
+                  method=METHOD_HLLD, bc=HANCOCK_BC, frozen_radius=GKR_FROZEN, mode=mode,
+                  scheme=scheme, x_max=xmax, y_max=ymax)
+
+
+def hancock_wind(N=3226, M=1792, xmax=9.0, ymax=5.0, scheme=SCHEME_HANCOCK_REF,
+                 mode=MODE_FAST, gamma=5.0 / 3.0):
+    """A wind for the MUSCL-Hancock step: the production wind profile of stellar_wind
+    (kernel.cu:3901-3941) filling the sphere dist < 1.01 * 2.0, which Kernel_GKR keeps
+    frozen, in the uniform ambient medium.  Cells are placed where Kernel_GKR places them
+    (kernel.cu:2669-2670): x = x0 + n (xmax - x0)/(N - 1), y = y0 + m ymax / M."""
+    cfg = hancock_config(N, M, xmax, ymax, gamma=gamma, scheme=scheme, mode=mode)
+    n = np.arange(N, dtype=np.float64)
+    m = np.arange(M, dtype=np.float64)
+    X, Y = np.meshgrid(cfg.x0 + n * (xmax - cfg.x0) / (N - 1), cfg.y0 + m * ymax / M)
+    X, Y = X.ravel(), Y.ravel()
+    K = N * M
+    dist = np.sqrt(X * X + Y * Y)
+    V_E = PHI_0
+    ro_E = 1.0 / (PHI_0 * PHI_0 * RR_0 * RR_0)
+    P_E = ro_E * V_E * V_E / (gamma * M_0 * M_0)
+    B_E = math.sqrt(4.0 * math.pi) / (M_ALF * RR_0)
+    inside = dist < GKR_FROZEN * 1.01
     dsafe = np.where(inside, dist, 1.0)
     s = np.stack([np.where(inside, ro_E / (dsafe / RR_0) ** 2, 1.0),
                   np.where(inside, P_E * (RR_0 / dsafe) ** (2.0 * gamma), 1.0 / gamma)], 1)

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GD_ABI_VERSION 2
+#define GD_ABI_VERSION 3
 
 typedef void* gd_stream; /* cudaStream_t */
 
@@ -57,6 +57,14 @@ enum {
     GD_BC_OUTFLOW = 5,       /* edge cell, vx<0 -> 0.01       (kernel.cu:2249-2256)        */
     GD_BC_AMBIENT_KEEPB = 6  /* AMBIENT with B of the edge cell (kernel.cu:1935-1940)      */
 };
+/* spatial scheme */
+enum {
+    GD_SCHEME_TVD = 0,          /* cfg.order 1: add2 / Ker_Dekard; 2: minmod TVD Kernel_TVD    */
+    GD_SCHEME_HANCOCK_REF = 1,  /* MUSCL-Hancock predictor-corrector, Kernel_GKR
+                                   (kernel.cu:2663-3284) as written: the v_y slopes are taken
+                                   from the pressures (kernel.cu:2966, 2974, 3006, 3038, ...)  */
+    GD_SCHEME_HANCOCK = 2       /* the same scheme with v_y slopes taken from v_y             */
+};
 /* execution mode */
 enum {
     GD_MODE_FAST = 0,   /* face-once tiles, hoisted reciprocals, FMA: within 1e-12 per step */
@@ -78,8 +86,17 @@ typedef struct gd_config {
     int method;            /* default flux code (GD_METHOD_*)                              */
     int bc[4];             /* left, right, bottom, top                                     */
     double frozen_radius;  /* cells with sqrt(x^2+y^2) < r are copied, 0 = none (ddist,
-                              Header.h:36; kernel.cu:2218-2225)                            */
+                              Header.h:36; kernel.cu:2218-2225; Kernel_GKR uses 2.0,
+                              kernel.cu:2692)                                              */
     int mode;              /* GD_MODE_FAST or GD_MODE_PARITY                               */
+    /* Added in ABI 3; zero keeps the ABI 2 behaviour. */
+    int scheme;            /* GD_SCHEME_*.  The Hancock schemes are Kernel_GKR's own setting:
+                              MHD, GD_AXISYM, method HLLD (its metod 3), bc = {MIRROR_X,
+                              OUTFLOW, AXIS, AMBIENT_KEEPB}; anything else is
+                              GD_ERR_UNSUPPORTED.  order is not used by them.              */
+    double x_max, y_max;   /* domain extents (kernel.cu:15, 17); the Hancock schemes place
+                              cell (n, m) at x = x0 + n (x_max - x0)/(N - 1),
+                              y = y0 + m y_max / M (kernel.cu:2669-2670)                   */
 } gd_config;
 
 typedef struct gd_stats {
@@ -116,6 +133,7 @@ int gd_abi_version(void);
  *   Kernel_TVD<<<K/256,256>>>(s,u,b,s2,u2,b2,T,T_do,i,method)  (kernel.cu:2198, 4113)
  *   add2<<<...>>>(...)            when cfg.order == 1, physics MHD (kernel.cu:1877, 4042)
  *   Ker_Dekard<<<...>>>(...)      when cfg.order == 1, physics Euler (kernel.cu:1736)
+ *   Kernel_GKR<<<...>>>(...)      when cfg.scheme is a Hancock scheme (kernel.cu:2663)
  * method is the reference's code (GD_METHOD_*), GD_METHOD_CONFIG (-1) uses cfg.method.  `i`
  * is the reference's step counter (unused, as there).
  * All pointers are device pointers; s/s2 etc. must not alias.  Unlike the reference, the

@@ -53,6 +53,7 @@ class OracleConfig(ctypes.Structure):
         ("physics", _i), ("geometry", _i), ("order", _i), ("method", _i),
         ("bc", _i * 4),
         ("frozen_radius", _d),
+        ("scheme", _i), ("x_max", _d), ("y_max", _d),
     ]
 
 
@@ -83,6 +84,9 @@ class Grid:
     method: int = 1
     bc: tuple = (BC_TRANSMISSIVE,) * 4
     frozen_radius: float = 0.0
+    scheme: int = 0
+    x_max: float = 0.0
+    y_max: float = 0.0
 
     def cstruct(self) -> OracleConfig:
         c = OracleConfig()
@@ -93,6 +97,7 @@ class Grid:
         for k in range(4):
             c.bc[k] = self.bc[k]
         c.frozen_radius = self.frozen_radius
+        c.scheme, c.x_max, c.y_max = self.scheme, self.x_max, self.y_max
         return c
 
 
@@ -250,7 +255,7 @@ class Reference:
             getattr(L, name).argtypes = [_pd, _pd, _d, _d, _d, _pd]
         L.gdref_hlld.restype = _d
         L.gdref_hlld.argtypes = [_pd, _pd, _d, _d, _d, _d, _i, _pd]
-        for name in ("gdref_kernel_tvd", "gdref_add2"):
+        for name in ("gdref_kernel_tvd", "gdref_add2", "gdref_kernel_gkr"):
             getattr(L, name).argtypes = [_pd, _pd, _pd, _pd, _pd, _pd, _pd, _d, _i, _i]
         for name in ("gdref_ker_dekard", "gdref_kernel_tvd_old"):
             getattr(L, name).argtypes = [_pd, _pd, _pd, _pd, _pd, _d, _i]
@@ -297,6 +302,9 @@ class Reference:
 
     def kernel_tvd(self, s, u, b, T_do, i=0, method=3, out=None):
         return self._mhd_kernel(self.lib.gdref_kernel_tvd, s, u, b, T_do, i, method, out)
+
+    def kernel_gkr(self, s, u, b, T_do, i=0, method=3, out=None):
+        return self._mhd_kernel(self.lib.gdref_kernel_gkr, s, u, b, T_do, i, method, out)
 
     def add2(self, s, u, b, T_do, i=0, method=2, out=None):
         return self._mhd_kernel(self.lib.gdref_add2, s, u, b, T_do, i, method, out)

@@ -705,8 +705,377 @@ static double mhd_cell(const gdo_config* c, const cell_faces* F, double y, doubl
     return tmin;
 }
 
+/* ------------------------------------------------------------------------------------- */
+/* MUSCL-Hancock step of Kernel_GKR (kernel.cu:2663-3284), term by term.                   */
+/* ------------------------------------------------------------------------------------- */
+
+#define GK_CPI4 12.56637061435917295384 /* Header.h:20-22 */
+#define GK_CPI8 25.13274122871834590768
+#define GK_SPI4 (3.544907701811032)
+
+typedef struct {
+    double sx, sy, ux, uy, bx, by, bz; /* s = (rho, p), u = (vx, vy), b = (Bx, By, Bz) */
+} gk_cell;
+
+static gk_cell gk_load(const double* s, const double* u, const double* b, long k) {
+    gk_cell c = {s[2 * k], s[2 * k + 1], u[2 * k], u[2 * k + 1], b[3 * k], b[3 * k + 1],
+                 b[3 * k + 2]};
+    return c;
+}
+
+/* U8 (Header.h:16): p/(ggg-1) + 0.5 rho |v|^2 + |B|^2 / (8 pi) */
+static double gk_u8(double g, double ro, double p, double u, double v, double w, double bx,
+                    double by, double bz) {
+    return p / (g - 1.0) + 0.5 * ro * ((u * u + v * v) + w * w) +
+           ((bx * bx + by * by) + bz * bz) / 25.13274122871834590768;
+}
+static double gk_kvv(double x, double y, double z) { return (x * x + y * y) + z * z; }
+static double gk_skk(double u, double v, double w, double bx, double by, double bz) {
+    return u * bx + v * by + w * bz;
+}
+
+/* POTOK_Korolkov (Gas_Dinamic.cu:70-180): the physical MHD flux through a face with normal
+ * n = (n1, n2, n3), rotated back to (x, y, z); P = {F_rho, F_mx, F_my, F_mz, F_Bx, F_By,
+ * F_Bz, F_E} with the field fluxes in Gaussian units. */
+static void gk_potok(double g, double ro_L, double Q_L, double p_L, double v1_L, double v2_L,
+                     double v3_L, double Bx_L, double By_L, double Bz_L, double* P, double n1,
+                     double n2, double n3) {
+    const double bx_L = Bx_L / GK_SPI4, by_L = By_L / GK_SPI4, bz_L = Bz_L / GK_SPI4;
+    double t1 = 0.0, t2 = 0.0, t3 = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;
+    if (n1 > 0.1) { t2 = 1.0; m3 = 1.0; }
+    else if (n2 > 0.1) { t3 = 1.0; m1 = 1.0; }
+    else if (n3 > 0.1) { t1 = 1.0; m2 = 1.0; }
+    else if (n1 < -0.1) { t3 = -1.0; m2 = -1.0; }
+    else if (n2 < -0.1) { t1 = -1.0; m3 = -1.0; }
+    else if (n3 < -0.1) { t1 = -1.0; m2 = -1.0; }
+    const double u1 = v1_L * n1 + v2_L * n2 + v3_L * n3;
+    const double v1 = v1_L * t1 + v2_L * t2 + v3_L * t3;
+    const double w1 = v1_L * m1 + v2_L * m2 + v3_L * m3;
+    const double bn1 = bx_L * n1 + by_L * n2 + bz_L * n3;
+    const double bt1 = bx_L * t1 + by_L * t2 + bz_L * t3;
+    const double bm1 = bx_L * m1 + by_L * m2 + bz_L * m3;
+    const double bb_L = bx_L * bx_L + by_L * by_L + bz_L * bz_L;
+    const double uu_L = (v1_L * v1_L + v2_L * v2_L + v3_L * v3_L) / 2.0;
+    const double pTL = p_L + bb_L / 2.0;
+    const double e1 = p_L / (g - 1.0) + ro_L * uu_L + bb_L / 2.0;
+    double PO[9];
+    PO[0] = ro_L * u1;
+    PO[1] = ro_L * u1 * u1 + pTL - bn1 * bn1;
+    PO[2] = ro_L * u1 * v1 - bn1 * bt1;
+    PO[3] = ro_L * u1 * w1 - bn1 * bm1;
+    PO[4] = (e1 + pTL) * u1 - bn1 * (u1 * bn1 + v1 * bt1 + w1 * bm1);
+    PO[5] = 0.0;
+    PO[6] = u1 * bt1 - v1 * bn1;
+    PO[7] = u1 * bm1 - w1 * bn1;
+    PO[8] = Q_L * u1;
+    P[1] = n1 * PO[1] + t1 * PO[2] + m1 * PO[3];
+    P[2] = n2 * PO[1] + t2 * PO[2] + m2 * PO[3];
+    P[3] = n3 * PO[1] + t3 * PO[2] + m3 * PO[3];
+    P[5] = GK_SPI4 * (n1 * PO[5] + t1 * PO[6] + m1 * PO[7]);
+    P[6] = GK_SPI4 * (n2 * PO[5] + t2 * PO[6] + m2 * PO[7]);
+    P[7] = GK_SPI4 * (n3 * PO[5] + t3 * PO[6] + m3 * PO[7]);
+    P[0] = PO[0];
+    P[4] = PO[4];
+    const double SWAP = P[4];
+    P[4] = P[5];
+    P[5] = P[6];
+    P[6] = P[7];
+    P[7] = SWAP;
+}
+
+/* predictor (kernel.cu:1612-1720): half step of a cell from its own slopes.  Q, DX, DY,
+ * QQ in the order rho, p, vx, vy, Bx, By, Bz. */
+static void gk_predictor(const gdo_config* c, const double* Q, const double* DX,
+                         const double* DY, double* QQ, double st, double y) {
+    const double g = c->gamma, dx = c->dx, dy = c->dy;
+    double P[8];
+    double PSx = 0.0, PSy = 0.0, PUx = 0.0, PUy = 0.0, PBx = 0.0, PBy = 0.0, PBz = 0.0;
+    /* faces -x, +x (times dy), +y, -y (times dx) */
+    const double sg[4] = {-1.0, 1.0, 1.0, -1.0};
+    for (int f = 0; f < 4; ++f) {
+        const double* D = f < 2 ? DX : DY;
+        const double h = f < 2 ? dy : dx;
+        double ro_, p_, a[7];
+        if (sg[f] < 0) {
+            ro_ = Q[0] - D[0] / 2.0;
+            p_ = Q[1] - D[1] / 2.0;
+            for (int i = 2; i < 7; ++i) a[i] = Q[i] - D[i] / 2.0;
+        } else {
+            ro_ = Q[0] + D[0] / 2.0;
+            p_ = Q[1] + D[1] / 2.0;
+            for (int i = 2; i < 7; ++i) a[i] = Q[i] + D[i] / 2.0;
+        }
+        if (ro_ <= 0.0) ro_ = Q[0];
+        if (p_ <= 0.0) p_ = Q[1];
+        const double n1 = f < 2 ? sg[f] : 0.0, n2 = f < 2 ? 0.0 : sg[f];
+        gk_potok(g, ro_, 0.0, p_, a[2], a[3], 0.0, a[4], a[5], a[6], P, n1, n2, 0.0);
+        PSx = PSx + P[0] * h;
+        PSy = PSy + P[7] * h;
+        PUx = PUx + P[1] * h;
+        PUy = PUy + P[2] * h;
+        PBx = PBx + P[4] * h;
+        PBy = PBy + P[5] * h;
+        PBz = PBz + P[6] * h;
+    }
+    const double dV = dx * dy;
+    QQ[0] = Q[0] - st * PSx / dV - st * Q[0] * Q[3] / y;
+    if (QQ[0] <= 0) QQ[0] = Q[0];
+    QQ[2] = (Q[0] * Q[2] - st * (PUx) / dV - st * (Q[0] * Q[2] * Q[3] - Q[4] * Q[5] / GK_CPI4) / y) /
+            QQ[0];
+    QQ[3] = (Q[0] * Q[3] - st * (PUy) / dV -
+             st * (Q[0] * Q[3] * Q[3] + (Q[6] * Q[6] - Q[5] * Q[5]) / GK_CPI4) / y) / QQ[0];
+    QQ[4] = (Q[4] - st * (PBx) / dV - st * (Q[3] * Q[4] - Q[5] * Q[2]) / y);
+    QQ[5] = (Q[5] - st * (PBy) / dV);
+    QQ[6] = (Q[6] - st * (PBz) / dV);
+    const double U = gk_u8(g, Q[0], Q[1], Q[2], Q[3], 0.0, Q[4], Q[5], Q[6]);
+    QQ[1] = (U - st * (PSy) / dV -
+             st * (((U + Q[1] + gk_kvv(Q[4], Q[5], Q[6]) / GK_CPI8) * Q[3] -
+                    Q[5] * gk_skk(Q[2], Q[3], 0.0, Q[4], Q[5], Q[6]) / GK_CPI4) / y) -
+             0.5 * QQ[0] * gk_kvv(QQ[2], QQ[3], 0.0) - gk_kvv(QQ[4], QQ[5], QQ[6]) / GK_CPI8) *
+            (g - 1.0);
+    if (QQ[1] <= 0) QQ[1] = 0.000001;
+}
+
+static void gk_to_q(const gk_cell* c, double* q) {
+    q[0] = c->sx; q[1] = c->sy; q[2] = c->ux; q[3] = c->uy;
+    q[4] = c->bx; q[5] = c->by; q[6] = c->bz;
+}
+
+/* dx * minmod((a - b)/dx, (b - c)/dx) for every component; component 3 (vy) from the
+ * pressures as written (kernel.cu:2966 ...) unless fixed */
+static void gk_slopes(const gk_cell* a, const gk_cell* b, const gk_cell* c, double h, int fixed,
+                      double* D) {
+    double qa[7], qb[7], qc[7];
+    gk_to_q(a, qa);
+    gk_to_q(b, qb);
+    gk_to_q(c, qc);
+    for (int i = 0; i < 7; ++i) {
+        const int j = (i == 3 && !fixed) ? 1 : i;
+        D[i] = h * gdo_minmod((qa[j] - qb[j]) / h, (qb[j] - qc[j]) / h);
+    }
+}
+
+static gk_cell gk_flip(gk_cell c, double fux, double fuy, double fbx, double fby, double fbz) {
+    gk_cell r = c;
+    r.ux = fux * c.ux; r.uy = fuy * c.uy;
+    r.bx = fbx * c.bx; r.by = fby * c.by; r.bz = fbz * c.bz;
+    return r;
+}
+
+/* mirrors as the reference writes them: vx, Bx, By odd (x); vy, Bz odd (y) */
+static gk_cell gk_mx(gk_cell c) {
+    gk_cell r = c;
+    r.ux = -c.ux; r.bx = -c.bx; r.by = -c.by;
+    return r;
+}
+static gk_cell gk_my(gk_cell c) {
+    gk_cell r = c;
+    r.uy = -c.uy; r.bz = -c.bz;
+    return r;
+}
+static gk_cell gk_clamp_vx(gk_cell c) {
+    if (c.ux < 0) c.ux = 0.01;
+    return c;
+}
+
+static double gk_cell_step(const gdo_config* c, const double* s, const double* u, const double* b,
+                           int n, int m, double T_do, double* out, int* frozen) {
+    const int N = c->N, M = c->M;
+    const double g = c->gamma, dx = c->dx, dy = c->dy;
+    const double x_min = c->x0, y_min = c->y0;
+    const double y = y_min + m * (c->y_max) / (M);
+    const double x = x_min + n * (c->x_max - x_min) / (N - 1);
+    const double dist = sqrt(x * x + y * y);
+    const int fixed = c->scheme == 2;
+    const gk_cell c1 = gk_load(s, u, b, (long)m * N + n);
+    *frozen = 0;
+    if (dist < c->frozen_radius) {
+        *frozen = 1;
+        return 1000.0;
+    }
+#define AT(nn, mm) gk_load(s, u, b, (long)(mm) * N + (nn))
+    const gk_cell amb = {1.0, 1.0 / g, 0.0, 0.0, 0.0, 0.0, 0.0};
+    gk_cell c2, c3, c4, c5, c6, c7, c8, c9, c10, c11, c12, c13;
+    if (m == M - 1) { c5 = amb; c5.bx = c1.bx; c5.by = c1.by; c5.bz = c1.bz; }
+    else c5 = AT(n, m + 1);
+    if (n == N - 1) c2 = gk_clamp_vx(c1);
+    else c2 = AT(n + 1, m);
+    if (n == 0) c4 = gk_mx(c1);
+    else c4 = AT(n - 1, m);
+    if (m == 0) c3 = gk_my(c1);
+    else c3 = AT(n, m - 1);
+    if (n == N - 1) c10 = c5;
+    else if (m == M - 1) { c10 = amb; c10.bx = c2.bx; c10.by = c2.by; c10.bz = c2.bz; }
+    else c10 = AT(n + 1, m + 1);
+    if (m == 0) {
+        c12 = gk_my(c4);
+        c11 = gk_my(c2);
+    } else {
+        if (n == 0) c12 = gk_mx(c3);
+        else c12 = AT(n - 1, m - 1);
+        if (n == N - 1) c11 = gk_clamp_vx(c3);
+        else c11 = AT(n + 1, m - 1);
+    }
+    if (n == 0) c13 = gk_mx(c5);
+    else if (m == M - 1) { c13 = amb; c13.bx = c4.bx; c13.by = c4.by; c13.bz = c4.bz; }
+    else c13 = AT(n - 1, m + 1);
+    if (n >= N - 2) c6 = gk_clamp_vx(c2);
+    else c6 = AT(n + 2, m);
+    if (m >= M - 2) c9 = c5;
+    else c9 = AT(n, m + 2);
+    if (n == 0 || n == 1) c8 = gk_mx(c2);
+    else c8 = AT(n - 2, m);
+    if (m == 1) c7 = gk_my(c5);
+    else if (m == 0) c7 = gk_my(c3);
+    else c7 = AT(n, m - 2);
+#undef AT
+    (void)gk_flip;
+    double DX1[7], DY1[7], DX2[7], DY2[7], DX3[7], DY3[7], DX4[7], DY4[7], DX5[7], DY5[7];
+    gk_slopes(&c2, &c1, &c4, dx, fixed, DX1);
+    gk_slopes(&c6, &c2, &c1, dx, fixed, DX2);
+    gk_slopes(&c1, &c4, &c8, dx, fixed, DX4);
+    gk_slopes(&c10, &c5, &c13, dx, fixed, DX5);
+    gk_slopes(&c11, &c3, &c12, dx, fixed, DX3);
+    gk_slopes(&c5, &c1, &c3, dy, fixed, DY1);
+    gk_slopes(&c9, &c5, &c1, dy, fixed, DY5);
+    gk_slopes(&c13, &c4, &c12, dy, fixed, DY4);
+    gk_slopes(&c10, &c2, &c11, dy, fixed, DY2);
+    gk_slopes(&c1, &c3, &c7, dy, fixed, DY3);
+    double Q1[7], Q2[7], Q3[7], Q4[7], Q5[7];
+    gk_to_q(&c1, Q1); gk_to_q(&c2, Q2); gk_to_q(&c3, Q3); gk_to_q(&c4, Q4); gk_to_q(&c5, Q5);
+    double QQ1[7], QQ2[7], QQ3[7], QQ4[7], QQ5[7];
+    const double st = T_do / 2.0;
+    gk_predictor(c, Q1, DX1, DY1, QQ1, st, y);
+    gk_predictor(c, Q2, DX2, DY2, QQ2, st, y);
+    gk_predictor(c, Q3, DX3, DY3, QQ3, st, y - dy);
+    gk_predictor(c, Q4, DX4, DY4, QQ4, st, y);
+    gk_predictor(c, Q5, DX5, DY5, QQ5, st, y + dy);
+    /* faces E (own +DX1, nbr Q2 -DX2), S (own -DY1, nbr Q3 +DY3), W (own -DX1, nbr Q4 +DX4),
+     * N (own +DY1, nbr Q5 -DY5) */
+    const double* nbrQ[4] = {Q2, Q3, Q4, Q5};
+    const double* nbrQQ[4] = {QQ2, QQ3, QQ4, QQ5};
+    const double* ownD[4] = {DX1, DY1, DX1, DY1};
+    const double* nbrD[4] = {DX2, DY3, DX4, DY5};
+    const double ownS[4] = {1.0, -1.0, -1.0, 1.0};
+    const double fn1[4] = {1.0, 0.0, -1.0, 0.0}, fn2[4] = {0.0, -1.0, 0.0, 1.0};
+    double tmin = 1000;
+    double PSx = 0.0, PSy = 0.0, PUx = 0.0, PUy = 0.0, PBx = 0.0, PBy = 0.0, PBz = 0.0;
+    for (int f = 0; f < 4; ++f) {
+        const double* A = nbrQ[f];
+        const double* AA = nbrQQ[f];
+        double L[8], R[8];
+        double ro_1, p_1, ro_2, p_2;
+        if (ownS[f] > 0) {
+            ro_1 = (Q1[0] + QQ1[0]) / 2.0 + ownD[f][0] / 2.0;
+            p_1 = (Q1[1] + QQ1[1]) / 2.0 + ownD[f][1] / 2.0;
+        } else {
+            ro_1 = (Q1[0] + QQ1[0]) / 2.0 - ownD[f][0] / 2.0;
+            p_1 = (Q1[1] + QQ1[1]) / 2.0 - ownD[f][1] / 2.0;
+        }
+        if (ro_1 <= 0.0) ro_1 = (Q1[0] + QQ1[0]) / 2.0;
+        if (p_1 <= 0.0) p_1 = (Q1[1] + QQ1[1]) / 2.0;
+        if (ownS[f] > 0) {
+            ro_2 = (A[0] + AA[0]) / 2.0 - nbrD[f][0] / 2.0;
+            p_2 = (A[1] + AA[1]) / 2.0 - nbrD[f][1] / 2.0;
+        } else {
+            ro_2 = (A[0] + AA[0]) / 2.0 + nbrD[f][0] / 2.0;
+            p_2 = (A[1] + AA[1]) / 2.0 + nbrD[f][1] / 2.0;
+        }
+        if (ro_2 <= 0.0) ro_2 = (A[0] + AA[0]) / 2.0;
+        if (p_2 <= 0.0) p_2 = (A[1] + AA[1]) / 2.0;
+        L[0] = ro_1; L[1] = p_1; L[4] = 0.0;
+        R[0] = ro_2; R[1] = p_2; R[4] = 0.0;
+        const int qi[5] = {2, 3, 4, 5, 6}, li[5] = {2, 3, 5, 6, 7};
+        for (int t = 0; t < 5; ++t) {
+            const int i = qi[t];
+            L[li[t]] = ownS[f] > 0 ? (Q1[i] + QQ1[i]) / 2.0 + ownD[f][i] / 2.0
+                                   : (Q1[i] + QQ1[i]) / 2.0 - ownD[f][i] / 2.0;
+            R[li[t]] = ownS[f] > 0 ? (A[i] + AA[i]) / 2.0 - nbrD[f][i] / 2.0
+                                   : (A[i] + AA[i]) / 2.0 + nbrD[f][i] / 2.0;
+        }
+        double P[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const double rad = (f == 0 || f == 2) ? dx : dy;
+        const double t = gdo_hlld(L, R, fn1[f], fn2[f], 0.0, rad, 3, g, c->krit, P);
+        tmin = my_min(tmin, t);
+        const double h = (f == 0 || f == 2) ? dy : dx;
+        PSx = PSx + P[0] * h;
+        PSy = PSy + P[7] * h;
+        PUx = PUx + P[1] * h;
+        PUy = PUy + P[2] * h;
+        PBx = PBx + P[4] * h;
+        PBy = PBy + P[5] * h;
+        PBz = PBz + P[6] * h;
+    }
+    const double dV = dx * dy;
+    const double Pdiv = 0.0;
+    const double hT = T_do / 2.0;
+    double A[7];
+    for (int i = 0; i < 7; ++i) A[i] = (Q1[i] + QQ1[i]) / 2.0;
+    double r2 = A[0] - hT * PSx / dV - hT * A[0] * A[3] / y;
+    if (r2 <= 0) r2 = A[0];
+    const double ux2 = (A[0] * A[2] - hT * (PUx + (A[4] / GK_CPI4) * Pdiv) / dV -
+                        hT * (A[0] * A[2] * A[3] - A[4] * A[5] / GK_CPI4) / y) / r2;
+    const double uy2 = (A[0] * A[3] - hT * (PUy + (A[5] / GK_CPI4) * Pdiv) / dV -
+                        hT * (A[0] * A[3] * A[3] + (A[6] * A[6] - A[5] * A[5]) / GK_CPI4) / y) / r2;
+    const double bx2 = (A[4] - hT * (PBx + A[2] * Pdiv) / dV - hT * (A[3] * A[4] - A[5] * A[2]) / y);
+    const double by2 = (A[5] - hT * (PBy + A[3] * Pdiv) / dV);
+    const double bz2 = (A[6] - hT * (PBz) / dV);
+    const double U = gk_u8(g, A[0], A[1], A[2], A[3], 0.0, A[4], A[5], A[6]);
+    const double sk = gk_skk(A[2], A[3], 0.0, A[4], A[5], A[6]);
+    double p2 = (U - hT * (PSy + (sk / GK_CPI4) * Pdiv) / dV -
+                 hT * (((U + A[1] + gk_kvv(A[4], A[5], A[6]) / GK_CPI8) * A[3] -
+                        A[5] * sk / GK_CPI4) / y) -
+                 0.5 * r2 * gk_kvv(ux2, uy2, 0.0) - gk_kvv(bx2, by2, bz2) / GK_CPI8) * (g - 1.0);
+    if (p2 <= 0) p2 = 0.000001;
+    out[0] = r2; out[1] = p2; out[2] = ux2; out[3] = uy2;
+    out[4] = bx2; out[5] = by2; out[6] = bz2;
+    return tmin;
+}
+
+static double gdo_step_hancock(const gdo_config* c, const double* s, const double* u,
+                               const double* b, double* s2, double* u2, double* b2, double T_do,
+                               double T_in, int dt_only) {
+    const int N = c->N, M = c->M;
+    double T = T_in;
+#pragma omp parallel
+    {
+        double tloc = T_in;
+#pragma omp for schedule(static)
+        for (int m = 0; m < M; ++m) {
+            for (int n = 0; n < N; ++n) {
+                const long k = (long)m * N + n;
+                double out[7];
+                int frozen = 0;
+                const double t = gk_cell_step(c, s, u, b, n, m, T_do, out, &frozen);
+                if (frozen) {
+                    if (!dt_only) {
+                        s2[2 * k] = s[2 * k]; s2[2 * k + 1] = s[2 * k + 1];
+                        u2[2 * k] = u[2 * k]; u2[2 * k + 1] = u[2 * k + 1];
+                        b2[3 * k] = b[3 * k]; b2[3 * k + 1] = b[3 * k + 1];
+                        b2[3 * k + 2] = b[3 * k + 2];
+                    }
+                    continue;
+                }
+                if (tloc > t) tloc = t;
+                if (!dt_only) {
+                    s2[2 * k] = out[0]; s2[2 * k + 1] = out[1];
+                    u2[2 * k] = out[2]; u2[2 * k + 1] = out[3];
+                    b2[3 * k] = out[4]; b2[3 * k + 1] = out[5]; b2[3 * k + 2] = out[6];
+                }
+            }
+        }
+#pragma omp critical
+        {
+            if (tloc < T) T = tloc;
+        }
+    }
+    return T;
+}
+
 double gdo_step(const gdo_config* c, const double* s, const double* u, const double* b,
                 double* s2, double* u2, double* b2, double T_do, double T_in, int dt_only) {
+    if (c->scheme == 1 || c->scheme == 2)
+        return gdo_step_hancock(c, s, u, b, s2, u2, b2, T_do, T_in, dt_only);
     const int N = c->N, M = c->M;
     double T = T_in;
 #pragma omp parallel

@@ -44,6 +44,12 @@ typedef struct {
     int method;            /* flux code: Euler 1 = HLLC; MHD 2 = HLLC-MHD, 3 = HLLD         */
     int bc[4];             /* left, right, bottom, top                                    */
     double frozen_radius;  /* cells with sqrt(x^2+y^2) < this are copied (kernel.cu:2218)  */
+    int scheme;            /* 0: TVD step by order; 1: MUSCL-Hancock Kernel_GKR
+                              (kernel.cu:2663) as written (v_y slopes from p, :2966);
+                              2: the same with v_y slopes from v_y                        */
+    double x_max, y_max;   /* the reference's x_max, y_max (kernel.cu:15, 17): Kernel_GKR
+                              places cells at x_min + n (x_max - x_min)/(N - 1),
+                              y_min + m y_max / M                                        */
 } gdo_config;
 
 /* kernel.cu:51-84 */

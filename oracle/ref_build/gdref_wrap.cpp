@@ -49,6 +49,8 @@ void Kernel_TVD(double2* s, double2* u, double3* b, double2* s2, double2* u2,
                 double3* b2, double* T, double* T_do, int i, int method);       /* kernel.cu:2198 */
 void Kernel_TVD_old(double2* s, double2* u, double2* s2, double2* u2, double* T,
                     double* T_do, int method);                                  /* kernel.cu:3286 */
+void Kernel_GKR(double2* s, double2* u, double3* b, double2* s2, double2* u2, double3* b2,
+                double* T, double* T_do, int i, int method);                    /* kernel.cu:2663 */
 void print_file_mini(double2* s, double2* u, std::string name);                 /* kernel.cu:3682 */
 void print_file_mini2(double2* s, double2* u, double3* b, std::string name);    /* kernel.cu:3724 */
 void print_file_mini2(double2* s, double2* u, double3* b, std::string name,
@@ -165,6 +167,20 @@ void gdref_kernel_tvd(const double* s, const double* u, const double* b, double*
     double tdo = T_do;
     for_each_cell(T, [&](double* t) {
         Kernel_TVD(ps.data(), pu.data(), pb.data(), (double2*)s2, (double2*)u2, (double3*)b2, t,
+                   &tdo, i, method);
+    });
+}
+
+/* MUSCL-Hancock step (Kernel_GKR, kernel.cu:2663-3284) over all cells. */
+void gdref_kernel_gkr(const double* s, const double* u, const double* b, double* s2, double* u2,
+                      double* b2, double* T, double T_do, int i, int method) {
+    const long K = (long)gdref_N * gdref_M;
+    auto ps = padded<double2>(s, K);
+    auto pu = padded<double2>(u, K);
+    auto pb = padded<double3>(b, K);
+    double tdo = T_do;
+    for_each_cell(T, [&](double* t) {
+        Kernel_GKR(ps.data(), pu.data(), pb.data(), (double2*)s2, (double2*)u2, (double3*)b2, t,
                    &tdo, i, method);
     });
 }

@@ -17,6 +17,10 @@ Fixtures:
                    reference's wind initial condition on a reduced axisymmetric grid
   faces_hll.npz    Euler HLL (kernel.cu:1485) on random and branch-targeted faces, and one
                    Ker_Dekard step with method 0 (HLL everywhere)
+  gkr.npz          Kernel_GKR (kernel.cu:2663-3284, the MUSCL-Hancock step): one step on
+                   random states of six small grids whose sizes reach every edge branch of
+                   its stencil, and 20 steps of Kernel_GKR + funk_time from the wind of
+                   problems.hancock_wind on a reduced grid
   io_files.npz     the reference's state files for one random state with hard-to-print
                    values: print_file_mini / print_file_mini2 (both overloads) Tecplot
                    snapshots (kernel.cu:3682-3808) and the restart dump of its main loop
@@ -252,12 +256,42 @@ def io_files(ref):
                         gamma=gamma, nmin=3, ttt=0.123456789, s=s, u=u, b=b, **out)
 
 
+GKR_CASES = ((40, 24, 9.0, 5.0), (33, 17, 9.0, 5.0), (24, 16, 30.0, 20.0), (7, 5, 9.0, 5.0),
+             (3, 3, 9.0, 5.0), (4, 6, 9.0, 5.0))
+
+
+def gkr_golden(ref, nsteps=20):
+    rng = np.random.default_rng(SEED + 13)
+    T_do = 2e-3
+    out = dict(ncases=len(GKR_CASES), T_do=T_do, gamma=5.0 / 3.0, krit=0.25)
+    for c, (N, M, xmax, ymax) in enumerate(GKR_CASES):
+        s, u, b = random_state(rng, N * M)
+        ref.set_params(5.0 / 3.0, 0.25, N, M, xmax, ymax)
+        s2, u2, b2, T = ref.kernel_gkr(s, u, b, T_do, 0, 3)
+        out.update({f"c{c}_NM": np.array([N, M]), f"c{c}_ext": np.array([xmax, ymax]),
+                    f"c{c}_s": s, f"c{c}_u": u, f"c{c}_b": b,
+                    f"c{c}_s2": s2, f"c{c}_u2": u2, f"c{c}_b2": b2, f"c{c}_T": T})
+    N, M, xmax, ymax = 72, 40, 9.0, 5.0
+    cfg, s, u, b = problems.hancock_wind(N, M, xmax, ymax)
+    ref.set_params(cfg.gamma, cfg.krit, N, M, xmax, ymax)
+    out.update(run_N=N, run_M=M, run_ext=np.array([xmax, ymax]), run_nsteps=nsteps,
+               run_s0=s.copy(), run_u0=u.copy(), run_b0=b.copy())
+    T_do, TT = 1e-8, 0.0
+    for _ in range(nsteps):
+        s, u, b, T = ref.kernel_gkr(s, u, b, T_do, 0, 3)
+        T_do = T
+        TT += T_do
+    out.update(run_s=s, run_u=u, run_b=b, run_T_do=T_do, run_TT=TT)
+    np.savez_compressed(os.path.join(HERE, "gkr.npz"), **out)
+
+
 def main():
     oracle.build(ref=True)
     ref = oracle.Reference()
     ref.lib.gdref_set_threads(1)
     jobs = {"faces": faces, "recon": recon, "step_native": step_native,
-            "run_native": run_native, "io_files": io_files, "hll": hll_golden}
+            "run_native": run_native, "io_files": io_files, "hll": hll_golden,
+            "gkr": gkr_golden}
     for name in (sys.argv[1:] or list(jobs)):
         jobs[name](ref)
     for f in sorted(os.listdir(HERE)):

@@ -10,7 +10,8 @@ import oracle
 def grid_of(cfg: g.Config) -> oracle.Grid:
     return oracle.Grid(cfg.N, cfg.M, cfg.dx, cfg.dy, cfg.x0, cfg.y0, cfg.gamma, cfg.krit,
                        physics=cfg.physics, geometry=cfg.geometry, order=cfg.order,
-                       method=cfg.method, bc=tuple(cfg.bc), frozen_radius=cfg.frozen_radius)
+                       method=cfg.method, bc=tuple(cfg.bc), frozen_radius=cfg.frozen_radius,
+                       scheme=cfg.scheme, x_max=cfg.x_max, y_max=cfg.y_max)
 
 
 def to_dev(a):

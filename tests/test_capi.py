@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(gdlib):
 
 
 def test_abi_version_and_status_strings(gdlib):
-    assert gdlib.gd_abi_version() == 2
+    assert gdlib.gd_abi_version() == 3
     assert gdlib.gd_status_string(0) == b"ok"
     assert gdlib.gd_status_string(1) == b"invalid argument"
 
@@ -63,6 +63,48 @@ def test_invalid_config_rejected_without_device(gdlib, mutate):
     h = ctypes.c_void_p()
     st = gdlib.gd_create(ctypes.byref(c.cstruct()), ctypes.byref(h))
     assert st == 1 and not h.value
+
+
+def test_config_layout_matches_header(tmp_path):
+    """sizeof(gd_config) and every field's offset, from the C compiler, equal the ctypes
+    mirror's (the Hancock fields were appended in ABI 3)."""
+    fields = [f for f, _ in g.gd_config._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "gd2d.h"\n'
+                   "int main(void) {\n"
+                   '  printf("%zu\\n", sizeof(gd_config));\n' +
+                   "".join(f'  printf("%zu\\n", offsetof(gd_config, {f}));\n' for f in fields) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(g.gd_config)
+    assert got[1:] == [getattr(g.gd_config, f).offset for f in fields]
+
+
+def hancock_base():
+    from golikov_2d_gb300 import problems
+    return problems.hancock_config(16, 16)
+
+
+@pytest.mark.parametrize("mutate,status", [
+    (lambda c: setattr(c, "scheme", 3), 1),
+    (lambda c: setattr(c, "scheme", -1), 1),
+    (lambda c: setattr(c, "x_max", 0.0), 1),
+    (lambda c: setattr(c, "y_max", float("inf")), 1),
+    (lambda c: setattr(c, "geometry", g.CARTESIAN), 5),       # Kernel_GKR is axisymmetric
+    (lambda c: setattr(c, "method", g.METHOD_HLLC_MHD), 5),   # its faces are HLLD (metod 3)
+    (lambda c: setattr(c, "bc", (g.BC_MIRROR_X, g.BC_OUTFLOW, g.BC_AXIS, g.BC_AMBIENT)), 5),
+    (lambda c: (setattr(c, "physics", g.EULER), setattr(c, "method", g.METHOD_HLLC)), 5),
+])
+def test_hancock_config_checks_without_device(gdlib, mutate, status):
+    c = hancock_base()
+    mutate(c)
+    h = ctypes.c_void_p()
+    st = gdlib.gd_create(ctypes.byref(c.cstruct()), ctypes.byref(h))
+    assert st == status and not h.value
 
 
 def test_null_arguments_rejected(gdlib):

@@ -1,0 +1,173 @@
+"""The MUSCL-Hancock step (Kernel_GKR, kernel.cu:2663-3284) on the GPU, through the C ABI.
+
+Parity mode reproduces the reference's own outputs bit for bit: the golden vectors written
+from its compiled Kernel_GKR (single steps on grids down to 3 x 3, and a 20-step run with
+funk_time), and the oracle on fresh states for both schemes.  Fast mode (face-once tiles
+plus the per-cell edge band) agrees with parity to 1e-12 per step, keeps that bound over a
+run, and follows the launch protocol (two launches per step, graphs)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import golikov_2d_gb300 as g
+from conftest import golden
+from golikov_2d_gb300 import problems
+from gpu_util import gpu_run, gpu_step_ref, grid_of, max_rel_l1, to_dev
+
+pytestmark = pytest.mark.gpu
+
+PER_STEP_TOL = 1e-12  # relative L1 per conserved field, fast vs parity, one step
+RUN_TOL = 1e-11       # the same after a 30-step run
+
+
+def case_cfg(gz, c, mode, scheme=g.SCHEME_HANCOCK_REF):
+    N, M = (int(v) for v in gz[f"c{c}_NM"])
+    xmax, ymax = (float(v) for v in gz[f"c{c}_ext"])
+    return problems.hancock_config(N, M, xmax, ymax, scheme=scheme, mode=mode)
+
+
+def random_state(rng, K):
+    s = np.stack([rng.uniform(0.3, 2.0, K), rng.uniform(0.1, 2.0, K)], 1)
+    u = rng.uniform(-1.0, 1.0, (K, 2))
+    b = rng.uniform(-2.0, 2.0, (K, 3))
+    return s, u, b
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_step_matches_reference(cuda, case):
+    gz = golden("gkr.npz")
+    cfg = case_cfg(gz, case, g.MODE_PARITY)
+    s2, u2, b2, T = gpu_step_ref(cfg, gz[f"c{case}_s"], gz[f"c{case}_u"], gz[f"c{case}_b"],
+                                 float(gz["T_do"]))
+    assert T == gz[f"c{case}_T"]
+    assert np.array_equal(s2, gz[f"c{case}_s2"])
+    assert np.array_equal(u2, gz[f"c{case}_u2"])
+    assert np.array_equal(b2, gz[f"c{case}_b2"])
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_run_matches_reference(cuda, use_graph):
+    """Kernel_GKR + funk_time, 20 steps from problems.hancock_wind: state, dt and time."""
+    gz = golden("gkr.npz")
+    N, M = int(gz["run_N"]), int(gz["run_M"])
+    xmax, ymax = (float(v) for v in gz["run_ext"])
+    cfg, *_ = problems.hancock_wind(N, M, xmax, ymax, mode=g.MODE_PARITY)
+    nsteps = int(gz["run_nsteps"])
+    s, u, b, st = gpu_run(cfg, gz["run_s0"], gz["run_u0"], gz["run_b0"], nsteps, T_do=1e-8,
+                          use_graph=use_graph)
+    assert st.dt == gz["run_T_do"] and st.t == gz["run_TT"] and st.steps == nsteps
+    assert np.array_equal(s, gz["run_s"]) and np.array_equal(u, gz["run_u"])
+    assert np.array_equal(b, gz["run_b"])
+
+
+@pytest.mark.parametrize("scheme", [g.SCHEME_HANCOCK_REF, g.SCHEME_HANCOCK])
+@pytest.mark.parametrize("N,M,xmax,ymax", [(45, 29, 9.0, 5.0), (6, 7, 9.0, 5.0), (3, 3, 9.0, 5.0),
+                                           (70, 40, 35.0, 20.0)])
+def test_parity_matches_oracle(cuda, oracle_lib, scheme, N, M, xmax, ymax):
+    rng = np.random.default_rng(1000 + N + 7 * M + scheme)
+    s, u, b = random_state(rng, N * M)
+    cfg = problems.hancock_config(N, M, xmax, ymax, scheme=scheme, mode=g.MODE_PARITY)
+    s2, u2, b2, T = gpu_step_ref(cfg, s, u, b, 2e-3)
+    so, uo, bo, To = oracle_lib.step(grid_of(cfg), s, u, b, 2e-3)
+    assert T == To
+    assert np.array_equal(s2, so) and np.array_equal(u2, uo) and np.array_equal(b2, bo)
+
+
+@pytest.mark.parametrize("scheme", [g.SCHEME_HANCOCK_REF, g.SCHEME_HANCOCK])
+@pytest.mark.parametrize("N,M,xmax,ymax", [(100, 70, 9.0, 5.0), (37, 9, 9.0, 5.0),
+                                           (5, 5, 9.0, 5.0), (130, 90, 40.0, 30.0)])
+def test_fast_step_matches_parity(cuda, scheme, N, M, xmax, ymax):
+    """Interior tiles and edge band together: within 1e-12 of the reference arithmetic."""
+    rng = np.random.default_rng(2000 + N + 7 * M + scheme)
+    s, u, b = random_state(rng, N * M)
+    par = problems.hancock_config(N, M, xmax, ymax, scheme=scheme, mode=g.MODE_PARITY)
+    fast = problems.hancock_config(N, M, xmax, ymax, scheme=scheme, mode=g.MODE_FAST)
+    s2p, u2p, b2p, Tp = gpu_step_ref(par, s, u, b, 2e-3)
+    s2f, u2f, b2f, Tf = gpu_step_ref(fast, s, u, b, 2e-3)
+    assert abs(Tf - Tp) <= PER_STEP_TOL * Tp
+    assert max_rel_l1(par, (s2f, u2f, b2f), (s2p, u2p, b2p)) <= PER_STEP_TOL
+    # cells of the frozen sphere (Kernel_GKR's coordinates) are copied bit for bit by both
+    x0, y0 = par.x0, par.y0
+    X, Y = np.meshgrid(x0 + np.arange(N) * (xmax - x0) / (N - 1), y0 + np.arange(M) * ymax / M)
+    frozen = (np.sqrt(X * X + Y * Y) < problems.GKR_FROZEN).ravel()
+    assert frozen.any()
+    for outs in ((s2f, u2f, b2f), (s2p, u2p, b2p)):
+        for out, src in zip(outs, (s, u, b)):
+            assert np.array_equal(out[frozen], src[frozen])
+
+
+def test_fast_run_matches_parity(cuda):
+    """30 steps of the wind, fast against parity, with the dt each computes itself."""
+    N, M = 120, 68
+    par, s, u, b = problems.hancock_wind(N, M, mode=g.MODE_PARITY)
+    fast, *_ = problems.hancock_wind(N, M, mode=g.MODE_FAST)
+    sp, up, bp, stp = gpu_run(par, s, u, b, 30, T_do=1e-3)
+    sf, uf, bf, stf = gpu_run(fast, s, u, b, 30, T_do=1e-3)
+    assert stf.steps == stp.steps == 30
+    assert abs(stf.t - stp.t) <= RUN_TOL * stp.t
+    assert max_rel_l1(par, (sf, uf, bf), (sp, up, bp)) <= RUN_TOL
+    assert stf.nonfinite == 0 and stp.nonfinite == 0
+
+
+def test_fast_graph_equals_plain_and_counts_launches(cuda):
+    N, M = 90, 50
+    cfg, s, u, b = problems.hancock_wind(N, M, mode=g.MODE_FAST)
+    a = gpu_run(cfg, s, u, b, 12, T_do=1e-3, use_graph=False)
+    c = gpu_run(cfg, s, u, b, 12, T_do=1e-3, use_graph=True)
+    for x, y in zip(a[:3], c[:3]):
+        assert np.array_equal(x, y)
+    assert a[3].dt == c[3].dt and a[3].t == c[3].t
+    for mode, per_step in ((g.MODE_FAST, 2), (g.MODE_PARITY, 1)):
+        cfg.mode = mode
+        sol = g.Solver(cfg)
+        sol.import_state(s, u, b)
+        sol.set_time(1e-3, 0.0)
+        l0 = sol.launch_count()
+        sol.advance(5)
+        assert sol.launch_count() - l0 == 5 * per_step
+        sol.close()
+
+
+def test_static_entry_matches_context_entry(cuda):
+    """gd_step_ref_static routes the Hancock schemes like gd_step_ref."""
+    import torch
+    rng = np.random.default_rng(7)
+    N, M = 41, 23
+    s, u, b = random_state(rng, N * M)
+    for mode in (g.MODE_PARITY, g.MODE_FAST):
+        cfg = problems.hancock_config(N, M, mode=mode)
+        ref = gpu_step_ref(cfg, s, u, b, 2e-3)
+        L = g.load()
+        ds, du, db = to_dev(s), to_dev(u), to_dev(b)
+        s2, u2, b2 = torch.zeros_like(ds), torch.zeros_like(du), torch.zeros_like(db)
+        T = torch.tensor([1e7], dtype=torch.float64, device="cuda")
+        Tdo = torch.tensor([2e-3], dtype=torch.float64, device="cuda")
+        c = cfg.cstruct()
+        st = L.gd_step_ref_static(ctypes.byref(c), ds.data_ptr(), du.data_ptr(), db.data_ptr(),
+                                  s2.data_ptr(), u2.data_ptr(), b2.data_ptr(), T.data_ptr(),
+                                  Tdo.data_ptr(), g.METHOD_CONFIG, None)
+        assert st == 0
+        torch.cuda.synchronize()
+        assert float(T.cpu()[0]) == ref[3]
+        assert np.array_equal(s2.cpu().numpy(), ref[0])
+        assert np.array_equal(u2.cpu().numpy(), ref[1])
+        assert np.array_equal(b2.cpu().numpy(), ref[2])
+
+
+def test_method_override_other_than_hlld_unsupported(cuda):
+    import torch
+    cfg = problems.hancock_config(16, 16, mode=g.MODE_PARITY)
+    rng = np.random.default_rng(3)
+    s, u, b = random_state(rng, 256)
+    sol = g.Solver(cfg)
+    ds, du, db = to_dev(s), to_dev(u), to_dev(b)
+    T = torch.tensor([1e7], dtype=torch.float64, device="cuda")
+    Tdo = torch.tensor([1e-3], dtype=torch.float64, device="cuda")
+    with pytest.raises(g.GdError) as e:
+        sol.kernel_step(ds, du, db, torch.zeros_like(ds), torch.zeros_like(du),
+                        torch.zeros_like(db), T, Tdo, 0, g.METHOD_HLLC_MHD)
+    assert e.value.status == 5
+    sol.kernel_step(ds, du, db, torch.zeros_like(ds), torch.zeros_like(du), torch.zeros_like(db),
+                    T, Tdo, 0, g.METHOD_HLLD)
+    sol.close()

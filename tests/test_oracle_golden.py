@@ -142,3 +142,65 @@ def test_hll_faces_and_first_order_step(oracle_lib):
     mask = mask.ravel()
     assert np.array_equal(s2[mask], g["dek_s"][mask])
     assert np.array_equal(u2[mask], g["dek_u"][mask])
+
+
+def gkr_grid(N, M, xmax, ymax, scheme=1, gamma=5.0 / 3.0, krit=0.25):
+    """Kernel_GKR's setting (kernel.cu:2663-3284): its edge cells, metod 3, frozen sphere 2.0."""
+    return oracle.Grid(N, M, xmax / N, ymax / M, xmax / (2.0 * N), ymax / (2.0 * M), gamma, krit,
+                       physics=oracle.MHD, geometry=oracle.AXISYM, order=2, method=3,
+                       bc=(oracle.BC_MIRROR_X, oracle.BC_OUTFLOW, oracle.BC_AXIS,
+                           oracle.BC_AMBIENT_KEEPB),
+                       frozen_radius=2.0, scheme=scheme, x_max=xmax, y_max=ymax)
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_hancock_step(oracle_lib, case):
+    """One Kernel_GKR step on the golden grids (down to 3 x 3, where every stencil point
+    of every cell is a substitute), bit for bit including the dt."""
+    g = golden("gkr.npz")
+    N, M = (int(v) for v in g[f"c{case}_NM"])
+    xmax, ymax = (float(v) for v in g[f"c{case}_ext"])
+    grid = gkr_grid(N, M, xmax, ymax)
+    s2, u2, b2, T = oracle_lib.step(grid, g[f"c{case}_s"], g[f"c{case}_u"], g[f"c{case}_b"],
+                                    float(g["T_do"]))
+    assert T == g[f"c{case}_T"]
+    assert np.array_equal(s2, g[f"c{case}_s2"])
+    assert np.array_equal(u2, g[f"c{case}_u2"])
+    assert np.array_equal(b2, g[f"c{case}_b2"])
+
+
+def test_hancock_run_20_steps(oracle_lib):
+    """20 steps of Kernel_GKR + funk_time from the wind of problems.hancock_wind, bit for bit
+    including the dt sequence."""
+    g = golden("gkr.npz")
+    N, M = int(g["run_N"]), int(g["run_M"])
+    xmax, ymax = (float(v) for v in g["run_ext"])
+    grid = gkr_grid(N, M, xmax, ymax)
+    s, u, b, T_do, TT = oracle_lib.run(grid, g["run_s0"], g["run_u0"], g["run_b0"],
+                                       int(g["run_nsteps"]), 1e-8)
+    assert T_do == g["run_T_do"] and TT == g["run_TT"]
+    assert np.array_equal(s, g["run_s"]) and np.array_equal(u, g["run_u"])
+    assert np.array_equal(b, g["run_b"])
+
+
+def test_hancock_schemes_differ_only_in_vy_slopes(oracle_lib):
+    """Scheme 1 takes the v_y slopes from the pressures (kernel.cu:2966 ...), scheme 2 from
+    v_y.  With v_y == p in every cell the two agree exactly on the rows whose stencils meet
+    no axis mirror (v_y odd) or ambient substitute (v_y = 0, p = 1/gamma): 2 <= m < M-2.
+    On a general state they differ."""
+    rng = np.random.default_rng(5)
+    N, M, xmax, ymax = 30, 20, 9.0, 5.0
+    K = N * M
+    s = np.stack([rng.uniform(0.3, 2.0, K), rng.uniform(0.1, 2.0, K)], 1)
+    u = np.stack([rng.uniform(-1, 1, K), s[:, 1]], 1)
+    b = rng.uniform(-2.0, 2.0, (K, 3))
+    r1 = oracle_lib.step(gkr_grid(N, M, xmax, ymax, scheme=1), s, u, b, 2e-3)
+    r2 = oracle_lib.step(gkr_grid(N, M, xmax, ymax, scheme=2), s, u, b, 2e-3)
+    rows = slice(2 * N, (M - 2) * N)
+    for a, c in zip(r1[:3], r2[:3]):
+        assert np.array_equal(a[rows], c[rows])
+    u[:, 1] = rng.uniform(-1, 1, K)
+    r1 = oracle_lib.step(gkr_grid(N, M, xmax, ymax, scheme=1), s, u, b, 2e-3)
+    r2 = oracle_lib.step(gkr_grid(N, M, xmax, ymax, scheme=2), s, u, b, 2e-3)
+    assert not np.array_equal(r1[1], r2[1])
+

@@ -96,3 +96,22 @@ def test_hll_random_faces(oracle_lib, reference, gamma):
         t0, F0 = reference.hll(L, R, n1, n2, 0.01)
         t1, F1 = oracle_lib.hll(L, R, n1, n2, 0.01, gamma, 0.4)
         assert t0 == t1 and np.array_equal(F0, F1, equal_nan=True)
+
+
+@pytest.mark.parametrize("seed,N,M,xmax,ymax", [(41, 40, 24, 9.0, 5.0), (42, 19, 11, 9.0, 5.0),
+                                                (43, 5, 4, 9.0, 5.0), (44, 30, 18, 25.0, 14.0)])
+def test_kernel_gkr_random(oracle_lib, reference, seed, N, M, xmax, ymax):
+    """Kernel_GKR (kernel.cu:2663-3284) against the oracle's MUSCL-Hancock restatement."""
+    rng = np.random.default_rng(seed)
+    reference.set_params(5.0 / 3.0, 0.25, N, M, xmax, ymax)
+    s, u, b = rand_state(rng, N * M)
+    s2r, u2r, b2r, Tr = reference.kernel_gkr(s, u, b, 1.5e-3, 0, 3)
+    g = oracle.Grid(N, M, xmax / N, ymax / M, xmax / (2.0 * N), ymax / (2.0 * M), 5.0 / 3.0, 0.25,
+                    physics=oracle.MHD, geometry=oracle.AXISYM, order=2, method=3,
+                    bc=(oracle.BC_MIRROR_X, oracle.BC_OUTFLOW, oracle.BC_AXIS,
+                        oracle.BC_AMBIENT_KEEPB),
+                    frozen_radius=2.0, scheme=1, x_max=xmax, y_max=ymax)
+    s2, u2, b2, T = oracle_lib.step(g, s, u, b, 1.5e-3)
+    assert T == Tr
+    assert np.array_equal(s2, s2r) and np.array_equal(u2, u2r) and np.array_equal(b2, b2r)
+
