@@ -587,6 +587,96 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
     return res
 
 
+HANCOCK_WORKLOAD = ("MUSCL-Hancock step of Kernel_GKR (scheme as written), axisymmetric MHD, "
+                    "HLLD, wind in ambient medium, 3226x1792 (the reference's production grid), "
+                    "CFL 0.25, FP64")
+
+
+def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792,
+                    cpu_steps=1, cpu=True):
+    """The MUSCL-Hancock step (Kernel_GKR) on the reference's production grid: fast and
+    parity modes timed with CUDA events on the launching stream (state 324 MB, larger than
+    L2), e2e through host buffers, and the oracle's restatement on the host cores."""
+    from golikov_2d_gb300 import problems
+    out = {"workload": HANCOCK_WORKLOAD, "cells": N * M, "unit": "cell-updates/s"}
+    stream = torch.cuda.current_stream()
+    for name, mode, k in (("fast", g.MODE_FAST, steps), ("parity", g.MODE_PARITY, parity_steps)):
+        cfg, s, u, b = problems.hancock_wind(N, M, mode=mode)
+        sol = g.Solver(cfg)
+        sol.import_state(s, u, b)
+        sol.set_time(0.0, 0.0)
+        sol.init_dt()
+        sol.advance(warmup)
+        torch.cuda.synchronize()
+        l0 = sol.launch_count()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sol.advance(k)
+        z.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(z) / k
+        st = sol.stats(allow_nonfinite=True)
+        entry = {"value": N * M / (ms * 1e-3), "ms_per_step": ms, "steps": k,
+                 "gpu_launches": sol.launch_count() - l0, "nonfinite": st.nonfinite,
+                 "rho_floor_hits": st.rho_floor_hits, "p_floor_hits": st.p_floor_hits}
+        if mode == g.MODE_FAST:
+            hs, hu, hb = (torch.from_numpy(x).pin_memory() for x in (s, u, b))
+            hs2, hu2, hb2 = (torch.empty_like(x).pin_memory() for x in (hs, hu, hb))
+            sol.import_state(hs, hu, hb)
+            sol.advance(1)
+            sol.export_state(hs2, hu2, hb2)
+            torch.cuda.synchronize()
+            n_e2e = 5
+            t0 = time.perf_counter()
+            for _ in range(n_e2e):
+                sol.import_state(hs, hu, hb)
+                sol.advance(1)
+                sol.export_state(hs2, hu2, hb2)
+            torch.cuda.synchronize()
+            io_bytes = N * M * 7 * 8
+            entry["e2e"] = {"value": N * M * n_e2e / (time.perf_counter() - t0),
+                            "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
+                            "d2h_bytes_per_step": io_bytes}
+            ops = ncu_fp64_per_cell("hancock3226")
+            if ops is not None:
+                pipe = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07e9
+                entry["fp64"] = {"ops_per_cell": ops, "achieved": ops * entry["value"],
+                                 "pipe_peak": pipe, "frac": ops * entry["value"] / pipe,
+                                 "ops_source": "ncu sm__inst_executed_pipe_fp64, "
+                                               "profiles/ncu_traffic.txt"}
+            peak_gbs, kind = measured_peaks()
+            ach = N * M * 7 * 16 / (ms * 1e-3) / 1e9
+            entry["hbm"] = {"achieved": ach, "peak": peak_gbs, "unit": "GB/s",
+                            "frac": ach / peak_gbs, "traffic": ncu_traffic("hancock3226"),
+                            "algorithmic_bytes_per_step": N * M * 7 * 16,
+                            "peak_source": kind}
+        out[name] = entry
+        sol.close()
+    out["fast_over_parity"] = out["fast"]["value"] / out["parity"]["value"]
+    if cpu:
+        import oracle
+        oracle.build(ref=False)
+        o = oracle.Oracle()
+        threads = os.cpu_count() or 1
+        o.set_threads(threads)
+        cfg, s, u, b = problems.hancock_wind(N, M)
+        grid = oracle.Grid(cfg.N, cfg.M, cfg.dx, cfg.dy, cfg.x0, cfg.y0, cfg.gamma, cfg.krit,
+                           physics=cfg.physics, geometry=cfg.geometry, order=cfg.order,
+                           method=cfg.method, bc=tuple(cfg.bc),
+                           frozen_radius=cfg.frozen_radius, scheme=cfg.scheme,
+                           x_max=cfg.x_max, y_max=cfg.y_max)
+        T_do = o.dt_only(grid, s, u, b)
+        t0 = time.perf_counter()
+        o.run(grid, s, u, b, cpu_steps, T_do)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": N * M * cpu_steps / dt, "unit": "cell-updates/s",
+                               "cores": threads, "kind": "port",
+                               "sample": f"{cpu_steps} full step(s) of the workload on "
+                                         f"{threads} host threads, oracle/gd_oracle.c "
+                                         f"(restatement of Kernel_GKR), {dt:.2f} s"}
+    return out
+
+
 def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
     """The oracle on all host cores, `nsteps` full steps of the workload."""
     import oracle
@@ -830,6 +920,11 @@ def run_gb300(args):
             line["io"] = measure_io(g, torch)
         except Exception as e:
             line["io"] = {"unavailable": str(e)}
+    if args.hancock:
+        try:
+            line["hancock"] = measure_hancock(g, torch, cpu=not args.no_cpu_baseline)
+        except Exception as e:
+            line["hancock"] = {"unavailable": str(e)}
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args.workload, cfg, s, u, b)
     print(json.dumps(line), flush=True)
@@ -850,9 +945,12 @@ def main():
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--adjoint", type=int, default=1)
     ap.add_argument("--io", type=int, default=1)
-    ap.add_argument("--case", default="bench", choices=["bench", "adjoint-step", "io"],
+    ap.add_argument("--hancock", type=int, default=1)
+    ap.add_argument("--case", default="bench",
+                    choices=["bench", "adjoint-step", "io", "hancock"],
                     help="adjoint-step: a short differentiation run for kernel profiles; "
-                         "io: the state-file measurement alone")
+                         "io: the state-file measurement alone; hancock: the MUSCL-Hancock "
+                         "measurement alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -866,6 +964,17 @@ def main():
         import torch
         import golikov_2d_gb300 as g
         print(json.dumps({"case": "io", "io": measure_io(g, torch)}), flush=True)
+        return 0
+    if args.case == "hancock":
+        import torch
+        import golikov_2d_gb300 as g
+        from golikov_2d_gb300 import _build
+        _build.build()
+        print(json.dumps({"case": "hancock",
+                          "hancock": measure_hancock(g, torch, steps=args.steps,
+                                                     warmup=args.warmup,
+                                                     cpu=not args.no_cpu_baseline)}),
+              flush=True)
         return 0
     return run_gb300(args)
 

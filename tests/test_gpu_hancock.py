@@ -97,11 +97,31 @@ def test_fast_step_matches_parity(cuda, scheme, N, M, xmax, ymax):
             assert np.array_equal(out[frozen], src[frozen])
 
 
+def smooth_pulse(N, M, mode, xmax=9.0, ymax=5.0):
+    """A smooth pressure / density pulse with a uniform oblique field (plasma beta ~ 3).
+
+    The run bound needs a problem whose own arithmetic is well conditioned: from a 1e-14
+    relative perturbation the reference's step (the oracle) drifts ~2e-13 on this one in
+    30 steps.  On problems.hancock_wind it drifts ~3e-5 within 5 steps, because HLLD's
+    |tt| >= 1e-5 guard (Gas_Dinamic.cu:1306-1350) switches the star field discontinuously
+    on some faces, so there fast and parity agree per step only, not over a run."""
+    cfg = problems.hancock_config(N, M, xmax, ymax, mode=mode)
+    X, Y = np.meshgrid(cfg.x0 + np.arange(N) * (xmax - cfg.x0) / (N - 1),
+                       cfg.y0 + np.arange(M) * ymax / M)
+    G = np.exp(-((X.ravel() - 5.0) ** 2 + (Y.ravel() - 2.5) ** 2) / 1.5)
+    s = np.stack([1.0 + 0.2 * G, (1.0 / cfg.gamma) * (1.0 + 0.3 * G)], 1)
+    u = np.stack([0.06 * G, -0.04 * G], 1)
+    sp4 = np.sqrt(4.0 * np.pi)
+    b = np.stack([np.full(N * M, 0.3 * sp4), 0.2 * sp4 * (1.0 + 0.1 * G),
+                  0.4 * sp4 * (1.0 + 0.2 * G)], 1)
+    return cfg, s, u, b
+
+
 def test_fast_run_matches_parity(cuda):
-    """30 steps of the wind, fast against parity, with the dt each computes itself."""
+    """30 steps, fast against parity, each with the dt it computes itself."""
     N, M = 120, 68
-    par, s, u, b = problems.hancock_wind(N, M, mode=g.MODE_PARITY)
-    fast, *_ = problems.hancock_wind(N, M, mode=g.MODE_FAST)
+    par, s, u, b = smooth_pulse(N, M, g.MODE_PARITY)
+    fast, *_ = smooth_pulse(N, M, g.MODE_FAST)
     sp, up, bp, stp = gpu_run(par, s, u, b, 30, T_do=1e-3)
     sf, uf, bf, stf = gpu_run(fast, s, u, b, 30, T_do=1e-3)
     assert stf.steps == stp.steps == 30
