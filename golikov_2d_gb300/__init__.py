@@ -35,6 +35,7 @@ SCHEME_TVD, SCHEME_HANCOCK_REF, SCHEME_HANCOCK = 0, 1, 2
 # the only setting Kernel_GKR is written for: left, right, bottom, top
 HANCOCK_BC = (BC_MIRROR_X, BC_OUTFLOW, BC_AXIS, BC_AMBIENT_KEEPB)
 MODE_FAST, MODE_PARITY = 0, 1
+DT_LAGGED, DT_CURRENT = 0, 1  # gd_set_dt_policy
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "non-finite state",
           4: "device wait timed out", 5: "unsupported combination"}
@@ -44,6 +45,7 @@ EXPORTS = (
     "gd_create", "gd_destroy", "gd_get_config", "gd_status_string", "gd_last_cuda_error",
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
+    "gd_set_dt_policy", "gd_advance_to",
     "gd_probe_fp64_peak", "gd_step_ref_static",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
@@ -90,6 +92,7 @@ class gd_stats(ctypes.Structure):
         ("t", ctypes.c_double), ("dt", ctypes.c_double), ("dt_next", ctypes.c_double),
         ("steps", ctypes.c_longlong), ("rho_floor_hits", ctypes.c_longlong),
         ("p_floor_hits", ctypes.c_longlong), ("nonfinite", ctypes.c_longlong),
+        ("t_state", ctypes.c_double),
     ]
 
 
@@ -129,6 +132,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_set_time.argtypes = [vp, d, d, vp]
     L.gd_init_dt.argtypes = [vp, vp]
     L.gd_advance.argtypes = [vp, i, i, vp]
+    L.gd_set_dt_policy.argtypes = [vp, i]
+    L.gd_advance_to.argtypes = [vp, d, ll, i, ctypes.POINTER(ll), vp]
     L.gd_get_stats.argtypes = [vp, ctypes.POINTER(gd_stats), vp]
     L.gd_field_ptr.argtypes = [vp, i, ctypes.POINTER(vp)]
     L.gd_launch_count.restype = ll
@@ -162,6 +167,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_batch_launch_count.argtypes = [vp]
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
+                 "gd_set_dt_policy", "gd_advance_to",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
@@ -293,6 +299,20 @@ class Solver:
     def advance(self, nsteps: int, use_graph: bool = False, stream=None) -> None:
         _check(self.lib.gd_advance(self.handle, int(nsteps), 1 if use_graph else 0,
                                    _stream_handle(stream)), "gd_advance")
+
+    def set_dt_policy(self, policy: int) -> None:
+        """DT_LAGGED (the reference's protocol) or DT_CURRENT (each step's own CFL dt)."""
+        _check(self.lib.gd_set_dt_policy(self.handle, int(policy)), "gd_set_dt_policy")
+
+    def advance_to(self, t_end: float, max_steps: int = 1 << 40, use_graph: bool = False,
+                   stream=None) -> int:
+        """Advance until the state's time reaches t_end (the last dt limited to land on it);
+        returns the number of steps taken."""
+        n = ctypes.c_longlong(0)
+        _check(self.lib.gd_advance_to(self.handle, float(t_end), int(max_steps),
+                                      1 if use_graph else 0, ctypes.byref(n),
+                                      _stream_handle(stream)), "gd_advance_to")
+        return int(n.value)
 
     def stats(self, stream=None, allow_nonfinite: bool = False) -> gd_stats:
         st = gd_stats()

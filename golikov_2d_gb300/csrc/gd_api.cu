@@ -120,7 +120,8 @@ cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const P
     if (P.scheme != GD_SCHEME_TVD)
         return ctx->cfg.mode == GD_MODE_PARITY
                    ? gd::launch_hancock_parity(P, in, out, T_do, T_bits, rot, ctr, dt_only, st)
-                   : gd::launch_hancock_fast(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+                   : gd::launch_hancock_fast(P, in, out, T_do, T_bits, rot, ctr, dt_only, st,
+                                             ctx->side);
     if (ctx->cfg.mode == GD_MODE_PARITY)
         return gd::launch_parity(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
     if (P.physics == GD_EULER)
@@ -181,7 +182,17 @@ gd_status gd_create(const gd_config* cfg, gd_ctx** out) {
     if (e == cudaSuccess && cfg->mode == GD_MODE_FAST) {
         if (cfg->scheme != GD_SCHEME_TVD) {
             e = gd::prepare_hancock_fast();
-            ctx->step_launches = 2;  // edge band, then the interior tiles
+            ctx->step_launches = 2;  // edge band and interior tiles
+            if (e == cudaSuccess) {
+                ctx->side = new (std::nothrow) gd::HancockStreams{nullptr, nullptr, nullptr};
+                if (!ctx->side) e = cudaErrorMemoryAllocation;
+            }
+            if (e == cudaSuccess)
+                e = cudaStreamCreateWithFlags(&ctx->side->stream, cudaStreamNonBlocking);
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&ctx->side->fork, cudaEventDisableTiming);
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&ctx->side->join, cudaEventDisableTiming);
         } else {
             e = cfg->physics == GD_EULER ? gd::prepare_euler_fast() : gd::prepare_mhd_fast();
         }
@@ -206,6 +217,12 @@ gd_status gd_destroy(gd_ctx* ctx) {
     cudaFree(ctx->aos);
     gd::adj_free(ctx);
     gd::io_free(ctx);
+    if (ctx->side) {
+        if (ctx->side->join) cudaEventDestroy(ctx->side->join);
+        if (ctx->side->fork) cudaEventDestroy(ctx->side->fork);
+        if (ctx->side->stream) cudaStreamDestroy(ctx->side->stream);
+        delete ctx->side;
+    }
     delete ctx;
     return GD_OK;
 }
@@ -323,11 +340,22 @@ gd_status gd_init_dt(gd_ctx* ctx, gd_stream stream) {
 static gd_status advance_plain(gd_ctx* ctx, int nsteps, cudaStream_t st) {
     for (int s = 0; s < nsteps; ++s) {
         const Planes in = ctx->planes(ctx->cur), out = ctx->planes(1 - ctx->cur);
+        if (ctx->dt_policy == GD_DT_CURRENT) {
+            // the CFL dt of this step's own input state (T was reset by the last rotation)
+            GD_CUDA(launch_step(ctx, ctx->P, gd_ctx::cplanes(in), out, &ctx->sc->T_do,
+                                &ctx->sc->T_bits, nullptr, nullptr, 1, st));
+            GD_CUDA(gd::launch_dt_commit(ctx->sc, st));
+            ctx->launches += 1;
+        }
         GD_CUDA(launch_step(ctx, ctx->P, gd_ctx::cplanes(in), out, &ctx->sc->T_do,
                             &ctx->sc->T_bits, ctx->sc, ctx->sc, 0, st));
         ctx->cur ^= 1;
     }
     return GD_OK;
+}
+
+static long long launches_per_step(const gd_ctx* ctx) {
+    return ctx->dt_policy == GD_DT_CURRENT ? 2LL * ctx->step_launches + 1 : ctx->step_launches;
 }
 
 gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream) {
@@ -365,8 +393,67 @@ gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream) {
         it = ctx->graphs.emplace(key, ge).first;
     }
     GD_CUDA(cudaGraphLaunch(it->second, st));
-    ctx->launches += (long long)nsteps * ctx->step_launches;
+    ctx->launches += (long long)nsteps * launches_per_step(ctx);
     if (nsteps & 1) ctx->cur ^= 1;
+    return GD_OK;
+}
+
+gd_status gd_set_dt_policy(gd_ctx* ctx, int policy) {
+    if (!ctx || (policy != GD_DT_LAGGED && policy != GD_DT_CURRENT)) return GD_ERR_INVALID_ARG;
+    if (policy != ctx->dt_policy) {
+        for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+        ctx->graphs.clear();
+        ctx->dt_policy = policy;
+    }
+    return GD_OK;
+}
+
+gd_status gd_advance_to(gd_ctx* ctx, double t_end, long long max_steps, int use_graph,
+                        long long* steps_taken, gd_stream stream) {
+    if (steps_taken) *steps_taken = 0;
+    if (!ctx || !(std::isfinite(t_end) && t_end > 0.0) || max_steps < 0)
+        return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    struct TimeView {
+        double T_do, t_state;
+    };
+    auto read_time = [&](TimeView* tv) -> gd_status {
+        Scalars h{};
+        GD_CUDA(cudaMemcpyAsync(&h, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        GD_CUDA(cudaStreamSynchronize(st));
+        tv->T_do = h.T_do;
+        tv->t_state = h.t_state;
+        return GD_OK;
+    };
+    TimeView tv{};
+    gd_status s = read_time(&tv);
+    if (s != GD_OK) return s;
+    if (!(t_end > tv.t_state)) return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::launch_set_end(ctx->sc, t_end, st));
+    ctx->launches += 1;
+    long long taken = 0;
+    // close enough: the last, limited step lands on t_end up to the rounding of the sum
+    const double tol = 1e-14 * t_end;
+    while (taken < max_steps) {
+        s = read_time(&tv);
+        if (s != GD_OK) break;
+        const double left = t_end - tv.t_state;
+        if (left <= tol || !(tv.T_do > 0.0)) break;
+        // about half of the steps the current dt needs: the dt may grow, and a step after
+        // t_end is reached would be a zero-dt step
+        const double need = left / tv.T_do;
+        long long chunk = need > 4.0 ? (long long)(0.5 * need) : 1;
+        if (chunk > max_steps - taken) chunk = max_steps - taken;
+        if (chunk > (1 << 20)) chunk = 1 << 20;
+        s = gd_advance(ctx, (int)chunk, use_graph, stream);
+        if (s != GD_OK) break;
+        taken += chunk;
+    }
+    const cudaError_t e = gd::launch_set_end(ctx->sc, 0.0, st);
+    ctx->launches += 1;
+    if (steps_taken) *steps_taken = taken;
+    if (s != GD_OK) return s;
+    if (e != cudaSuccess) return cuda_fail(e);
     return GD_OK;
 }
 
@@ -385,6 +472,7 @@ gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream) {
     out->rho_floor_hits = (long long)h.rho_floor;
     out->p_floor_hits = (long long)h.p_floor;
     out->nonfinite = (long long)h.nonfinite;
+    out->t_state = h.t_state;
     return h.nonfinite ? GD_ERR_NONPHYSICAL : GD_OK;
 }
 

@@ -360,6 +360,7 @@ gd_status gd_batch_get_stats(gd_batch* b, int grid, gd_stats* out, gd_stream str
     out->rho_floor_hits = (long long)h.rho_floor;
     out->p_floor_hits = (long long)h.p_floor;
     out->nonfinite = (long long)h.nonfinite;
+    out->t_state = h.t_state;
     return h.nonfinite ? GD_ERR_NONPHYSICAL : GD_OK;
 }
 

@@ -51,6 +51,8 @@ struct gd_ctx {
     double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
     long long launches = 0;
     int step_launches = 1;                  // kernel launches of one step (fast Hancock: 2)
+    int dt_policy = GD_DT_LAGGED;           // gd_set_dt_policy
+    gd::HancockStreams* side = nullptr;     // fast Hancock: stream + events of the band launch
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
     gd::AdjStore* adj = nullptr;            // differentiation record (gd_adj_forward)
     gd::IoScratch* io = nullptr;            // state I/O work buffers (gd_io.cu)

@@ -17,7 +17,9 @@
 //        sources, the half-step mean A = (Q + QQ)/2
 //     F  each face once: HLLD between A_L + D_L/2 and A_R - D_R/2 (gd_mhd_flux.cuh)
 //     U  the corrector of kernel.cu:3256-3281 (Pdiv = 0) from A and the four faces
-// The tile kernel runs second and performs the funk_time rotation.
+// Given a side stream, the band kernel runs on it concurrently with the tile kernel (they
+// write disjoint cells); the blocks of both share one ticket, and the last block of either to
+// finish performs the funk_time rotation.
 //
 // Differences from the parity step are rounding only: contraction, reciprocals instead of
 // divisions, slopes minmod(a - b, b - c) instead of h minmod((a - b)/h, (b - c)/h), the
@@ -40,7 +42,7 @@ constexpr int kPred = NF * PY * PX;            // one array each of A, DX, DY
 constexpr int NFX = (TX + 1) * TY, NFY = TX * (TY + 1);
 constexpr int kFx = NF * NFX, kFy = NF * NFY;
 constexpr int kUnion = kRaw > kFx + kFy ? kRaw : kFx + kFy;  // state, later the fluxes
-constexpr size_t kSmemBytes = sizeof(double) * (kUnion + 3 * kPred + 2 * PY) + TX * TY;
+constexpr size_t kSmemBytes = sizeof(double) * (kUnion + 3 * kPred + 2 * PY + TX) + TX * TY;
 
 constexpr int BNT = 128;  // band kernel
 
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
                                                           const double* __restrict__ T_do_ptr,
                                                           unsigned long long* T_bits,
                                                           Scalars* rot, Scalars* ctr,
-                                                          int dt_only) {
+                                                          int dt_only, unsigned int nblocks) {
     extern __shared__ __align__(16) double smem[];
     double* raw = smem;            // [NF][RY][RX], then fx [NF][TY][TX+1], fy [NF][TY+1][TX]
     double* fx = smem;
@@ -99,7 +101,8 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
     double* pDY = pDX + kPred;
     double* rowy = pDY + kPred;    // radius of prediction rows
     double* rowiy = rowy + PY;     // its reciprocal
-    unsigned char* flag = reinterpret_cast<unsigned char*>(rowiy + PY);  // [TY][TX]
+    double* colx = rowiy + PY;     // x of the tile's columns
+    unsigned char* flag = reinterpret_cast<unsigned char*>(colx + TX);  // [TY][TX]
 
     const int tid = threadIdx.x;
     const int N = P.N, M = P.M;
@@ -132,14 +135,16 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
         const double y = hancock_y(P, ty0 + tid - 1);
         rowy[tid] = y;
         rowiy[tid] = 1.0 / y;
+    } else if (tid >= 32 && tid < 32 + TX) {
+        colx[tid - 32] = hancock_x(P, tx0 + tid - 32);
     }
+    __syncthreads();
     // this thread's cell: 0 outside the interior, 1 interior and frozen, 2 interior, updated
     const int cx = tid % TX, cy = tid / TX;
     const int gx = tx0 + cx, gy = ty0 + cy;
     int my_flag = 0;
-    if (gx < N - 2 && gy < M - 2) my_flag = hancock_frozen(P, gx, hancock_y(P, gy)) ? 1 : 2;
+    if (gx < N - 2 && gy < M - 2) my_flag = hancock_frozen_fast(P, colx[cx], rowy[cy + 1]) ? 1 : 2;
     flag[tid] = (unsigned char)my_flag;
-    __syncthreads();
 
     // ---- P: predictions of the tile + 1 halo (not its corners) ---------------------------
     const double T_do = *T_do_ptr;
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
         if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
     }
     const bool any_active = __syncthreads_or(my_flag == 2) != 0;
-    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot);
+    block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot, nblocks);
 }
 
 // The band: rows m < 2 and m >= M-2 whole, and columns n < 2, n >= N-2 of the rows between.
@@ -359,7 +364,9 @@ template <bool VYP>
 __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in, Planes out,
                                                            const double* __restrict__ T_do_ptr,
                                                            unsigned long long* T_bits,
-                                                           Scalars* ctr, int dt_only, Band b) {
+                                                           Scalars* rot, Scalars* ctr,
+                                                           int dt_only, Band b,
+                                                           unsigned int nblocks) {
     const int i = blockIdx.x * BNT + threadIdx.x;
     double tmin = kCellTmin0;
     bool active = false;
@@ -401,24 +408,38 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
         if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
         if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
     }
-    block_tmin_and_rotate<BNT>(tmin, active, T_bits, nullptr);
+    block_tmin_and_rotate<BNT>(tmin, active, T_bits, rot, nblocks);
 }
 
 template <bool VYP>
 cudaError_t launch_v(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
                      unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
-                     cudaStream_t st) {
+                     cudaStream_t st, const HancockStreams* side) {
     const Band b = make_band(P.N, P.M);
-    hancock_band_kernel<VYP><<<(b.total + BNT - 1) / BNT, BNT, 0, st>>>(P, in, out, T_do, T_bits,
-                                                                        ctr, dt_only, b);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    // interior tiles; at least one block, which performs the rotation
+    const unsigned int band_blocks = (b.total + BNT - 1) / BNT;
+    // interior tiles: at least one block
     const int nx = P.N - 4 > 0 ? (P.N - 4 + TX - 1) / TX : 1;
     const int ny = P.M - 4 > 0 ? (P.M - 4 + TY - 1) / TY : 1;
+    const unsigned int total = band_blocks + (unsigned int)(nx * ny);
+    cudaStream_t bs = st;
+    cudaError_t e;
+    if (side != nullptr) {
+        e = cudaEventRecord(side->fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
+        if (e != cudaSuccess) return e;
+        bs = side->stream;
+    }
+    hancock_band_kernel<VYP><<<band_blocks, BNT, 0, bs>>>(P, in, out, T_do, T_bits, rot, ctr,
+                                                          dt_only, b, total);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     hancock_tile_kernel<VYP><<<dim3(nx, ny), NT, kSmemBytes, st>>>(P, in, out, T_do, T_bits, rot,
-                                                                   ctr, dt_only);
-    return cudaGetLastError();
+                                                                   ctr, dt_only, total);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || side == nullptr) return e;
+    e = cudaEventRecord(side->join, side->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, side->join, 0);
+    return e;
 }
 
 }  // namespace
@@ -435,10 +456,11 @@ cudaError_t prepare_hancock_fast() {
 
 cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes& out,
                                 const double* T_do, unsigned long long* T_bits, Scalars* rot,
-                                Scalars* ctr, int dt_only, cudaStream_t st) {
+                                Scalars* ctr, int dt_only, cudaStream_t st,
+                                const HancockStreams* side) {
     if (P.scheme == GD_SCHEME_HANCOCK_REF)
-        return launch_v<true>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
-    return launch_v<false>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+        return launch_v<true>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st, side);
+    return launch_v<false>(P, in, out, T_do, T_bits, rot, ctr, dt_only, st, side);
 }
 
 }  // namespace gd

@@ -315,10 +315,26 @@ __device__ __forceinline__ double hancock_face(const Params& P, const CPlanes& i
 __device__ __forceinline__ double hancock_y(const Params& P, int m) {
     return P.y0 + m * (P.y_max) / (P.M);
 }
-__device__ __forceinline__ bool hancock_frozen(const Params& P, int n, double y) {
-    const double x = P.x0 + n * (P.x_max - P.x0) / (P.N - 1);
+__device__ __forceinline__ double hancock_x(const Params& P, int n) {
+    return P.x0 + n * (P.x_max - P.x0) / (P.N - 1);
+}
+__device__ __forceinline__ bool hancock_frozen_xy(const Params& P, double x, double y) {
     return P.frozen_radius > 0.0 &&
            sqrt(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y))) < P.frozen_radius;
+}
+__device__ __forceinline__ bool hancock_frozen(const Params& P, int n, double y) {
+    return hancock_frozen_xy(P, hancock_x(P, n), y);
+}
+// The same decision without the square root away from the sphere: sqrt is correctly
+// rounded and monotone, so for x^2 + y^2 outside R^2 (1 -+ 1e-12) its comparison with R is
+// decided by the squares; only the thin shell in between takes the square root.
+__device__ __forceinline__ bool hancock_frozen_fast(const Params& P, double x, double y) {
+    if (!(P.frozen_radius > 0.0)) return false;
+    const double s = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+    const double R2 = P.frozen_radius * P.frozen_radius;
+    if (dlt(s, R2 * (1.0 - 1e-12))) return true;
+    if (dlt(R2 * (1.0 + 1e-12), s)) return false;
+    return sqrt(s) < P.frozen_radius;
 }
 
 // Kernel_GKR's update of the non-frozen cell (n, m) at radius y with step T_do: res gets

@@ -48,6 +48,13 @@ struct CPlanes {
 
 struct Scalars;
 
+// A side stream and the two events that fork the fast Hancock step's edge-band launch onto it
+// and join it back (null: both launches on the caller's stream, one after the other).
+struct HancockStreams {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+
 // One grid of a batch, device-resident: its parameters, its two state buffers (nf planes
 // of K doubles each), its scalars, and its tiling for the kernel variant in use.
 struct BatchGrid {
@@ -68,7 +75,20 @@ struct Scalars {
     unsigned int done;          // blocks finished in the current launch (last-block rotation)
     unsigned int pad;
     unsigned long long rho_floor, p_floor, nonfinite;
+    double t_state;  // simulated time of the current state: the sum of the dt each step used
+    double t_end;    // > 0: no step is given a dt that carries t_state past it (gd_advance_to)
+    double T_cfl;    // the last CFL dt before that limit
 };
+
+// The dt the next step will use: T, or what is left to t_end when that is set.
+__device__ __forceinline__ double clamp_to_end(const Scalars* sc, double T) {
+    if (sc->t_end > 0.0) {
+        const double rem = sc->t_end - sc->t_state;
+        const double r = rem > 0.0 ? rem : 0.0;
+        return T < r ? T : r;
+    }
+    return T;
+}
 
 // ---------------------------------------------------------------------------------------
 // Bit-pattern helpers (integer pipe).
@@ -257,7 +277,10 @@ __device__ __forceinline__ void rotate_if_last(Scalars* sc, unsigned int nblocks
     const unsigned int ticket = atomicAdd(&sc->done, 1u);
     if (ticket == nb - 1) {
         __threadfence();
-        const double T = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
+        sc->t_state = sc->t_state + sc->T_do;
+        const double Tc = from_bits((long long)atomicAdd(&sc->T_bits, 0ULL));
+        sc->T_cfl = Tc;
+        const double T = clamp_to_end(sc, Tc);
         sc->T_do = T;
         sc->TT = sc->TT + T;
         sc->T_bits = (unsigned long long)bits(kTReset);
@@ -317,10 +340,11 @@ __device__ void block_dt_and_rotate(const Params& P, double umax_x, double umax_
 
 // Block minimum of per-thread dt values (positive doubles order like their bit patterns),
 // min-combined into *T_bits when the block holds an active cell, then the funk_time
-// rotation as in block_dt_and_rotate.  Must be called by every thread of the block.
+// rotation as in block_dt_and_rotate (`nblocks` as there).  Must be called by every thread
+// of the block.
 template <int NTHREADS>
 __device__ void block_tmin_and_rotate(double tmin, bool active, unsigned long long* T_bits,
-                                      Scalars* sc) {
+                                      Scalars* sc, unsigned int nblocks = 0) {
     __shared__ unsigned long long red[NTHREADS / 32];
     __shared__ int act[NTHREADS / 32];
     unsigned long long tb = active ? (unsigned long long)bits(tmin) : ~0ULL;
@@ -343,7 +367,7 @@ __device__ void block_tmin_and_rotate(double tmin, bool active, unsigned long lo
             any |= act[w];
         }
         if (any) atomicMin(T_bits, mn);
-        if (sc != nullptr) rotate_if_last(sc, 0);
+        if (sc != nullptr) rotate_if_last(sc, nblocks);
     }
 }
 

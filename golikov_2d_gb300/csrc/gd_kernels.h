@@ -72,13 +72,15 @@ cudaError_t launch_parity(const Params& P, const CPlanes& in, const Planes& out,
 // MUSCL-Hancock step of Kernel_GKR (P.scheme GD_SCHEME_HANCOCK_REF / GD_SCHEME_HANCOCK).
 // Parity: every cell as the reference computes it (built without FMA contraction;
 // bit-identical).  Fast: face-once tiles for the cells away from the edges, the per-cell
-// evaluation for the two-cell band along the edges (two launches).
+// evaluation for the two-cell band along the edges (two launches, concurrent when a side
+// stream is given).
 cudaError_t launch_hancock_parity(const Params& P, const CPlanes& in, const Planes& out,
                                   const double* T_do, unsigned long long* T_bits, Scalars* rot,
                                   Scalars* ctr, int dt_only, cudaStream_t st);
 cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes& out,
                                 const double* T_do, unsigned long long* T_bits, Scalars* rot,
-                                Scalars* ctr, int dt_only, cudaStream_t st);
+                                Scalars* ctr, int dt_only, cudaStream_t st,
+                                const HancockStreams* side = nullptr);
 cudaError_t prepare_hancock_fast();
 
 // Utilities (gd_util.cu).
@@ -88,6 +90,7 @@ cudaError_t launch_soa_to_aos(CPlanes in, double* s, double* u, double* b, long 
                               cudaStream_t st);
 cudaError_t launch_funk_time(double* T, double* T_do, double* TT, int* i, cudaStream_t st);
 cudaError_t launch_set_time(Scalars* sc, double T_do, double TT, cudaStream_t st);
+cudaError_t launch_set_end(Scalars* sc, double t_end, cudaStream_t st);
 cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
 cudaError_t probe_fp64_peak(double* flops);

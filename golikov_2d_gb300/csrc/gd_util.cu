@@ -49,6 +49,7 @@ __global__ void funk_time_kernel(double* T, double* T_do, double* TT, int* i) {
 __device__ __forceinline__ void set_time_kernel_body(Scalars* sc, double T_do, double TT) {
     sc->T_do = T_do;
     sc->TT = TT;
+    sc->t_state = TT;
     sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
     sc->done = 0;
 }
@@ -57,11 +58,31 @@ __global__ void set_time_kernel(Scalars* sc, double T_do, double TT) {
     set_time_kernel_body(sc, T_do, TT);
 }
 
-// End of a dt-only pass: T_do <- T, T <- 1e7 (TT and the step counter unchanged).
+// End of a dt-only pass: T_do <- T (limited by t_end when set), T <- 1e7 (TT and the step
+// counter unchanged).
 __global__ void dt_commit_kernel(Scalars* sc) {
-    sc->T_do = __longlong_as_double((long long)sc->T_bits);
+    sc->T_cfl = __longlong_as_double((long long)sc->T_bits);
+    sc->T_do = clamp_to_end(sc, sc->T_cfl);
     sc->T_bits = (unsigned long long)__double_as_longlong(kTReset);
     sc->done = 0;
+}
+
+// Sets t_end and limits the pending T_do to it; t_end = 0 clears it and gives back the CFL dt
+// the limit replaced (TT follows, so that it still includes the pending dt).
+__global__ void set_end_kernel(Scalars* sc, double t_end) {
+    if (t_end > 0.0) {
+        sc->T_cfl = sc->T_do;
+        sc->t_end = t_end;
+        const double T = clamp_to_end(sc, sc->T_cfl);
+        sc->TT = sc->TT + (T - sc->T_do);
+        sc->T_do = T;
+    } else {
+        if (sc->t_end > 0.0) {
+            sc->TT = sc->TT + (sc->T_cfl - sc->T_do);
+            sc->T_do = sc->T_cfl;
+        }
+        sc->t_end = 0.0;
+    }
 }
 
 __global__ void reset_T_kernel(Scalars* sc) {
@@ -129,6 +150,11 @@ cudaError_t launch_soa_to_aos(CPlanes in, double* s, double* u, double* b, long 
 
 cudaError_t launch_funk_time(double* T, double* T_do, double* TT, int* i, cudaStream_t st) {
     funk_time_kernel<<<1, 1, 0, st>>>(T, T_do, TT, i);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_end(Scalars* sc, double t_end, cudaStream_t st) {
+    set_end_kernel<<<1, 1, 0, st>>>(sc, t_end);
     return cudaGetLastError();
 }
 

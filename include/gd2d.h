@@ -107,6 +107,10 @@ typedef struct gd_stats {
     long long rho_floor_hits;   /* cells whose density was floored (kernel.cu:1862, 2622)   */
     long long p_floor_hits;     /* cells whose pressure was floored (kernel.cu:1872, 2657)  */
     long long nonfinite;        /* cells that produced a non-finite value                   */
+    /* Added in ABI 3. */
+    double t_state;             /* time of the current state: the sum of the dt every step
+                                   used (t lags the reference's way: TT already includes the
+                                   dt of the next step, kernel.cu:1724-1725)                  */
 } gd_stats;
 
 typedef struct gd_ctx gd_ctx;
@@ -172,6 +176,24 @@ gd_status gd_init_dt(gd_ctx* ctx, gd_stream stream);
  * use_graph != 0 captures the nsteps launches in a CUDA graph on first use and replays
  * it (the graph is cached per nsteps). */
 gd_status gd_advance(gd_ctx* ctx, int nsteps, int use_graph, gd_stream stream);
+
+/* Time-step policy of gd_advance / gd_advance_to.
+ *   GD_DT_LAGGED (default): the reference's protocol -- a step uses the dt reduced during the
+ *     previous step (kernel.cu:2607-2611 + funk_time), i.e. the CFL dt of the state before.
+ *   GD_DT_CURRENT: a step uses the CFL dt of its own input state (a dt-only pass and a
+ *     commit launch before every step; ~2x the work per step).
+ * Changing the policy drops the cached graphs. */
+enum { GD_DT_LAGGED = 0, GD_DT_CURRENT = 1 };
+gd_status gd_set_dt_policy(gd_ctx* ctx, int policy);
+
+/* Advances until the time of the state (gd_stats.t_state) reaches t_end or max_steps steps
+ * were taken: each step's dt is limited to what is left to t_end, so the last step lands
+ * on it (to rounding).  Runs chunks of gd_advance (graphs when use_graph != 0) sized from
+ * the current dt, reading the time back between chunks (one synchronisation each; about
+ * log2 of the step count in all).  *steps_taken (may be NULL) receives the steps run.
+ * Afterwards t_end is cleared.  t_end must be larger than the current t_state. */
+gd_status gd_advance_to(gd_ctx* ctx, double t_end, long long max_steps, int use_graph,
+                        long long* steps_taken, gd_stream stream);
 
 /* Synchronises `stream` and reads time, dt and the floor / non-finite counters. */
 gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
