@@ -26,6 +26,11 @@ void adj_free(gd_ctx* ctx) {
     cudaFree(a->lam);
     cudaFree(a->scratch);
     cudaFree(a->tbits);
+    cudaFree(a->seg2);
+    cudaFree(a->aux2);
+    for (cudaEvent_t e : {a->ev_start, a->ev_rec[0], a->ev_rec[1], a->ev_rev[0], a->ev_rev[1]})
+        if (e) cudaEventDestroy(e);
+    if (a->side) cudaStreamDestroy(a->side);
     delete a;
     ctx->adj = nullptr;
 }
@@ -90,40 +95,55 @@ gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stre
         GD_TRY(cudaMalloc(&a->scratch,
                           sizeof(double) * (size_t)gd::adjoint_scratch_planes() * (size_t)K));
         GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
+        GD_TRY(cudaMalloc(&a->seg2, state * (every + 1)));
+        GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * 8 * (size_t)K * every));
+        GD_TRY(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&a->ev_start, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0],
+                               &a->ev_rev[1]})
+            GD_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         GD_TRY(gd::prepare_adjoint());
     }
     cudaStream_t st = (cudaStream_t)stream;
-    // The last segment is stepped out of `seg` with the update terms stored, so the backward
-    // sweep starts reversing at once instead of recomputing it.
+    // The last two segments are stepped out of the two segment buffers with the update terms
+    // stored (the last in seg/aux, the one before in seg2/aux2: the buffers the backward sweep
+    // alternates between), so the sweep starts reversing at once and recomputes two segments
+    // fewer.
     const int k_last = (a->nckpt - 1) * every;
+    const int k_prev = a->nckpt >= 2 ? k_last - every : k_last;
     a->seg_holds = -1;
+    a->seg2_holds = -1;
     for (int s = 0; s < nsteps; ++s) {
         if (s % every == 0)
             GD_TRY(cudaMemcpyAsync(a->ckpt + (size_t)(s / every) * nf * K, ctx->state[ctx->cur],
                                    state, cudaMemcpyDeviceToDevice, st));
         GD_TRY(cudaMemcpyAsync(a->dts + s, &ctx->sc->T_do, sizeof(double),
                                cudaMemcpyDeviceToDevice, st));
-        if (s < k_last) {
+        if (s < k_prev) {
             const gd_status r = gd_advance(ctx, 1, 0, stream);
             if (r != GD_OK) return r;
             continue;
         }
         // the same step as gd_advance (dt rotation and counters included), reading its input
-        // from seg[j] and writing its output to seg[j + 1]
-        const int j = s - k_last;
+        // from buffer[j] and writing its output to buffer[j + 1]
+        const bool last = s >= k_last;
+        double* seg = last ? a->seg : a->seg2;
+        double* aux = last ? a->aux : a->aux2;
+        const int j = s - (last ? k_last : k_prev);
         if (j == 0)
-            GD_TRY(cudaMemcpyAsync(a->seg, ctx->state[ctx->cur], state, cudaMemcpyDeviceToDevice,
+            GD_TRY(cudaMemcpyAsync(seg, ctx->state[ctx->cur], state, cudaMemcpyDeviceToDevice,
                                    st));
-        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
-                                       planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
+        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(seg + (size_t)j * nf * K, nf, K),
+                                       planes_at(seg + (size_t)(j + 1) * nf * K, nf, K),
                                        &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc, ctx->sc,
-                                       a->aux + (size_t)j * 8 * K, st));
+                                       aux + (size_t)j * 8 * K, st));
         ctx->launches += 1;
+        // the segment's last output is the context's state for what follows
+        if (j + 1 == (last ? nsteps - k_last : every))
+            GD_TRY(cudaMemcpyAsync(ctx->state[ctx->cur], seg + (size_t)(j + 1) * nf * K, state,
+                                   cudaMemcpyDeviceToDevice, st));
     }
-    // the final state back into the context
-    GD_TRY(cudaMemcpyAsync(ctx->state[ctx->cur], a->seg + (size_t)(nsteps - k_last) * nf * K,
-                           state, cudaMemcpyDeviceToDevice, st));
     a->seg_holds = a->nckpt - 1;
+    if (a->nckpt >= 2) a->seg2_holds = a->nckpt - 2;
     return GD_OK;
 }
 
@@ -137,36 +157,75 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
     cudaStream_t st = (cudaStream_t)stream;
     const size_t state = sizeof(double) * (size_t)nf * K;
     double* lam[2] = {a->lam, a->lam + (size_t)nf * K};
+    double* segb[2] = {a->seg, a->seg2};
+    double* auxb[2] = {a->aux, a->aux2};
     int c = 0;
     GD_TRY(gd::launch_aos_to_soa(gs, gu, gb, planes_at(lam[0], nf, K), K, nf, st));
-    for (int sg = a->nckpt - 1; sg >= 0; --sg) {
-        const int k0 = sg * a->every;
-        const int k1 = k0 + a->every < a->nsteps ? k0 + a->every : a->nsteps;
-        const int len = k1 - k0;
-        // recompute the segment (input states and update terms of every step) unless seg/aux
-        // already hold it
-        if (a->seg_holds != sg) {
-            GD_TRY(cudaMemcpyAsync(a->seg, a->ckpt + (size_t)sg * nf * K, state,
-                                   cudaMemcpyDeviceToDevice, st));
-            for (int j = 0; j < len; ++j) {
-                GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
-                                               planes_at(a->seg + (size_t)(j + 1) * nf * K, nf, K),
-                                               a->dts + k0 + j, (unsigned long long*)a->tbits,
-                                               nullptr, nullptr, a->aux + (size_t)j * 8 * K, st));
-                ctx->launches += 1;
-            }
-            a->seg_holds = sg;
+    auto seg_range = [&](int sg, int* k0, int* len) {
+        *k0 = sg * a->every;
+        const int k1 = *k0 + a->every < a->nsteps ? *k0 + a->every : a->nsteps;
+        *len = k1 - *k0;
+    };
+    // the input states and update terms of every step of segment sg, into buffer b
+    auto recompute = [&](int sg, int b, cudaStream_t s) -> gd_status {
+        int k0, len;
+        seg_range(sg, &k0, &len);
+        GD_TRY(cudaMemcpyAsync(segb[b], a->ckpt + (size_t)sg * nf * K, state,
+                               cudaMemcpyDeviceToDevice, s));
+        for (int j = 0; j < len; ++j) {
+            GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
+                                           planes_at(segb[b] + (size_t)(j + 1) * nf * K, nf, K),
+                                           a->dts + k0 + j, (unsigned long long*)a->tbits,
+                                           nullptr, nullptr, auxb[b] + (size_t)j * 8 * K, s));
+            ctx->launches += 1;
         }
-        // reverse through the segment
+        return GD_OK;
+    };
+    // Segments last to first.  While segment sg is reversed out of buffer b on `st`, segment
+    // sg - 1 is recomputed into buffer b ^ 1 on the side stream, after the reversal that last
+    // read that buffer; the reversal of sg - 1 waits for its recomputation.  Same launches and
+    // inputs as one stream, so the result is the same bit for bit.
+    int holds[2] = {a->seg_holds, a->seg2_holds};
+    const int last = a->nckpt - 1;
+    int b = holds[1] == last ? 1 : 0;
+    if (holds[b] != last) {
+        const gd_status r = recompute(last, b, st);
+        if (r != GD_OK) return r;
+        holds[b] = last;
+    }
+    GD_TRY(cudaEventRecord(a->ev_start, st));
+    GD_TRY(cudaStreamWaitEvent(a->side, a->ev_start, 0));
+    bool other_busy = false;  // buffer b ^ 1 has a recorded reversal to wait for
+    for (int sg = last; sg >= 0; --sg) {
+        bool wait_rec = false;
+        if (sg > 0 && holds[b ^ 1] != sg - 1) {
+            if (other_busy) GD_TRY(cudaStreamWaitEvent(a->side, a->ev_rev[b ^ 1], 0));
+            const gd_status r = recompute(sg - 1, b ^ 1, a->side);
+            if (r != GD_OK) return r;
+            GD_TRY(cudaEventRecord(a->ev_rec[b ^ 1], a->side));
+            holds[b ^ 1] = sg - 1;
+            wait_rec = true;
+        }
+        int k0, len;
+        seg_range(sg, &k0, &len);
         for (int j = len - 1; j >= 0; --j) {
-            GD_TRY(gd::launch_adjoint_step(P, cplanes_at(a->seg + (size_t)j * nf * K, nf, K),
-                                           a->aux + (size_t)j * 8 * K, cplanes_at(lam[c], nf, K),
+            GD_TRY(gd::launch_adjoint_step(P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
+                                           auxb[b] + (size_t)j * 8 * K, cplanes_at(lam[c], nf, K),
                                            planes_at(lam[c ^ 1], nf, K), a->scratch,
                                            a->dts + k0 + j, st));
             ctx->launches += 3;
             c ^= 1;
         }
+        if (sg > 0) {
+            GD_TRY(cudaEventRecord(a->ev_rev[b], st));
+            if (wait_rec) GD_TRY(cudaStreamWaitEvent(st, a->ev_rec[b ^ 1], 0));
+            other_busy = true;
+            b ^= 1;
+        }
     }
+    // the reversal only reads the buffers: they still hold what they were filled with
+    a->seg_holds = holds[0];
+    a->seg2_holds = holds[1];
     GD_TRY(gd::launch_soa_to_aos(cplanes_at(lam[c], nf, K), os, ou, ob, K, nf, st));
     return GD_OK;
 }

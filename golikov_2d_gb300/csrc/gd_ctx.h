@@ -21,6 +21,13 @@ struct AdjStore {
     double* scratch = nullptr;   // adjoint_scratch_planes() * K
     double* tbits = nullptr;     // dt accumulator the recompute pass writes (unused value)
     int seg_holds = -1;          // segment whose input states and update terms seg/aux hold
+    // second segment buffer: the backward sweep recomputes segment k-1 into one buffer on
+    // `side` while it reverses segment k out of the other
+    double* seg2 = nullptr;      // as seg
+    double* aux2 = nullptr;      // as aux
+    int seg2_holds = -1;         // segment seg2/aux2 hold
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
 };
 
 // Work buffers of the state I/O entry points (gd_io.cu), grown on demand.
