@@ -7,9 +7,10 @@ One step = one pass of the fused step (reconstruction + fluxes + update + CFL dt
 funk_time rotation) over the whole grid.  Metric: FP64 cell-updates/s, whole job.
 
 * value     K steps timed with CUDA events on the launching stream, state resident in HBM.
-* e2e       the same metric through the C ABI with HOST buffers: every step imports the
-            state from pinned host memory (gd_import), advances one step and exports it
-            back (gd_export); copies inside the timed region.
+* e2e       the same metric through the C ABI with HOST buffers: every step takes the state
+            from pinned host memory and returns the result to it (gd_step_host: uploads, the
+            step and downloads overlapped in bands of tile rows); copies inside the timed
+            region.
 * roofline  HBM roofline of the step kernel: algorithmic bytes per launch (each state field
             read once and written once, 8 B each) / average launch time, against the
             measured HBM bandwidth.  The step is FP64-issue bound on GB300; the "fp64"
@@ -651,16 +652,12 @@ def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792
         if mode == g.MODE_FAST:
             hs, hu, hb = (torch.from_numpy(x).pin_memory() for x in (s, u, b))
             hs2, hu2, hb2 = (torch.empty_like(x).pin_memory() for x in (hs, hu, hb))
-            sol.import_state(hs, hu, hb)
-            sol.advance(1)
-            sol.export_state(hs2, hu2, hb2)
+            sol.step_host(hs, hu, hb, hs2, hu2, hb2)
             torch.cuda.synchronize()
             n_e2e = 5
             t0 = time.perf_counter()
             for _ in range(n_e2e):
-                sol.import_state(hs, hu, hb)
-                sol.advance(1)
-                sol.export_state(hs2, hu2, hb2)
+                sol.step_host(hs, hu, hb, hs2, hu2, hb2)
             torch.cuda.synchronize()
             io_bytes = N * M * 7 * 8
             entry["e2e"] = {"value": N * M * n_e2e / (time.perf_counter() - t0),
@@ -763,6 +760,30 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def measure_e2e(g, torch, cfg, s, u, b, steps=10):
+    """gd_step_host per step from and to pinned host buffers, host clock, after one call."""
+    sol = g.Solver(cfg)
+    hs, hu = torch.from_numpy(s).pin_memory(), torch.from_numpy(u).pin_memory()
+    hb = torch.from_numpy(b).pin_memory() if b is not None else None
+    hs2, hu2 = torch.empty_like(hs).pin_memory(), torch.empty_like(hu).pin_memory()
+    hb2 = torch.empty_like(hb).pin_memory() if hb is not None else None
+    sol.import_state(hs, hu, hb)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.step_host(hs, hu, hb, hs2, hu2, hb2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sol.step_host(hs, hu, hb, hs2, hu2, hb2)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    sol.close()
+    K = cfg.N * cfg.M
+    io = K * (4 + (3 if b is not None else 0)) * 8
+    return {"value": K * steps / dt, "unit": "cell-updates/s", "h2d_bytes_per_step": io,
+            "d2h_bytes_per_step": io, "path": "gd_step_host"}
 
 
 def time_workload(name, steps, warmup, torch, g, flush_l2):
@@ -868,24 +889,24 @@ def run_gb300(args):
     hs2, hu2 = torch.empty_like(hs).pin_memory(), torch.empty_like(hu).pin_memory()
     hb2 = torch.empty_like(hb).pin_memory() if hb is not None else None
     e2e_steps = max(1, min(args.steps, 10))
-    sol.import_state(hs, hu, hb)
-    sol.advance(1)
-    sol.export_state(hs2, hu2, hb2)
+    sol.step_host(hs, hu, hb, hs2, hu2, hb2)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sol.import_state(hs, hu, hb)
-        sol.advance(1)
-        sol.export_state(hs2, hu2, hb2)  # synchronises the stream
+        # state up from pinned host memory, one step, result down: gd_step_host overlaps
+        # the two copy directions with the step band by band; returns with the result on
+        # the host
+        sol.step_host(hs, hu, hb, hs2, hu2, hb2)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s, e2e_cells = job_aggregate(e2e_s, K * e2e_steps, "cuda")
     io_bytes = K * (4 + (3 if b is not None else 0)) * 8
     e2e = {"value": e2e_cells / e2e_s, "unit": "cell-updates/s",
            "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-           "path": "gd_import(host, pinned) + gd_advance(1) + gd_export(host) per step"}
+           "path": "gd_step_host per step: host (pinned) -> device -> step -> host, bands of "
+                   "tile rows overlapping the uploads, the step and the downloads"}
     sol.close()
 
     if rank != 0:
@@ -931,7 +952,8 @@ def run_gb300(args):
                                               "traffic": ncu_traffic("ot1024")},
                                  "fp64": fp64_roofline(g, "ot1024", K2 / (ms2 * 1e-3), torch),
                                  "l2": "flushed before every timed step",
-                                 "gpu_launches": l2}
+                                 "gpu_launches": l2,
+                                 "e2e": measure_e2e(g, torch, *make_problem("ot1024"))}
         except Exception as e:  # the MHD fast path may be unavailable in this build
             line["secondary"] = {"workload": WORKLOADS["ot1024"], "unavailable": str(e)}
     if args.secondary:

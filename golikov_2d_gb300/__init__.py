@@ -45,7 +45,7 @@ EXPORTS = (
     "gd_create", "gd_destroy", "gd_get_config", "gd_status_string", "gd_last_cuda_error",
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
-    "gd_set_dt_policy", "gd_advance_to",
+    "gd_set_dt_policy", "gd_advance_to", "gd_step_host",
     "gd_probe_fp64_peak", "gd_step_ref_static",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
@@ -133,6 +133,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_init_dt.argtypes = [vp, vp]
     L.gd_advance.argtypes = [vp, i, i, vp]
     L.gd_set_dt_policy.argtypes = [vp, i]
+    L.gd_step_host.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.gd_advance_to.argtypes = [vp, d, ll, i, ctypes.POINTER(ll), vp]
     L.gd_get_stats.argtypes = [vp, ctypes.POINTER(gd_stats), vp]
     L.gd_field_ptr.argtypes = [vp, i, ctypes.POINTER(vp)]
@@ -167,7 +168,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_batch_launch_count.argtypes = [vp]
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
-                 "gd_set_dt_policy", "gd_advance_to",
+                 "gd_set_dt_policy", "gd_advance_to", "gd_step_host",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
@@ -299,6 +300,16 @@ class Solver:
     def advance(self, nsteps: int, use_graph: bool = False, stream=None) -> None:
         _check(self.lib.gd_advance(self.handle, int(nsteps), 1 if use_graph else 0,
                                    _stream_handle(stream)), "gd_advance")
+
+    def step_host(self, s, u, b, s2, u2, b2, stream=None) -> None:
+        """gd_step_host: one step from host arrays (s, u, b) into host arrays (s2, u2, b2);
+        torch CPU tensors in pinned memory take the overlapped path."""
+        host, pin = self._ptrs(s, u, b)
+        host2, pout = self._ptrs(s2, u2, b2)
+        if not (host and host2):
+            raise ValueError("step_host takes host arrays")
+        _check(self.lib.gd_step_host(self.handle, *pin, *pout, _stream_handle(stream)),
+               "gd_step_host")
 
     def set_dt_policy(self, policy: int) -> None:
         """DT_LAGGED (the reference's protocol) or DT_CURRENT (each step's own CFL dt)."""

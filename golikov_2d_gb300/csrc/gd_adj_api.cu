@@ -41,7 +41,8 @@ namespace {
 
 #define GD_TRY(call)                                          \
     do {                                                      \
-        if ((call) != cudaSuccess) return GD_ERR_CUDA;        \
+        const cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return gd::cuda_error(e_);     \
     } while (0)
 
 bool adj_supported(const gd_ctx* ctx) {

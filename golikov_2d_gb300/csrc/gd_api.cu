@@ -132,6 +132,7 @@ cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const P
 }  // namespace
 
 namespace gd {
+gd_status cuda_error(cudaError_t e) { return cuda_fail(e); }
 // Configuration checks and launch parameters for entry points that have no context.
 gd_status validate_config(const gd_config* c) { return validate(c); }
 Params params_from_config(const gd_config& c) { return make_params(c); }
@@ -217,6 +218,7 @@ gd_status gd_destroy(gd_ctx* ctx) {
     cudaFree(ctx->aos);
     gd::adj_free(ctx);
     gd::io_free(ctx);
+    gd::pipe_free(ctx);
     if (ctx->side) {
         if (ctx->side->join) cudaEventDestroy(ctx->side->join);
         if (ctx->side->fork) cudaEventDestroy(ctx->side->fork);

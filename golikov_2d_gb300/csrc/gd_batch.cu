@@ -24,7 +24,7 @@ using gd::Planes;
 using gd::Scalars;
 
 namespace {
-gd_status cuda_status(cudaError_t e) { return e == cudaSuccess ? GD_OK : GD_ERR_CUDA; }
+gd_status cuda_status(cudaError_t e) { return e == cudaSuccess ? GD_OK : gd::cuda_error(e); }
 }  // namespace
 
 #define GD_TRY(call)                                        \
@@ -184,7 +184,7 @@ gd_status gd_batch_create(const gd_config* cfgs, int ngrids, gd_batch** out) {
     }
     if (e != cudaSuccess) {
         gd_batch_destroy(b);
-        return GD_ERR_CUDA;
+        return gd::cuda_error(e);
     }
     *out = b;
     return GD_OK;
@@ -287,19 +287,20 @@ gd_status gd_batch_advance(gd_batch* b, int nsteps, int schedule, int use_graph,
         const long long l0 = b->launches;
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        gd_status s = ce == cudaSuccess ? advance_plain(b, nsteps, schedule, cap) : GD_ERR_CUDA;
+        gd_status s = ce == cudaSuccess ? advance_plain(b, nsteps, schedule, cap)
+                                        : gd::cuda_error(ce);
         if (ce == cudaSuccess) ce = cudaStreamEndCapture(cap, &g);
         b->cur = cur0;
         b->launches = l0;
         if (own) cudaStreamDestroy(cap);
         if (s != GD_OK || ce != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
-            return s != GD_OK ? s : GD_ERR_CUDA;
+            return s != GD_OK ? s : gd::cuda_error(ce);
         }
         cudaGraphExec_t ge = nullptr;
         ce = cudaGraphInstantiate(&ge, g, 0);
         cudaGraphDestroy(g);
-        if (ce != cudaSuccess) return GD_ERR_CUDA;
+        if (ce != cudaSuccess) return gd::cuda_error(ce);
         it = b->graphs.emplace(key, ge).first;
     }
     GD_TRY(cudaGraphLaunch(it->second, st));

@@ -11,6 +11,17 @@ namespace gd {
 
 // Record of a differentiated forward run (gd_adj_forward): dt sequence, checkpoints and
 // work buffers of the reverse and tangent sweeps.
+// gd_step_host: the two copy streams, the events of the band pipeline and the AoS staging
+// of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
+constexpr int kMaxBands = 16;
+struct HostPipe {
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t start = nullptr, down_done = nullptr;
+    cudaEvent_t ev_up[kMaxBands] = {}, ev_out[kMaxBands] = {};
+    double* aos_in = nullptr;
+    double* aos_out = nullptr;
+};
+
 struct AdjStore {
     int nsteps = 0, every = 0, nckpt = 0;
     double* dts = nullptr;       // nsteps
@@ -60,6 +71,7 @@ struct gd_ctx {
     int step_launches = 1;                  // kernel launches of one step (fast Hancock: 2)
     int dt_policy = GD_DT_LAGGED;           // gd_set_dt_policy
     gd::HancockStreams* side = nullptr;     // fast Hancock: stream + events of the band launch
+    gd::HostPipe* pipe = nullptr;           // gd_step_host: copy streams, events, AoS staging
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph
     gd::AdjStore* adj = nullptr;            // differentiation record (gd_adj_forward)
     gd::IoScratch* io = nullptr;            // state I/O work buffers (gd_io.cu)
@@ -86,4 +98,5 @@ struct gd_ctx {
 namespace gd {
 void adj_free(gd_ctx* ctx);
 void io_free(gd_ctx* ctx);
+void pipe_free(gd_ctx* ctx);
 }  // namespace gd

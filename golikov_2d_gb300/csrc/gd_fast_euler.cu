@@ -345,10 +345,10 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
                                                         Scalars* ctr, int dt_only) {
     extern __shared__ double smem[];
     TileResult r;
-    euler_tile<ORDER, TX, TY>(P, in, out, blockIdx.x * TX, blockIdx.y * TY, *T_do_ptr, dt_only,
-                              smem, r);
+    euler_tile<ORDER, TX, TY>(P, in, out, blockIdx.x * TX, (blockIdx.y + P.tile_row0) * TY,
+                              *T_do_ptr, dt_only, smem, r);
     add_counters(ctr, r);
-    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot);
+    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot, P.tile_nblocks);
 }
 
 // Persistent batched step: CTAs stride over the flattened (grid, tile) work list; each tile
@@ -406,7 +406,7 @@ template <int ORDER, int TX, int TY>
 cudaError_t launch_single(const Params& P, const CPlanes& in, const Planes& out,
                           const double* T_do, unsigned long long* T_bits, Scalars* rot,
                           Scalars* ctr, int dt_only, cudaStream_t st) {
-    dim3 grid((P.N + TX - 1) / TX, (P.M + TY - 1) / TY);
+    dim3 grid((P.N + TX - 1) / TX, P.tile_rows ? P.tile_rows : (P.M + TY - 1) / TY);
     euler_fast_kernel<ORDER, TX, TY><<<grid, NT, Shape<ORDER, TX, TY>::bytes, st>>>(
         P, in, out, T_do, T_bits, rot, ctr, dt_only);
     return cudaGetLastError();

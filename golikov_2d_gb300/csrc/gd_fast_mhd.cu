@@ -356,14 +356,15 @@ __global__ void __launch_bounds__(NT, 2) mhd_fast_kernel(Params P, CPlanes in, P
                                                       Scalars* ctr, int dt_only, double* aux) {
     extern __shared__ __align__(16) double smem[];
     MhdTileResult r;
-    mhd_tile<double, ORDER, TY>(P, in, out, blockIdx.x * TX, blockIdx.y * TY, *T_do_ptr, dt_only,
+    mhd_tile<double, ORDER, TY>(P, in, out, blockIdx.x * TX, (blockIdx.y + P.tile_row0) * TY,
+                                *T_do_ptr, dt_only,
                                 smem, r, aux);
     if (ctr != nullptr && (r.nfl_r | r.nfl_p | r.nbad)) {
         if (r.nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)r.nfl_r);
         if (r.nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)r.nfl_p);
         if (r.nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)r.nbad);
     }
-    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot);
+    block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot, P.tile_nblocks);
 }
 
 // Tangent of one step: (U, dU) -> (U', dU') with the dt read from *T_do_ptr (held fixed).
@@ -388,7 +389,7 @@ template <int ORDER>
 cudaError_t launch_t(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
                      unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
                      cudaStream_t st, double* aux = nullptr) {
-    dim3 grid((P.N + TX - 1) / TX, (P.M + kTY - 1) / kTY);
+    dim3 grid((P.N + TX - 1) / TX, P.tile_rows ? P.tile_rows : (P.M + kTY - 1) / kTY);
     mhd_fast_kernel<ORDER, kTY><<<grid, NT, SmemM<double, ORDER, kTY>::bytes, st>>>(
         P, in, out, T_do, T_bits, rot, ctr, dt_only, aux);
     return cudaGetLastError();
@@ -405,6 +406,8 @@ cudaError_t launch_tangent_t(const Params& P, const CPlanes& in, const CPlanes& 
 }
 
 }  // namespace
+
+int mhd_tile_height() { return kTY; }
 
 cudaError_t prepare_mhd_fast() {
     cudaError_t e = cudaFuncSetAttribute(mhd_fast_kernel<1, kTY>,

@@ -1,0 +1,245 @@
+// gd_hoststep.cu -- gd_step_host: one step of the resident loop whose state comes from host
+// memory and whose result goes back to host memory, with the transfers overlapped with the
+// step.
+//
+// The reference moves its state between host and device with blocking cudaMemcpy calls
+// around its loop (kernel.cu:4005-4010, 4093-4095, 4163-4165).  gd_import + gd_advance(1) +
+// gd_export does the same in three sequential phases.  Here the grid is cut into bands of
+// whole tile rows.  Band k's rows go up and are converted to planes on one copy stream; on
+// the caller's stream band k is stepped as soon as its neighbours' rows (the stencil's halo)
+// are there; its output is converted back and goes down on a second copy stream while later
+// bands are stepped.  The two copy directions and the SMs work at once, so a step costs
+// about the step itself plus one band of each copy.  The step is the same kernel with the
+// same arithmetic, launched once per band (Params::tile_row0 / tile_rows); the bands' blocks
+// share one dt rotation ticket, so dt, time and counters are those of gd_advance(1).
+#include <cstring>
+#include <new>
+
+#include "../../include/gd2d.h"
+#include "gd_ctx.h"
+#include "gd_internal.cuh"
+#include "gd_kernels.h"
+
+using gd::CPlanes;
+using gd::Params;
+using gd::Planes;
+
+namespace {
+
+#define HS_TRY(call)                                   \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return e_;              \
+    } while (0)
+
+bool device_visible_host(const void* p) {
+    if (p == nullptr) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory: clear the error, not visible
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+cudaError_t pipe_init(gd_ctx* ctx) {
+    if (ctx->pipe) return cudaSuccess;
+    gd::HostPipe* p = new (std::nothrow) gd::HostPipe();
+    if (!p) return cudaErrorMemoryAllocation;
+    ctx->pipe = p;
+    HS_TRY(cudaStreamCreateWithFlags(&p->up, cudaStreamNonBlocking));
+    HS_TRY(cudaStreamCreateWithFlags(&p->down, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&p->start, &p->down_done})
+        HS_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (int k = 0; k < gd::kMaxBands; ++k) {
+        HS_TRY(cudaEventCreateWithFlags(&p->ev_up[k], cudaEventDisableTiming));
+        HS_TRY(cudaEventCreateWithFlags(&p->ev_out[k], cudaEventDisableTiming));
+    }
+    HS_TRY(cudaMalloc(&p->aos_in, sizeof(double) * 7 * (size_t)ctx->K));
+    HS_TRY(cudaMalloc(&p->aos_out, sizeof(double) * 7 * (size_t)ctx->K));
+    return cudaSuccess;
+}
+
+// AoS views of rows [r0, r1): s (2 per cell), u (2), b (3), at base + {0, 2K, 4K}
+struct Rows {
+    long long c0, n;  // first cell, cells
+};
+
+cudaError_t copy_rows(double* dst_s, double* dst_u, double* dst_b, const double* src_s,
+                      const double* src_u, const double* src_b, Rows r, int nf, cudaMemcpyKind k,
+                      cudaStream_t st) {
+    HS_TRY(cudaMemcpyAsync(dst_s + 2 * r.c0, src_s + 2 * r.c0, sizeof(double) * 2 * r.n, k, st));
+    HS_TRY(cudaMemcpyAsync(dst_u + 2 * r.c0, src_u + 2 * r.c0, sizeof(double) * 2 * r.n, k, st));
+    if (nf == 7)
+        HS_TRY(cudaMemcpyAsync(dst_b + 3 * r.c0, src_b + 3 * r.c0, sizeof(double) * 3 * r.n, k,
+                               st));
+    return cudaSuccess;
+}
+
+Planes shift(Planes p, int nf, long long c0) {
+    for (int f = 0; f < nf; ++f) p.f[f] += c0;
+    return p;
+}
+CPlanes cshift(Planes p, int nf, long long c0) {
+    CPlanes c{};
+    for (int f = 0; f < nf; ++f) c.f[f] = p.f[f] + c0;
+    return c;
+}
+
+cudaError_t to_planes(gd_ctx* ctx, Rows r, cudaStream_t st) {
+    const double* a = ctx->pipe->aos_in;
+    const long long K = ctx->K;
+    ctx->launches += 1;
+    return gd::launch_aos_to_soa(a + 2 * r.c0, a + 2 * K + 2 * r.c0, a + 4 * K + 3 * r.c0,
+                                 shift(ctx->planes(ctx->cur), ctx->nf, r.c0), r.n, ctx->nf, st);
+}
+
+cudaError_t from_planes(gd_ctx* ctx, Rows r, cudaStream_t st) {
+    double* a = ctx->pipe->aos_out;
+    const long long K = ctx->K;
+    ctx->launches += 1;
+    return gd::launch_soa_to_aos(cshift(ctx->planes(1 - ctx->cur), ctx->nf, r.c0),
+                                 a + 2 * r.c0, a + 2 * K + 2 * r.c0, a + 4 * K + 3 * r.c0, r.n,
+                                 ctx->nf, st);
+}
+
+// The banded step.  Returns a CUDA error or cudaSuccess; the caller synchronises.
+cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                        double* s2, double* u2, double* b2, int TX, int TY, cudaStream_t st) {
+    gd::HostPipe* p = ctx->pipe;
+    const int N = ctx->cfg.N, M = ctx->cfg.M, nf = ctx->nf;
+    const long long K = ctx->K;
+    const int T = (M + TY - 1) / TY;                 // tile rows
+    const int nx = (N + TX - 1) / TX;                // tiles per tile row
+    // Bands run one after another on the caller's stream, so each should fill the GPU for
+    // several waves (a band's last partial wave idles SMs): at least 4 waves of the two
+    // resident CTAs per SM the fast kernels have; 2 to kMaxBands bands of >= 2 tile rows.
+    int sms = 0;
+    HS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const long long per_band_min = 4LL * 2 * (sms > 0 ? sms : 1);
+    int B = (int)(((long long)nx * T) / per_band_min);
+    if (B > gd::kMaxBands) B = gd::kMaxBands;
+    if (B > T / 2) B = T / 2;
+    if (B < 2) B = 2;
+    const int H = ctx->cfg.order == 2 ? 2 : 1;       // halo rows of the stencil
+    const bool wrap = ctx->cfg.bc[2] == GD_BC_PERIODIC;
+    auto band_tiles = [&](int k, int* t0, int* t1) {
+        *t0 = (int)((long long)k * T / B);
+        *t1 = (int)((long long)(k + 1) * T / B);
+    };
+    auto band_rows = [&](int k) {
+        int t0, t1;
+        band_tiles(k, &t0, &t1);
+        const int r0 = t0 * TY, r1 = t1 * TY < M ? t1 * TY : M;
+        return Rows{(long long)r0 * N, (long long)(r1 - r0) * N};
+    };
+    // the last band's upload leaves out the seam rows a periodic y-edge has sent first
+    auto band_rows_up = [&](int k) {
+        Rows r = band_rows(k);
+        if (wrap && k == B - 1) r.n -= (long long)H * N;
+        return r;
+    };
+    double* ai = p->aos_in;
+    double* ao = p->aos_out;
+    HS_TRY(cudaEventRecord(p->start, st));
+    HS_TRY(cudaStreamWaitEvent(p->up, p->start, 0));
+    HS_TRY(cudaStreamWaitEvent(p->down, p->start, 0));
+    // up stream: host rows to the AoS staging, then to the planes of the current state; the
+    // seam rows first, then the bands in order
+    const Rows wrap_rows{(long long)(M - H) * N, (long long)H * N};
+    if (wrap) {
+        HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, wrap_rows, nf,
+                         cudaMemcpyHostToDevice, p->up));
+        HS_TRY(to_planes(ctx, wrap_rows, p->up));
+    }
+    for (int k = 0; k < B; ++k) {
+        const Rows r = band_rows_up(k);
+        HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, r, nf, cudaMemcpyHostToDevice,
+                         p->up));
+        HS_TRY(to_planes(ctx, r, p->up));
+        HS_TRY(cudaEventRecord(p->ev_up[k], p->up));
+    }
+    // caller's stream: the step on band k once bands k and k + 1 are planes (band k - 1, and
+    // the seam rows, came before)
+    Params P = ctx->P;
+    P.tile_nblocks = (unsigned int)(nx * T);
+    const CPlanes in = gd_ctx::cplanes(ctx->planes(ctx->cur));
+    const Planes out = ctx->planes(1 - ctx->cur);
+    HS_TRY(cudaStreamWaitEvent(st, p->ev_up[0], 0));
+    for (int k = 0; k < B; ++k) {
+        if (k + 1 < B) HS_TRY(cudaStreamWaitEvent(st, p->ev_up[k + 1], 0));
+        int t0, t1;
+        band_tiles(k, &t0, &t1);
+        P.tile_row0 = t0;
+        P.tile_rows = t1 - t0;
+        ctx->launches += 1;
+        if (P.physics == GD_EULER)
+            HS_TRY(gd::launch_euler_fast(P, in, out, &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc,
+                                         ctx->sc, 0, st));
+        else
+            HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc,
+                                       ctx->sc, 0, st));
+        HS_TRY(cudaEventRecord(p->ev_out[k], st));
+        // down stream: band k's result to AoS and to the host while later bands are stepped
+        HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
+        HS_TRY(from_planes(ctx, band_rows(k), p->down));
+        HS_TRY(copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
+                         cudaMemcpyDeviceToHost, p->down));
+    }
+    HS_TRY(cudaEventRecord(p->down_done, p->down));
+    HS_TRY(cudaStreamWaitEvent(st, p->down_done, 0));
+    return cudaSuccess;
+}
+
+}  // namespace
+
+namespace gd {
+void pipe_free(gd_ctx* ctx) {
+    HostPipe* p = ctx->pipe;
+    if (!p) return;
+    cudaFree(p->aos_in);
+    cudaFree(p->aos_out);
+    for (cudaEvent_t e : {p->start, p->down_done})
+        if (e) cudaEventDestroy(e);
+    for (int k = 0; k < kMaxBands; ++k) {
+        if (p->ev_up[k]) cudaEventDestroy(p->ev_up[k]);
+        if (p->ev_out[k]) cudaEventDestroy(p->ev_out[k]);
+    }
+    if (p->up) cudaStreamDestroy(p->up);
+    if (p->down) cudaStreamDestroy(p->down);
+    delete p;
+    ctx->pipe = nullptr;
+}
+}  // namespace gd
+
+extern "C" gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                                  double* s2, double* u2, double* b2, gd_stream stream) {
+    if (!ctx || !s || !u || !s2 || !u2) return GD_ERR_INVALID_ARG;
+    if (ctx->nf == 7 && (!b || !b2)) return GD_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const gd_config& c = ctx->cfg;
+    int TX = 32, TY = 0;  // the tile shape of the launch the bands are cut for
+    if (c.physics == GD_EULER)
+        gd::euler_tile_shape(0, &TX, &TY);
+    else
+        TY = gd::mhd_tile_height();
+    // the banded pipeline: the fast TVD step with the reference's dt protocol, grids of at
+    // least four tile rows, host buffers the device can read and write (pinned)
+    const bool banded = c.mode == GD_MODE_FAST && c.scheme == GD_SCHEME_TVD &&
+                        ctx->dt_policy == GD_DT_LAGGED && (c.M + TY - 1) / TY >= 4 &&
+                        device_visible_host(s) && device_visible_host(u) &&
+                        device_visible_host(b) && device_visible_host(s2) &&
+                        device_visible_host(u2) && device_visible_host(b2);
+    if (!banded) {
+        gd_status r = gd_import(ctx, s, u, b, 1, stream);
+        if (r == GD_OK) r = gd_advance(ctx, 1, 0, stream);
+        if (r == GD_OK) r = gd_export(ctx, s2, u2, b2, 1, stream);
+        return r;
+    }
+    cudaError_t e = pipe_init(ctx);
+    if (e == cudaSuccess) e = banded_step(ctx, s, u, b, s2, u2, b2, TX, TY, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return gd::cuda_error(e);
+    ctx->cur ^= 1;
+    return GD_OK;
+}

@@ -31,6 +31,11 @@ struct Params {
     double frozen_radius;
     int scheme;           // GD_SCHEME_*
     double x_max, y_max;  // domain extents of the Hancock schemes' cell coordinates
+    // A launch of the fast step over a band of tile rows (gd_step_host): the band starts at
+    // tile row tile_row0 and has tile_rows rows (0: the whole grid); the blocks of all the
+    // band launches of one step share one rotation ticket, tile_nblocks (0: this grid's).
+    int tile_row0, tile_rows;
+    unsigned int tile_nblocks;
     // derived
     double gm1, inv_gm1;
     double ambient_p;   // 1/gamma

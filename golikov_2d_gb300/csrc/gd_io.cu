@@ -18,6 +18,7 @@
 
 #include "../../include/gd2d.h"
 #include "gd_ctx.h"
+#include "gd_kernels.h"
 #include "gd_text.cuh"
 
 namespace gd {
@@ -41,7 +42,8 @@ using gd::text::put_uint;
 
 #define IO_TRY(call)                                  \
     do {                                              \
-        if ((call) != cudaSuccess) return GD_ERR_CUDA; \
+        const cudaError_t e_ = (call);                \
+        if (e_ != cudaSuccess) return gd::cuda_error(e_); \
     } while (0)
 
 constexpr int NT = 256;
@@ -556,10 +558,11 @@ gd_status to_file(gd_ctx* ctx, const char* img, size_t n, const char* path, cuda
     if (!f) return GD_ERR_INVALID_ARG;
     for (size_t o = 0; o < n; o += kStage) {
         const size_t c = n - o < kStage ? n - o : kStage;
-        if (cudaMemcpyAsync(ctx->io->host, img + o, c, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaError_t e = cudaMemcpyAsync(ctx->io->host, img + o, c, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
             std::fclose(f);
-            return GD_ERR_CUDA;
+            return gd::cuda_error(e);
         }
         if (std::fwrite(ctx->io->host, 1, c, f) != c) {
             std::fclose(f);

@@ -21,6 +21,9 @@ cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& 
 cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& out,
                             const double* T_do, unsigned long long* T_bits, Scalars* rot,
                             Scalars* ctr, int dt_only, cudaStream_t st);
+// Rows of a tile of launch_mhd_fast (the Euler step's are euler_tile_shape(0)).  Both fast
+// launches honour Params::tile_row0 / tile_rows / tile_nblocks (a band of tile rows).
+int mhd_tile_height();
 
 // Tile-shape variants of the fast Euler kernels (0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8).
 constexpr int kEulerVariants = 4;
@@ -94,6 +97,10 @@ cudaError_t launch_set_end(Scalars* sc, double t_end, cudaStream_t st);
 cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
 cudaError_t probe_fp64_peak(double* flops);
+
+// Records e as the process's last CUDA error (gd_last_cuda_error) and returns GD_ERR_CUDA;
+// every entry point reports a failed CUDA call through it.
+gd_status cuda_error(cudaError_t e);
 
 // Configuration checks and launch parameters (gd_api.cu), shared with entry points that
 // work without a context.

@@ -43,11 +43,12 @@ gd_status scratch_for_device(int dev, void** out) {
     if (g_scratch_addr[dev] == nullptr) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess || p == nullptr) return GD_ERR_CUDA;
+        if (e != cudaSuccess) return gd::cuda_error(e);
+        if (p == nullptr) return GD_ERR_CUDA;
         e = gd::prepare_euler_fast();
         if (e == cudaSuccess) e = gd::prepare_mhd_fast();
         if (e == cudaSuccess) e = gd::prepare_hancock_fast();
-        if (e != cudaSuccess) return GD_ERR_CUDA;
+        if (e != cudaSuccess) return gd::cuda_error(e);
         g_scratch_addr[dev] = p;
     }
     *out = g_scratch_addr[dev];
@@ -77,7 +78,8 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
         P.method = method;
     }
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return GD_ERR_CUDA;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return gd::cuda_error(ce);
     if (dev < 0 || dev >= kMaxDevices) return GD_ERR_UNSUPPORTED;
     void* base = nullptr;
     const gd_status st = scratch_for_device(dev, &base);
@@ -95,8 +97,9 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
         cout.f[f] = out.f[f];
     }
     // the floor / non-finite counters start from zero at every call
-    if (cudaMemsetAsync(ctr, 0, sizeof(gd::Scalars), cs) != cudaSuccess) return GD_ERR_CUDA;
-    if (gd::launch_aos_to_soa(s, u, b, in, K, nf, cs) != cudaSuccess) return GD_ERR_CUDA;
+    ce = cudaMemsetAsync(ctr, 0, sizeof(gd::Scalars), cs);
+    if (ce == cudaSuccess) ce = gd::launch_aos_to_soa(s, u, b, in, K, nf, cs);
+    if (ce != cudaSuccess) return gd::cuda_error(ce);
     cudaError_t e;
     unsigned long long* Tb = (unsigned long long*)T;
     if (cfg->scheme != GD_SCHEME_TVD)
@@ -109,7 +112,7 @@ extern "C" gd_status gd_step_ref_static(const gd_config* cfg, const double* s, c
         e = gd::launch_euler_fast(P, cin, out, T_do, (unsigned long long*)T, nullptr, ctr, 0, cs);
     else
         e = gd::launch_mhd_fast(P, cin, out, T_do, (unsigned long long*)T, nullptr, ctr, 0, cs);
-    if (e != cudaSuccess) return GD_ERR_CUDA;
-    if (gd::launch_soa_to_aos(cout, s2, u2, b2, K, nf, cs) != cudaSuccess) return GD_ERR_CUDA;
+    if (e == cudaSuccess) e = gd::launch_soa_to_aos(cout, s2, u2, b2, K, nf, cs);
+    if (e != cudaSuccess) return gd::cuda_error(e);
     return GD_OK;
 }
