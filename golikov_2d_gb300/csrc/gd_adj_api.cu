@@ -54,6 +54,35 @@ bool adj_supported(const gd_ctx* ctx) {
            c.geometry == GD_CARTESIAN && c.mode == GD_MODE_FAST && c.frozen_radius == 0.0;
 }
 
+// (Re)allocates the recording store for nsteps steps with a checkpoint every `every`
+// steps; called only when the recording's shape changes, so a gradient loop allocates once.
+gd_status alloc_store(gd_ctx* ctx, int nsteps, int every, size_t state) {
+    const long long K = ctx->K;
+    gd::adj_free(ctx);
+    gd::AdjStore* a = new (std::nothrow) gd::AdjStore();
+    if (!a) return GD_ERR_INVALID_ARG;
+    ctx->adj = a;
+    a->nsteps = nsteps;
+    a->every = every;
+    a->nckpt = (nsteps + every - 1) / every;
+    GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
+    GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
+    GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
+    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
+    GD_TRY(cudaMalloc(&a->lam, 2 * state));
+    GD_TRY(cudaMalloc(&a->scratch,
+                      sizeof(double) * (size_t)gd::adjoint_scratch_planes() * (size_t)K));
+    GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
+    GD_TRY(cudaMalloc(&a->seg2, state * (every + 1)));
+    GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * 8 * (size_t)K * every));
+    GD_TRY(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&a->ev_start, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0],
+                           &a->ev_rev[1]})
+        GD_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    GD_TRY(gd::prepare_adjoint());
+    return GD_OK;
+}
+
 Planes planes_at(double* base, int nf, long long K) {
     Planes p{};
     for (int f = 0; f < nf; ++f) p.f[f] = base + (size_t)f * K;
@@ -79,30 +108,12 @@ gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stre
     const size_t state = sizeof(double) * (size_t)nf * K;
     gd::AdjStore* a = ctx->adj;
     if (!a || a->nsteps != nsteps || a->every != every) {
-        // (re)allocate only when the recording's shape changes; a repeated recording of the
-        // same length reuses the store, so a gradient loop allocates once
-        gd::adj_free(ctx);
-        a = new (std::nothrow) gd::AdjStore();
-        if (!a) return GD_ERR_INVALID_ARG;
-        ctx->adj = a;
-        a->nsteps = nsteps;
-        a->every = every;
-        a->nckpt = (nsteps + every - 1) / every;
-        GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
-        GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
-        GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
-        GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
-        GD_TRY(cudaMalloc(&a->lam, 2 * state));
-        GD_TRY(cudaMalloc(&a->scratch,
-                          sizeof(double) * (size_t)gd::adjoint_scratch_planes() * (size_t)K));
-        GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
-        GD_TRY(cudaMalloc(&a->seg2, state * (every + 1)));
-        GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * 8 * (size_t)K * every));
-        GD_TRY(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&a->ev_start, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0],
-                               &a->ev_rev[1]})
-            GD_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-        GD_TRY(gd::prepare_adjoint());
+        const gd_status r = alloc_store(ctx, nsteps, every, state);
+        if (r != GD_OK) {
+            gd::adj_free(ctx);  // all or nothing: the next call allocates afresh
+            return r;
+        }
+        a = ctx->adj;
     }
     cudaStream_t st = (cudaStream_t)stream;
     // The last two segments are stepped out of the two segment buffers with the update terms

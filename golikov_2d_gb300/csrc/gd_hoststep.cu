@@ -42,8 +42,7 @@ bool device_visible_host(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
-cudaError_t pipe_init(gd_ctx* ctx) {
-    if (ctx->pipe) return cudaSuccess;
+cudaError_t pipe_create(gd_ctx* ctx) {
     gd::HostPipe* p = new (std::nothrow) gd::HostPipe();
     if (!p) return cudaErrorMemoryAllocation;
     ctx->pipe = p;
@@ -58,6 +57,14 @@ cudaError_t pipe_init(gd_ctx* ctx) {
     HS_TRY(cudaMalloc(&p->aos_in, sizeof(double) * 7 * (size_t)ctx->K));
     HS_TRY(cudaMalloc(&p->aos_out, sizeof(double) * 7 * (size_t)ctx->K));
     return cudaSuccess;
+}
+
+// all or nothing: a partly created pipeline is released, so a later call starts afresh
+cudaError_t pipe_init(gd_ctx* ctx) {
+    if (ctx->pipe) return cudaSuccess;
+    const cudaError_t e = pipe_create(ctx);
+    if (e != cudaSuccess) gd::pipe_free(ctx);
+    return e;
 }
 
 // AoS views of rows [r0, r1): s (2 per cell), u (2), b (3), at base + {0, 2K, 4K}
