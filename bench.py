@@ -243,7 +243,7 @@ def measure_ot_to_end(g, torch, N=1024, t_end=0.5):
 
 
 def measure_batched(g, torch, steps, ngrids=512):
-    """BASELINE config 4: 512 independent four-quadrant Riemann problems, sides log-uniform
+    """The batched workload: 512 independent four-quadrant Riemann problems, sides log-uniform
     in [64, 512] (seeded), HLLC + minmod.  Persistent launch per step under a captured CUDA
     graph (tile shape from the autotuner) vs a loop of plain launches (one per grid)."""
     from golikov_2d_gb300 import problems

@@ -3,8 +3,8 @@
 Two libraries live here:
 
 * ``_build/libgd_oracle.so`` -- the project's C restatement of the reference step
-  (``gd_oracle.c``).  Built everywhere by ``make -C oracle``; it is the checker in the
-  tests and the timed CPU baseline in ``bench.py``.
+  (``gd_oracle.c``).  Built everywhere by ``make -C oracle``; it is the oracle the tests
+  compare against and the timed CPU baseline in ``bench.py``.
 * ``_ref/libgdref.so`` -- the reference's own ``Gas_Dinamic.cu`` / ``kernel.cu`` compiled
   for the host (``ref_build/Makefile``).  It exists only where the reference sources are
   present; tests that need it skip elsewhere.

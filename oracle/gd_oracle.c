@@ -2,7 +2,7 @@
  * gd_oracle.c -- CPU restatement of the reference's explicit finite-volume step.
  *
  * TEST INFRASTRUCTURE ONLY: the oracle.  Loaded by tests/, __graft_entry__.smoke() and
- * bench.py (CPU-baseline leg) as the checker or the timed CPU baseline, never by the product.
+ * bench.py (CPU-baseline leg) as the oracle or the timed CPU baseline, never by the product.
  *
  * Each routine restates the reference routine named beside it, keeping the reference's
  * arithmetic order (compile with -ffp-contract=off) so that results are bit-identical; the

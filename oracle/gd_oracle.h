@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA library is checked against.  Only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it, and only as
- * the checker or the timed CPU baseline; the product never calls it.
+ * the oracle or the timed CPU baseline; the product never calls it.
  *
  * Every function restates a reference routine (file:line given at each definition) with
  * the reference's arithmetic order, so that, compiled with -ffp-contract=off, it reproduces

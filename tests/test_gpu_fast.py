@@ -56,7 +56,7 @@ def test_fast_one_step_within_tolerance(cuda, oracle_lib, case):
 
 
 def test_fast_sod_200_steps(cuda, oracle_lib):
-    """BASELINE config 1: Sod 256^2, HLLC + minmod, CFL 0.4, 200 steps, transmissive."""
+    """The Sod benchmark at full size: 256^2, HLLC + minmod, CFL 0.4, 200 steps, transmissive."""
     cfg, s, u, b = problems.sod(256, 256)
     so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 200)
     sg, ug, bg, st = gpu_run(cfg, s, u, b, 200)
@@ -134,7 +134,7 @@ def test_fast_mhd_one_step_within_tolerance(cuda, oracle_lib, case):
 
 
 def test_fast_orszag_tang_nsteps(cuda, oracle_lib):
-    """BASELINE config 2 at reduced size: Orszag-Tang 128^2, HLLD, 100 steps."""
+    """The Orszag-Tang benchmark at reduced size: 128^2, HLLD, 100 steps."""
     cfg, s, u, b = problems.orszag_tang(128, 128)
     so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 100)
     sg, ug, bg, st = gpu_run(cfg, s, u, b, 100)
