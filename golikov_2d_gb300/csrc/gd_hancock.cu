@@ -18,7 +18,7 @@ __global__ void __launch_bounds__(HNT) hancock_parity_kernel(Params P, CPlanes i
                                                              Scalars* rot, Scalars* ctr,
                                                              int dt_only) {
     const int n = blockIdx.x * HTX + (threadIdx.x % HTX);
-    const int m = blockIdx.y * HTY + (threadIdx.x / HTX);
+    const int m = (blockIdx.y + P.tile_row0) * HTY + (threadIdx.x / HTX);
     double tmin = kCellTmin0;
     bool active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(HNT) hancock_parity_kernel(Params P, CPlanes i
         if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
         if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
     }
-    block_tmin_and_rotate<HNT>(tmin, active, T_bits, rot);
+    block_tmin_and_rotate<HNT>(tmin, active, T_bits, rot, P.tile_nblocks);
 }
 
 }  // namespace
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(HNT) hancock_parity_kernel(Params P, CPlanes i
 cudaError_t launch_hancock_parity(const Params& P, const CPlanes& in, const Planes& out,
                                   const double* T_do, unsigned long long* T_bits, Scalars* rot,
                                   Scalars* ctr, int dt_only, cudaStream_t st) {
-    const dim3 grid((P.N + HTX - 1) / HTX, (P.M + HTY - 1) / HTY);
+    const dim3 grid((P.N + HTX - 1) / HTX, P.tile_rows ? P.tile_rows : (P.M + HTY - 1) / HTY);
     if (P.scheme == GD_SCHEME_HANCOCK_REF)
         hancock_parity_kernel<true><<<grid, HNT, 0, st>>>(P, in, out, T_do, T_bits, rot, ctr,
                                                            dt_only);

@@ -128,7 +128,9 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     if (B > gd::kMaxBands) B = gd::kMaxBands;
     if (B > T / 2) B = T / 2;
     if (B < 2) B = 2;
-    const int H = ctx->cfg.order == 2 ? 2 : 1;       // halo rows of the stencil
+    // halo rows of the stencil: two for minmod TVD and for the Hancock step (whatever its
+    // `order`), one at first order
+    const int H = (ctx->cfg.order == 2 || ctx->cfg.scheme != GD_SCHEME_TVD) ? 2 : 1;
     const bool wrap = ctx->cfg.bc[2] == GD_BC_PERIODIC;
     auto band_tiles = [&](int k, int* t0, int* t1) {
         *t0 = (int)((long long)k * T / B);
@@ -180,12 +182,18 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         P.tile_row0 = t0;
         P.tile_rows = t1 - t0;
         ctx->launches += 1;
-        if (P.physics == GD_EULER)
-            HS_TRY(gd::launch_euler_fast(P, in, out, &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc,
-                                         ctx->sc, 0, st));
+        unsigned long long* Tb = &ctx->sc->T_bits;
+        if (ctx->cfg.mode == GD_MODE_PARITY)
+            HS_TRY(P.scheme != GD_SCHEME_TVD
+                       ? gd::launch_hancock_parity(P, in, out, &ctx->sc->T_do, Tb, ctx->sc,
+                                                   ctx->sc, 0, st)
+                       : gd::launch_parity(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0,
+                                           st));
+        else if (P.physics == GD_EULER)
+            HS_TRY(gd::launch_euler_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0,
+                                         st));
         else
-            HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc,
-                                       ctx->sc, 0, st));
+            HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0, st));
         HS_TRY(cudaEventRecord(p->ev_out[k], st));
         // down stream: band k's result to AoS and to the host while later bands are stepped
         HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
@@ -225,15 +233,19 @@ extern "C" gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u,
     if (ctx->nf == 7 && (!b || !b2)) return GD_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     const gd_config& c = ctx->cfg;
-    int TX = 32, TY = 0;  // the tile shape of the launch the bands are cut for
-    if (c.physics == GD_EULER)
+    int TX = 32, TY = 0;  // the block shape of the launch the bands are cut for
+    if (c.mode == GD_MODE_PARITY)
+        TY = gd::kParityBlockRows;
+    else if (c.physics == GD_EULER)
         gd::euler_tile_shape(0, &TX, &TY);
     else
         TY = gd::mhd_tile_height();
-    // the banded pipeline: the fast TVD step with the reference's dt protocol, grids of at
-    // least four tile rows, host buffers the device can read and write (pinned)
-    const bool banded = c.mode == GD_MODE_FAST && c.scheme == GD_SCHEME_TVD &&
-                        ctx->dt_policy == GD_DT_LAGGED && (c.M + TY - 1) / TY >= 4 &&
+    // the banded pipeline: a step that is one launch over tiles or per-cell blocks (the fast
+    // TVD step, either parity step; not the fast Hancock step's two launches), the reference's
+    // dt protocol, grids of at least four block rows, host buffers the device can read and
+    // write (pinned)
+    const bool one_launch = c.mode == GD_MODE_PARITY || c.scheme == GD_SCHEME_TVD;
+    const bool banded = one_launch && ctx->dt_policy == GD_DT_LAGGED && (c.M + TY - 1) / TY >= 4 &&
                         device_visible_host(s) && device_visible_host(u) &&
                         device_visible_host(b) && device_visible_host(s2) &&
                         device_visible_host(u2) && device_visible_host(b2);

@@ -24,6 +24,9 @@ cudaError_t launch_mhd_fast(const Params& P, const CPlanes& in, const Planes& ou
 // Rows of a tile of launch_mhd_fast (the Euler step's are euler_tile_shape(0)).  Both fast
 // launches honour Params::tile_row0 / tile_rows / tile_nblocks (a band of tile rows).
 int mhd_tile_height();
+// Rows of the blocks of the per-cell parity kernels (launch_parity, launch_hancock_parity),
+// which honour the same band parameters; their blocks are 32 cells wide.
+constexpr int kParityBlockRows = 4;
 
 // Tile-shape variants of the fast Euler kernels (0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8).
 constexpr int kEulerVariants = 4;

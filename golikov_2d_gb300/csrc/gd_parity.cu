@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(PNT) parity_kernel(Params P, CPlanes in, Plane
                                                      unsigned long long* T_bits, Scalars* rot,
                                                      Scalars* ctr, int dt_only) {
     const int n = blockIdx.x * PTX + (threadIdx.x % PTX);
-    const int mm = blockIdx.y * PTY + (threadIdx.x / PTX);
+    const int mm = (blockIdx.y + P.tile_row0) * PTY + (threadIdx.x / PTX);
     const bool inside = n < P.N && mm < P.M;
     double tmin = kCellTmin0;
     bool active = false;
@@ -210,14 +210,14 @@ __global__ void __launch_bounds__(PNT) parity_kernel(Params P, CPlanes in, Plane
         if (nfl_p) atomicAdd(&ctr->p_floor, (unsigned long long)nfl_p);
         if (nbad) atomicAdd(&ctr->nonfinite, (unsigned long long)nbad);
     }
-    block_tmin_and_rotate<PNT>(tmin, active, T_bits, rot);
+    block_tmin_and_rotate<PNT>(tmin, active, T_bits, rot, P.tile_nblocks);
 }
 
 template <int NF, int ORDER>
 cudaError_t launch_t(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
                      unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
                      cudaStream_t st) {
-    dim3 grid((P.N + PTX - 1) / PTX, (P.M + PTY - 1) / PTY);
+    dim3 grid((P.N + PTX - 1) / PTX, P.tile_rows ? P.tile_rows : (P.M + PTY - 1) / PTY);
     parity_kernel<NF, ORDER><<<grid, PNT, 0, st>>>(P, in, out, T_do, T_bits, rot, ctr, dt_only);
     return cudaGetLastError();
 }

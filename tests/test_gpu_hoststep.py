@@ -1,7 +1,8 @@
 """gd_step_host: a step from host memory to host memory with the transfers overlapped (bands
-of tile rows on two copy streams) equals gd_import + gd_advance(1) + gd_export bit for bit,
-on periodic, transmissive and the reference's native boundaries, over several steps, and
-through the sequential path for pageable buffers and small grids."""
+of block rows on two copy streams) equals gd_import + gd_advance(1) + gd_export bit for bit,
+on periodic, transmissive and the reference's native boundaries, in fast and parity modes
+(the Hancock scheme's too), over several steps, and through the sequential path for pageable
+buffers, small grids and the fast Hancock step."""
 import numpy as np
 import pytest
 
@@ -16,6 +17,11 @@ CASES = {
     "ot256_mhd_periodic": lambda: problems.orszag_tang(256, 256),
     "wind_native": lambda: problems.stellar_wind(200, 136, 2.25, 1.25),
     "small_grid": lambda: problems.sod(40, 24),
+    "sod256_parity": lambda: problems.sod(256, 256, mode=g.MODE_PARITY),
+    "wind_native_parity": lambda: problems.stellar_wind(200, 136, 2.25, 1.25,
+                                                        mode=g.MODE_PARITY),
+    "hancock_parity": lambda: problems.hancock_wind(160, 96, mode=g.MODE_PARITY),
+    "hancock_fast": lambda: problems.hancock_wind(160, 96),
 }
 
 
