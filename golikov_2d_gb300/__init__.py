@@ -45,7 +45,7 @@ EXPORTS = (
     "gd_create", "gd_destroy", "gd_get_config", "gd_status_string", "gd_last_cuda_error",
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
-    "gd_set_dt_policy", "gd_advance_to", "gd_step_host",
+    "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
     "gd_probe_fp64_peak", "gd_step_ref_static",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
@@ -133,6 +133,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_init_dt.argtypes = [vp, vp]
     L.gd_advance.argtypes = [vp, i, i, vp]
     L.gd_set_dt_policy.argtypes = [vp, i]
+    L.gd_set_floor_limit.argtypes = [vp, ll]
     L.gd_step_host.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.gd_advance_to.argtypes = [vp, d, ll, i, ctypes.POINTER(ll), vp]
     L.gd_get_stats.argtypes = [vp, ctypes.POINTER(gd_stats), vp]
@@ -168,7 +169,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_batch_launch_count.argtypes = [vp]
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
-                 "gd_set_dt_policy", "gd_advance_to", "gd_step_host",
+                 "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
@@ -310,6 +311,11 @@ class Solver:
             raise ValueError("step_host takes host arrays")
         _check(self.lib.gd_step_host(self.handle, *pin, *pout, _stream_handle(stream)),
                "gd_step_host")
+
+    def set_floor_limit(self, max_floor_hits: int) -> None:
+        """stats() reports GD_ERR_NONPHYSICAL once floor hits exceed this (0: no limit)."""
+        _check(self.lib.gd_set_floor_limit(self.handle, int(max_floor_hits)),
+               "gd_set_floor_limit")
 
     def set_dt_policy(self, policy: int) -> None:
         """DT_LAGGED (the reference's protocol) or DT_CURRENT (each step's own CFL dt)."""

@@ -475,7 +475,15 @@ gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream) {
     out->p_floor_hits = (long long)h.p_floor;
     out->nonfinite = (long long)h.nonfinite;
     out->t_state = h.t_state;
-    return h.nonfinite ? GD_ERR_NONPHYSICAL : GD_OK;
+    const bool floors = ctx->floor_limit > 0 &&
+                        out->rho_floor_hits + out->p_floor_hits > ctx->floor_limit;
+    return (h.nonfinite || floors) ? GD_ERR_NONPHYSICAL : GD_OK;
+}
+
+gd_status gd_set_floor_limit(gd_ctx* ctx, long long max_floor_hits) {
+    if (!ctx || max_floor_hits < 0) return GD_ERR_INVALID_ARG;
+    ctx->floor_limit = max_floor_hits;
+    return GD_OK;
 }
 
 gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out) {

@@ -70,6 +70,7 @@ struct gd_ctx {
     long long launches = 0;
     int step_launches = 1;                  // kernel launches of one step (fast Hancock: 2)
     int dt_policy = GD_DT_LAGGED;           // gd_set_dt_policy
+    long long floor_limit = 0;              // gd_set_floor_limit (0: none)
     gd::HancockStreams* side = nullptr;     // fast Hancock: stream + events of the band launch
     gd::HostPipe* pipe = nullptr;           // gd_step_host: copy streams, events, AoS staging
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, cur) -> graph

@@ -206,6 +206,12 @@ gd_status gd_advance_to(gd_ctx* ctx, double t_end, long long max_steps, int use_
 gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u, const double* b,
                        double* s2, double* u2, double* b2, gd_stream stream);
 
+/* A limit on the floor hits (density and pressure floors together, gd_stats
+ * rho_floor_hits + p_floor_hits, counted since gd_create): when it is exceeded,
+ * gd_get_stats returns GD_ERR_NONPHYSICAL, as it does for non-finite cells.  0 (the
+ * default) sets no limit. */
+gd_status gd_set_floor_limit(gd_ctx* ctx, long long max_floor_hits);
+
 /* Synchronises `stream` and reads time, dt and the floor / non-finite counters. */
 gd_status gd_get_stats(gd_ctx* ctx, gd_stats* out, gd_stream stream);
 

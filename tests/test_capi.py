@@ -111,6 +111,7 @@ def test_null_arguments_rejected(gdlib):
     assert gdlib.gd_create(None, None) == 1
     assert gdlib.gd_advance(None, 1, 0, None) == 1
     assert gdlib.gd_set_dt_policy(None, 0) == 1
+    assert gdlib.gd_set_floor_limit(None, 0) == 1
     assert gdlib.gd_advance_to(None, 1.0, 10, 0, None, None) == 1
     assert gdlib.gd_step_ref(None, None, None, None, None, None, None, None, None, 0, 0, None) == 1
     assert gdlib.gd_probe_fp64_peak(None) == 1

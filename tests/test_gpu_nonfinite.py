@@ -19,6 +19,35 @@ CASES = {
 }
 
 
+def test_floor_limit(cuda):
+    """Two streams moving apart at Mach ~1e6 open a vacuum: the pressure floor
+    (p <= 0 -> 1e-6) is hit; a limit below the hits turns gd_get_stats into
+    GD_ERR_NONPHYSICAL, no limit (0) does not."""
+    cfg, s, u, b = problems.sod(64, 16)
+    s = s.copy()
+    u = u.copy()
+    s[:, 0], s[:, 1] = 1.0, 1e-12
+    x = np.tile(np.arange(cfg.N), cfg.M)
+    u[:, 0] = np.where(x < cfg.N // 2, -1.0, 1.0)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(1e-3, 0.0)
+    sol.advance(2)
+    st = sol.stats()  # no limit: floors are counted, not an error
+    hits = st.rho_floor_hits + st.p_floor_hits
+    assert hits > 0 and st.nonfinite == 0
+    sol.set_floor_limit(hits)
+    sol.stats()  # at the limit
+    sol.set_floor_limit(hits - 1 if hits > 1 else 1)
+    if hits > 1:
+        with pytest.raises(g.GdError) as e:
+            sol.stats()
+        assert e.value.status == 3
+    with pytest.raises(g.GdError):
+        sol.set_floor_limit(-1)
+    sol.close()
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_nan_in_the_state_is_reported(cuda, case):
     cfg, s, u, b = CASES[case]()
