@@ -963,7 +963,7 @@ def run_gb300(args):
             line["ot_to_t05"] = {"unavailable": str(e)}
     if args.batched:
         try:
-            line["batched"] = measure_batched(g, torch, min(args.steps, 100))
+            line["batched"] = measure_batched(g, torch, 100)  # the workload's 100 steps
         except Exception as e:
             line["batched"] = {"unavailable": str(e)}
     if args.adjoint:
