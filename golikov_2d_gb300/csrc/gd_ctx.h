@@ -13,10 +13,10 @@ namespace gd {
 // work buffers of the reverse and tangent sweeps.
 // gd_step_host: the two copy streams, the events of the band pipeline and the AoS staging
 // of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
-constexpr int kMaxBands = 16;
+constexpr int kMaxBands = 32;
 struct HostPipe {
-    cudaStream_t up = nullptr, down = nullptr;
-    cudaEvent_t start = nullptr, down_done = nullptr;
+    cudaStream_t up = nullptr, down = nullptr, comp = nullptr;
+    cudaEvent_t start = nullptr, down_done = nullptr, comp_done = nullptr;
     cudaEvent_t ev_up[kMaxBands] = {}, ev_out[kMaxBands] = {};
     double* aos_in = nullptr;
     double* aos_out = nullptr;

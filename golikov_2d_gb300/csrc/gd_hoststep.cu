@@ -48,7 +48,8 @@ cudaError_t pipe_create(gd_ctx* ctx) {
     ctx->pipe = p;
     HS_TRY(cudaStreamCreateWithFlags(&p->up, cudaStreamNonBlocking));
     HS_TRY(cudaStreamCreateWithFlags(&p->down, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&p->start, &p->down_done})
+    HS_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done})
         HS_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int k = 0; k < gd::kMaxBands; ++k) {
         HS_TRY(cudaEventCreateWithFlags(&p->ev_up[k], cudaEventDisableTiming));
@@ -118,12 +119,13 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     const long long K = ctx->K;
     const int T = (M + TY - 1) / TY;                 // tile rows
     const int nx = (N + TX - 1) / TX;                // tiles per tile row
-    // Bands run one after another on the caller's stream, so each should fill the GPU for
-    // several waves (a band's last partial wave idles SMs): at least 4 waves of the two
-    // resident CTAs per SM the fast kernels have; 2 to kMaxBands bands of >= 2 tile rows.
+    // Smaller bands shorten the pipeline's fill (two bands up before the first step) and
+    // drain (one band down after the last); each band should still fill the GPU for a few
+    // waves: at least 2 waves of the two resident CTAs per SM the kernels have; 2 to
+    // kMaxBands bands of >= 2 block rows.
     int sms = 0;
     HS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    const long long per_band_min = 4LL * 2 * (sms > 0 ? sms : 1);
+    const long long per_band_min = 2LL * 2 * (sms > 0 ? sms : 1);
     int B = (int)(((long long)nx * T) / per_band_min);
     if (B > gd::kMaxBands) B = gd::kMaxBands;
     if (B > T / 2) B = T / 2;
@@ -168,15 +170,17 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         HS_TRY(to_planes(ctx, r, p->up));
         HS_TRY(cudaEventRecord(p->ev_up[k], p->up));
     }
-    // caller's stream: the step on band k once bands k and k + 1 are planes (band k - 1, and
-    // the seam rows, came before)
+    // the step on band k once bands k and k + 1 are planes (band k - 1, and the seam rows,
+    // came before), bands alternating between the caller's stream and a second compute
+    // stream: the bands write disjoint rows and share one rotation ticket, so the next band's
+    // blocks may start while the last wave of this one drains
     Params P = ctx->P;
     P.tile_nblocks = (unsigned int)(nx * T);
     const CPlanes in = gd_ctx::cplanes(ctx->planes(ctx->cur));
     const Planes out = ctx->planes(1 - ctx->cur);
-    HS_TRY(cudaStreamWaitEvent(st, p->ev_up[0], 0));
     for (int k = 0; k < B; ++k) {
-        if (k + 1 < B) HS_TRY(cudaStreamWaitEvent(st, p->ev_up[k + 1], 0));
+        const cudaStream_t cs = (k & 1) ? p->comp : st;
+        HS_TRY(cudaStreamWaitEvent(cs, p->ev_up[k + 1 < B ? k + 1 : k], 0));
         int t0, t1;
         band_tiles(k, &t0, &t1);
         P.tile_row0 = t0;
@@ -186,21 +190,23 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         if (ctx->cfg.mode == GD_MODE_PARITY)
             HS_TRY(P.scheme != GD_SCHEME_TVD
                        ? gd::launch_hancock_parity(P, in, out, &ctx->sc->T_do, Tb, ctx->sc,
-                                                   ctx->sc, 0, st)
+                                                   ctx->sc, 0, cs)
                        : gd::launch_parity(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0,
-                                           st));
+                                           cs));
         else if (P.physics == GD_EULER)
             HS_TRY(gd::launch_euler_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0,
-                                         st));
+                                         cs));
         else
-            HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0, st));
-        HS_TRY(cudaEventRecord(p->ev_out[k], st));
+            HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0, cs));
+        HS_TRY(cudaEventRecord(p->ev_out[k], cs));
         // down stream: band k's result to AoS and to the host while later bands are stepped
         HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
         HS_TRY(from_planes(ctx, band_rows(k), p->down));
         HS_TRY(copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
                          cudaMemcpyDeviceToHost, p->down));
     }
+    HS_TRY(cudaEventRecord(p->comp_done, p->comp));
+    HS_TRY(cudaStreamWaitEvent(st, p->comp_done, 0));
     HS_TRY(cudaEventRecord(p->down_done, p->down));
     HS_TRY(cudaStreamWaitEvent(st, p->down_done, 0));
     return cudaSuccess;
@@ -214,7 +220,7 @@ void pipe_free(gd_ctx* ctx) {
     if (!p) return;
     cudaFree(p->aos_in);
     cudaFree(p->aos_out);
-    for (cudaEvent_t e : {p->start, p->down_done})
+    for (cudaEvent_t e : {p->start, p->down_done, p->comp_done})
         if (e) cudaEventDestroy(e);
     for (int k = 0; k < kMaxBands; ++k) {
         if (p->ev_up[k]) cudaEventDestroy(p->ev_up[k]);
@@ -222,6 +228,7 @@ void pipe_free(gd_ctx* ctx) {
     }
     if (p->up) cudaStreamDestroy(p->up);
     if (p->down) cudaStreamDestroy(p->down);
+    if (p->comp) cudaStreamDestroy(p->comp);
     delete p;
     ctx->pipe = nullptr;
 }
