@@ -15,8 +15,8 @@ namespace gd {
 // of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
 constexpr int kMaxBands = 32;
 struct HostPipe {
-    cudaStream_t up = nullptr, down = nullptr, comp = nullptr;
-    cudaEvent_t start = nullptr, down_done = nullptr, comp_done = nullptr;
+    cudaStream_t up = nullptr, down = nullptr, comp = nullptr, edge = nullptr;
+    cudaEvent_t start = nullptr, down_done = nullptr, comp_done = nullptr, edge_done = nullptr;
     cudaEvent_t ev_up[kMaxBands] = {}, ev_out[kMaxBands] = {};
     double* aos_in = nullptr;
     double* aos_out = nullptr;

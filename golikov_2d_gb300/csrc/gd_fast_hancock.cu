@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
 
     const int tid = threadIdx.x;
     const int N = P.N, M = P.M;
-    const int tx0 = 2 + blockIdx.x * TX, ty0 = 2 + blockIdx.y * TY;
+    const int tx0 = 2 + blockIdx.x * TX, ty0 = 2 + (blockIdx.y + P.tile_row0) * TY;
     const double ig = P.inv_gm1;
 
     // ---- L: state of the tile + 2 halo; corner blocks the stencils never reach are skipped
@@ -341,22 +341,32 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
     block_dt_and_rotate<NT>(P, umax_x, umax_y, any_active, T_bits, rot, nblocks);
 }
 
-// The band: rows m < 2 and m >= M-2 whole, and columns n < 2, n >= N-2 of the rows between.
+// The edge cells of rows [r0, r1): rows m < 2 and m >= M-2 whole, and the columns n < 2 and
+// n >= N-2 of the rows between.
 struct Band {
-    int rows_lo, rows_hi0, cols_lo, cols_hi0, nrows, ncols, mid0, nmid, total;
+    int lo0, nlo;    // whole rows [lo0, lo0 + nlo) at the bottom
+    int hi0, nhi;    // whole rows [hi0, hi0 + nhi) at the top
+    int mid0, nmid;  // rows [mid0, mid0 + nmid) between, their edge columns only
+    int cols_lo, cols_hi0, ncols;
+    int total;
 };
 
-Band make_band(int N, int M) {
+int clamp_count(int a, int b) { return b > a ? b - a : 0; }
+
+Band make_band(int N, int M, int r0, int r1) {
     Band b;
-    b.rows_lo = M < 2 ? M : 2;              // rows [0, rows_lo)
-    b.rows_hi0 = M - 2 > 2 ? M - 2 : 2;     // rows [rows_hi0, M)
-    b.nrows = b.rows_lo + (M - b.rows_hi0);
+    const int bot = M < 2 ? M : 2;           // rows [0, bot) are whole
+    const int top = M - 2 > 2 ? M - 2 : 2;   // rows [top, M) are whole
+    b.lo0 = r0;
+    b.nlo = clamp_count(r0, r1 < bot ? r1 : bot);
+    b.hi0 = r0 > top ? r0 : top;
+    b.nhi = clamp_count(b.hi0, r1 < M ? r1 : M);
+    b.mid0 = r0 > bot ? r0 : bot;
+    b.nmid = clamp_count(b.mid0, r1 < top ? r1 : top);
     b.cols_lo = N < 2 ? N : 2;
     b.cols_hi0 = N - 2 > 2 ? N - 2 : 2;
     b.ncols = b.cols_lo + (N - b.cols_hi0);
-    b.mid0 = 2;
-    b.nmid = M - 4 > 0 ? M - 4 : 0;          // rows [2, M-2)
-    b.total = b.nrows * N + b.nmid * b.ncols;
+    b.total = (b.nlo + b.nhi) * N + b.nmid * b.ncols;
     return b;
 }
 
@@ -373,12 +383,12 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
     if (i < b.total) {
         int n, m;
-        if (i < b.nrows * P.N) {
+        if (i < (b.nlo + b.nhi) * P.N) {
             const int r = i / P.N;
             n = i - r * P.N;
-            m = r < b.rows_lo ? r : b.rows_hi0 + (r - b.rows_lo);
+            m = r < b.nlo ? b.lo0 + r : b.hi0 + (r - b.nlo);
         } else {
-            const int j = i - b.nrows * P.N;
+            const int j = i - (b.nlo + b.nhi) * P.N;
             const int r = j / b.ncols, c = j - r * b.ncols;
             m = b.mid0 + r;
             n = c < b.cols_lo ? c : b.cols_hi0 + (c - b.cols_lo);
@@ -411,15 +421,42 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
     block_tmin_and_rotate<BNT>(tmin, active, T_bits, rot, nblocks);
 }
 
+// Interior tile rows (at least one launch row, so a step always has a tile block) and the
+// tile rows [t0, t1) of the rows [r0, r1), whose ends are 0, M or 2 + a multiple of TY.
+int tile_rows_all(const Params& P) { return P.M - 4 > 0 ? (P.M - 4 + TY - 1) / TY : 1; }
+void tile_range(const Params& P, int r0, int r1, int* t0, int* t1) {
+    *t0 = r0 <= 2 ? 0 : (r0 - 2) / TY;
+    *t1 = r1 >= P.M ? tile_rows_all(P) : (r1 - 2) / TY;
+}
+int tile_cols(const Params& P) { return P.N - 4 > 0 ? (P.N - 4 + TX - 1) / TX : 1; }
+
+template <bool VYP>
+cudaError_t launch_rows(const Params& P0, const CPlanes& in, const Planes& out,
+                        const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                        Scalars* ctr, int r0, int r1, unsigned int nblocks, int parts,
+                        cudaStream_t st) {
+    const Band b = make_band(P0.N, P0.M, r0, r1);
+    int t0, t1;
+    tile_range(P0, r0, r1, &t0, &t1);
+    Params P = P0;
+    P.tile_row0 = t0;
+    if ((parts & 1) && b.total > 0)
+        hancock_band_kernel<VYP><<<(b.total + BNT - 1) / BNT, BNT, 0, st>>>(
+            P, in, out, T_do, T_bits, rot, ctr, 0, b, nblocks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !(parts & 2) || t1 <= t0) return e;
+    hancock_tile_kernel<VYP><<<dim3(tile_cols(P), t1 - t0), NT, kSmemBytes, st>>>(
+        P, in, out, T_do, T_bits, rot, ctr, 0, nblocks);
+    return cudaGetLastError();
+}
+
 template <bool VYP>
 cudaError_t launch_v(const Params& P, const CPlanes& in, const Planes& out, const double* T_do,
                      unsigned long long* T_bits, Scalars* rot, Scalars* ctr, int dt_only,
                      cudaStream_t st, const HancockStreams* side) {
-    const Band b = make_band(P.N, P.M);
+    const Band b = make_band(P.N, P.M, 0, P.M);
     const unsigned int band_blocks = (b.total + BNT - 1) / BNT;
-    // interior tiles: at least one block
-    const int nx = P.N - 4 > 0 ? (P.N - 4 + TX - 1) / TX : 1;
-    const int ny = P.M - 4 > 0 ? (P.M - 4 + TY - 1) / TY : 1;
+    const int nx = tile_cols(P), ny = tile_rows_all(P);
     const unsigned int total = band_blocks + (unsigned int)(nx * ny);
     cudaStream_t bs = st;
     cudaError_t e;
@@ -452,6 +489,26 @@ cudaError_t prepare_hancock_fast() {
         e = cudaFuncSetAttribute(hancock_tile_kernel<false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
     return e;
+}
+
+int hancock_tile_height() { return TY; }
+
+unsigned int hancock_fast_blocks(const Params& P, int r0, int r1, int parts) {
+    const Band b = make_band(P.N, P.M, r0, r1);
+    int t0, t1;
+    tile_range(P, r0, r1, &t0, &t1);
+    return ((parts & 1) ? (unsigned int)((b.total + BNT - 1) / BNT) : 0u) +
+           ((parts & 2) && t1 > t0 ? (unsigned int)((t1 - t0) * tile_cols(P)) : 0u);
+}
+
+cudaError_t launch_hancock_fast_rows(const Params& P, const CPlanes& in, const Planes& out,
+                                     const double* T_do, unsigned long long* T_bits,
+                                     Scalars* rot, Scalars* ctr, int r0, int r1,
+                                     unsigned int nblocks, int parts, cudaStream_t st) {
+    if (P.scheme == GD_SCHEME_HANCOCK_REF)
+        return launch_rows<true>(P, in, out, T_do, T_bits, rot, ctr, r0, r1, nblocks, parts,
+                                 st);
+    return launch_rows<false>(P, in, out, T_do, T_bits, rot, ctr, r0, r1, nblocks, parts, st);
 }
 
 cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes& out,

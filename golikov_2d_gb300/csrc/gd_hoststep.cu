@@ -49,7 +49,8 @@ cudaError_t pipe_create(gd_ctx* ctx) {
     HS_TRY(cudaStreamCreateWithFlags(&p->up, cudaStreamNonBlocking));
     HS_TRY(cudaStreamCreateWithFlags(&p->down, cudaStreamNonBlocking));
     HS_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done})
+    HS_TRY(cudaStreamCreateWithFlags(&p->edge, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done, &p->edge_done})
         HS_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int k = 0; k < gd::kMaxBands; ++k) {
         HS_TRY(cudaEventCreateWithFlags(&p->ev_up[k], cudaEventDisableTiming));
@@ -117,15 +118,19 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     gd::HostPipe* p = ctx->pipe;
     const int N = ctx->cfg.N, M = ctx->cfg.M, nf = ctx->nf;
     const long long K = ctx->K;
-    const int T = (M + TY - 1) / TY;                 // tile rows
-    const int nx = (N + TX - 1) / TX;                // tiles per tile row
+    // The fast Hancock step's interior tiles start at row 2 and its edge cells (two rows or
+    // columns from every edge) are a launch of their own; a band there is the rows between
+    // two interior tile-row boundaries, edge cells included.
+    const bool hk = ctx->cfg.mode == GD_MODE_FAST && ctx->cfg.scheme != GD_SCHEME_TVD;
+    const int T = hk ? (M - 4 + TY - 1) / TY : (M + TY - 1) / TY;  // tile (block) rows
+    const int nx = hk ? (N - 4 + TX - 1) / TX : (N + TX - 1) / TX;  // tiles per tile row
     // Smaller bands shorten the pipeline's fill (two bands up before the first step) and
     // drain (one band down after the last); each band should still fill the GPU for a few
     // waves: at least 2 waves of the two resident CTAs per SM the kernels have; 2 to
     // kMaxBands bands of >= 2 block rows.
     int sms = 0;
     HS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    const long long per_band_min = 2LL * 2 * (sms > 0 ? sms : 1);
+    const long long per_band_min = (hk ? 4LL : 2LL) * 2 * (sms > 0 ? sms : 1);
     int B = (int)(((long long)nx * T) / per_band_min);
     if (B > gd::kMaxBands) B = gd::kMaxBands;
     if (B > T / 2) B = T / 2;
@@ -138,10 +143,15 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         *t0 = (int)((long long)k * T / B);
         *t1 = (int)((long long)(k + 1) * T / B);
     };
+    // first row of band k (band B: M)
+    auto row_bound = [&](int k) -> int {
+        if (k <= 0) return 0;
+        if (k >= B) return M;
+        const int t = (int)((long long)k * T / B);
+        return hk ? 2 + t * TY : t * TY;
+    };
     auto band_rows = [&](int k) {
-        int t0, t1;
-        band_tiles(k, &t0, &t1);
-        const int r0 = t0 * TY, r1 = t1 * TY < M ? t1 * TY : M;
+        const int r0 = row_bound(k), r1 = row_bound(k + 1);
         return Rows{(long long)r0 * N, (long long)(r1 - r0) * N};
     };
     // the last band's upload leaves out the seam rows a periodic y-edge has sent first
@@ -175,7 +185,21 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     // stream: the bands write disjoint rows and share one rotation ticket, so the next band's
     // blocks may start while the last wave of this one drains
     Params P = ctx->P;
-    P.tile_nblocks = (unsigned int)(nx * T);
+    unsigned int nblocks = (unsigned int)(nx * T);
+    if (hk) {
+        // the edge cells in one launch over the whole grid (a band's few edge cells would
+        // sit on a few SMs for as long as all of them take), the tiles band by band
+        nblocks = gd::hancock_fast_blocks(P, 0, M, 1);
+        for (int k = 0; k < B; ++k)
+            nblocks += gd::hancock_fast_blocks(P, row_bound(k), row_bound(k + 1), 2);
+        HS_TRY(cudaStreamWaitEvent(p->edge, p->ev_up[B - 1], 0));
+        HS_TRY(gd::launch_hancock_fast_rows(P, gd_ctx::cplanes(ctx->planes(ctx->cur)),
+                                            ctx->planes(1 - ctx->cur), &ctx->sc->T_do,
+                                            &ctx->sc->T_bits, ctx->sc, ctx->sc, 0, M, nblocks, 1,
+                                            p->edge));
+        HS_TRY(cudaEventRecord(p->edge_done, p->edge));
+    }
+    P.tile_nblocks = nblocks;
     const CPlanes in = gd_ctx::cplanes(ctx->planes(ctx->cur));
     const Planes out = ctx->planes(1 - ctx->cur);
     for (int k = 0; k < B; ++k) {
@@ -187,7 +211,10 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         P.tile_rows = t1 - t0;
         ctx->launches += 1;
         unsigned long long* Tb = &ctx->sc->T_bits;
-        if (ctx->cfg.mode == GD_MODE_PARITY)
+        if (hk)
+            HS_TRY(gd::launch_hancock_fast_rows(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc,
+                                                row_bound(k), row_bound(k + 1), nblocks, 2, cs));
+        else if (ctx->cfg.mode == GD_MODE_PARITY)
             HS_TRY(P.scheme != GD_SCHEME_TVD
                        ? gd::launch_hancock_parity(P, in, out, &ctx->sc->T_do, Tb, ctx->sc,
                                                    ctx->sc, 0, cs)
@@ -201,12 +228,14 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         HS_TRY(cudaEventRecord(p->ev_out[k], cs));
         // down stream: band k's result to AoS and to the host while later bands are stepped
         HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
+        if (hk) HS_TRY(cudaStreamWaitEvent(p->down, p->edge_done, 0));
         HS_TRY(from_planes(ctx, band_rows(k), p->down));
         HS_TRY(copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
                          cudaMemcpyDeviceToHost, p->down));
     }
     HS_TRY(cudaEventRecord(p->comp_done, p->comp));
     HS_TRY(cudaStreamWaitEvent(st, p->comp_done, 0));
+    if (hk) HS_TRY(cudaStreamWaitEvent(st, p->edge_done, 0));
     HS_TRY(cudaEventRecord(p->down_done, p->down));
     HS_TRY(cudaStreamWaitEvent(st, p->down_done, 0));
     return cudaSuccess;
@@ -220,7 +249,7 @@ void pipe_free(gd_ctx* ctx) {
     if (!p) return;
     cudaFree(p->aos_in);
     cudaFree(p->aos_out);
-    for (cudaEvent_t e : {p->start, p->down_done, p->comp_done})
+    for (cudaEvent_t e : {p->start, p->down_done, p->comp_done, p->edge_done})
         if (e) cudaEventDestroy(e);
     for (int k = 0; k < kMaxBands; ++k) {
         if (p->ev_up[k]) cudaEventDestroy(p->ev_up[k]);
@@ -229,6 +258,7 @@ void pipe_free(gd_ctx* ctx) {
     if (p->up) cudaStreamDestroy(p->up);
     if (p->down) cudaStreamDestroy(p->down);
     if (p->comp) cudaStreamDestroy(p->comp);
+    if (p->edge) cudaStreamDestroy(p->edge);
     delete p;
     ctx->pipe = nullptr;
 }
@@ -243,16 +273,16 @@ extern "C" gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u,
     int TX = 32, TY = 0;  // the block shape of the launch the bands are cut for
     if (c.mode == GD_MODE_PARITY)
         TY = gd::kParityBlockRows;
+    else if (c.scheme != GD_SCHEME_TVD)
+        TY = gd::hancock_tile_height();
     else if (c.physics == GD_EULER)
         gd::euler_tile_shape(0, &TX, &TY);
     else
         TY = gd::mhd_tile_height();
-    // the banded pipeline: a step that is one launch over tiles or per-cell blocks (the fast
-    // TVD step, either parity step; not the fast Hancock step's two launches), the reference's
-    // dt protocol, grids of at least four block rows, host buffers the device can read and
-    // write (pinned)
-    const bool one_launch = c.mode == GD_MODE_PARITY || c.scheme == GD_SCHEME_TVD;
-    const bool banded = one_launch && ctx->dt_policy == GD_DT_LAGGED && (c.M + TY - 1) / TY >= 4 &&
+    // the banded pipeline: the reference's dt protocol, grids of at least four tile (block)
+    // rows, host buffers the device can read and write (pinned)
+    const int rows = (c.mode == GD_MODE_FAST && c.scheme != GD_SCHEME_TVD) ? c.M - 4 : c.M;
+    const bool banded = ctx->dt_policy == GD_DT_LAGGED && rows > 0 && (rows + TY - 1) / TY >= 4 &&
                         device_visible_host(s) && device_visible_host(u) &&
                         device_visible_host(b) && device_visible_host(s2) &&
                         device_visible_host(u2) && device_visible_host(b2);

@@ -88,6 +88,17 @@ cudaError_t launch_hancock_fast(const Params& P, const CPlanes& in, const Planes
                                 Scalars* ctr, int dt_only, cudaStream_t st,
                                 const HancockStreams* side = nullptr);
 cudaError_t prepare_hancock_fast();
+// The fast Hancock step on rows [r0, r1) only, for a step cut into bands: `parts` 1 launches
+// the edge cells, 2 the interior tiles, 3 both (in that order on `st`); r0 and r1 are 0, M or
+// 2 + a multiple of hancock_tile_height() (the interior tiles start at row 2).  All launches
+// of the step share one rotation ticket of `nblocks` blocks: the sum over the launches of
+// hancock_fast_blocks(P, r0, r1, parts).
+int hancock_tile_height();
+unsigned int hancock_fast_blocks(const Params& P, int r0, int r1, int parts);
+cudaError_t launch_hancock_fast_rows(const Params& P, const CPlanes& in, const Planes& out,
+                                     const double* T_do, unsigned long long* T_bits,
+                                     Scalars* rot, Scalars* ctr, int r0, int r1,
+                                     unsigned int nblocks, int parts, cudaStream_t st);
 
 // Utilities (gd_util.cu).
 cudaError_t launch_aos_to_soa(const double* s, const double* u, const double* b, Planes out,

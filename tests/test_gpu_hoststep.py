@@ -2,7 +2,7 @@
 of block rows on two copy streams) equals gd_import + gd_advance(1) + gd_export bit for bit,
 on periodic, transmissive and the reference's native boundaries, in fast and parity modes
 (the Hancock scheme's too), over several steps, and through the sequential path for pageable
-buffers, small grids and the fast Hancock step."""
+buffers and small grids."""
 import numpy as np
 import pytest
 
@@ -22,6 +22,7 @@ CASES = {
                                                         mode=g.MODE_PARITY),
     "hancock_parity": lambda: problems.hancock_wind(160, 96, mode=g.MODE_PARITY),
     "hancock_fast": lambda: problems.hancock_wind(160, 96),
+    "hancock_fast_ragged": lambda: problems.hancock_wind(131, 77, scheme=g.SCHEME_HANCOCK),
 }
 
 
