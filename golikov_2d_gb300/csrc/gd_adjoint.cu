@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(FBX * FBY) adj_face_kernel(Params P, CPlanes U
     const int iy = blockIdx.y * FBY + threadIdx.y;  // row (x) or y-face index (y)
     if (ix >= N || iy >= M) return;
     const double T_do = *T_do_ptr;
-    const double kk = isx ? T_do / P.dx : T_do / P.dy;
+    const double kk = T_do * (isx ? P.inv_dx : P.inv_dy);  // the forward's scaling
     // the face lies between cells a-1 and a along its normal; cells a-2 .. a+1
     long long kc[4];
 #pragma unroll
@@ -836,7 +836,7 @@ __global__ void __launch_bounds__(FBX * FBY) adj_gather_kernel(Params P,
     if (gx >= N || gy >= M) return;
     const long long k = (long long)gy * N + gx;
     const double T_do = *T_do_ptr;
-    const double kx = T_do / P.dx, ky = T_do / P.dy;
+    const double kx = T_do * P.inv_dx, ky = T_do * P.inv_dy;
     double lam[NF];
 #pragma unroll
     for (int f = 0; f < NF; ++f) lam[f] = scratch[(size_t)f * K + k];

@@ -95,10 +95,13 @@ Params make_params(const gd_config& c) {
     P.gamma = c.gamma;
     P.krit = c.krit;
     P.frozen_radius = c.frozen_radius;
+    P.frozen = c.frozen_radius > 0.0 ? 1 : 0;
     P.scheme = c.scheme;
     P.x_max = c.x_max;
     P.y_max = c.y_max;
     P.gm1 = c.gamma - 1.0;
+    P.inv_dx = 1.0 / c.dx;
+    P.inv_dy = 1.0 / c.dy;
     P.inv_gm1 = 1.0 / (c.gamma - 1.0);
     P.ambient_p = 1.0 / c.gamma;
     // rad passed to the flux: dy on x-faces in the Euler kernels (kernel.cu:1811, 3562),

@@ -69,6 +69,7 @@ __device__ __forceinline__ bool gt_zero(Dual x) { return gt_zero(x.v); }
 __device__ __forceinline__ bool lt_zero(Dual x) { return lt_zero(x.v); }
 __device__ __forceinline__ bool ge_zero(Dual x) { return ge_zero(x.v); }
 __device__ __forceinline__ bool isfinite(Dual x) { return ::isfinite(x.v); }
+__device__ __forceinline__ bool finite_bits(Dual x) { return finite_bits(x.v); }
 __device__ __forceinline__ Dual dabs(Dual x) { return lt_zero(x.v) ? -x : x; }
 __device__ __forceinline__ Dual dmin(Dual a, Dual b) { return dlt(b.v, a.v) ? b : a; }
 __device__ __forceinline__ Dual dmax(Dual a, Dual b) { return dlt(a.v, b.v) ? b : a; }

@@ -150,8 +150,11 @@ struct TileResult {
 
 // One TX x TY tile whose lower-left cell is (tx0, ty0).  Reads `in`, writes `out`, returns
 // the per-thread wave-speed maxima and counters.  Every thread of the block must call it.
+// Not inlined: the single-grid kernel and the persistent batch kernel call one compiled
+// function per tile shape, so a grid's arithmetic, and its bits, do not depend on which
+// schedule advanced it (inlined into each, the compiler may fuse the two differently).
 template <int ORDER, int TX, int TY>
-__device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, const Planes& out,
+__device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, const Planes& out,
                                            int tx0, int ty0, double T_do, int dt_only,
                                            double* smem, TileResult& res) {
     using S = Shape<ORDER, TX, TY>;
@@ -225,7 +228,7 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
         }
         // cells on either side: A (low) and B (high)
         const int ax = isx ? lx - 1 : lx, ay = isx ? ly : ly - 1;
-        if (P.frozen_radius > 0.0 && !cell_active(P, tx0 + ax, ty0 + ay) &&
+        if (P.frozen && !cell_active(P, tx0 + ax, ty0 + ay) &&
             !cell_active(P, tx0 + lx, ty0 + ly))
             continue;  // no updated cell uses this face
         const double* pa = prim + (ay + H) * SX + (ax + H);
@@ -281,7 +284,7 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
     __syncthreads();
 
     // ---- U: update --------------------------------------------------------------------------
-    const double kx = T_do / P.dx, ky = T_do / P.dy;
+    const double kx = T_do * P.inv_dx, ky = T_do * P.inv_dy;
     bool any_active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
     for (int i = tid; i < TX * TY; i += NT) {
@@ -291,7 +294,7 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
         const double* c = prim + (ly + H) * SX + (lx + H);
         const double r = c[0], p = c[SY * SX], u = c[2 * SY * SX], v = c[3 * SY * SX];
         const long long k = (long long)gy * N + gx;
-        if (P.frozen_radius > 0.0 && !cell_active(P, gx, gy)) {  // the faces' own test
+        if (P.frozen && !cell_active(P, gx, gy)) {  // the faces' own test
             if (!dt_only) {
                 out.f[0][k] = r; out.f[1][k] = p; out.f[2][k] = u; out.f[3][k] = v;
             }
@@ -316,7 +319,7 @@ __device__ __forceinline__ void euler_tile(const Params& P, const CPlanes& in, c
         const double v2 = fma(r, v, -d[3]) * inv;
         double p2 = fma(-0.5 * r2, fma(u2, u2, v2 * v2), E - d[1]) * P.gm1;
         if (le_zero(p2)) { p2 = 0.000001; ++nfl_p; }
-        if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2)) ++nbad;
+        if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2)) ++nbad;
         out.f[0][k] = r2;
         out.f[1][k] = p2;
         out.f[2][k] = u2;

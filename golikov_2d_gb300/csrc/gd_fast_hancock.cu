@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
     // ---- P: predictions of the tile + 1 halo (not its corners) ---------------------------
     const double T_do = *T_do_ptr;
     const double st = 0.5 * T_do;
-    const double sx = st / P.dx, sy = st / P.dy;
+    const double sx = st * P.inv_dx, sy = st * P.inv_dy;
     for (int i = tid; i < PY * PX; i += NT) {
         const int py = i / PX, px = i - py * PX;
         if ((px == 0 || px == PX - 1) && (py == 0 || py == PY - 1)) continue;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
         for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
     } else if (my_flag == 2 && !dt_only) {
         const double hT = 0.5 * T_do;
-        const double kx = hT / P.dx, ky = hT / P.dy;
+        const double kx = hT * P.inv_dx, ky = hT * P.inv_dy;
         const double hTy = hT * rowiy[cy + 1];
         const int o = (cy + 1) * PX + (cx + 1);
         double A[NF], d[NF];
@@ -320,8 +320,8 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
             p2 = 0.000001;
             ++nfl_p;
         }
-        if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2) ||
-            !isfinite(bx2) || !isfinite(by2) || !isfinite(bz2))
+        if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2) ||
+            !finite_bits(bx2) || !finite_bits(by2) || !finite_bits(bz2))
             ++nbad;
         const long long k = (long long)gy * N + gx;
         out.f[0][k] = r2;
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
             tmin = hancock_cell<VYP>(P, in, n, m, y, *T_do_ptr, res, nfl_r, nfl_p);
             if (!dt_only) {
                 for (int f = 0; f < NF; ++f) {
-                    if (!isfinite(res[f])) {
+                    if (!finite_bits(res[f])) {
                         ++nbad;
                         break;
                     }

@@ -195,7 +195,7 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
             if (tx0 + lx >= N || ty0 + ly > M) continue;
         }
         const int ax = isx ? lx - 1 : lx, ay = isx ? ly : ly - 1;
-        if (P.frozen_radius > 0.0 && !cell_active(P, tx0 + ax, ty0 + ay) &&
+        if (P.frozen && !cell_active(P, tx0 + ax, ty0 + ay) &&
             !cell_active(P, tx0 + lx, ty0 + ly))
             continue;
         const T* pa = prim + (ay + H) * SX + (ax + H);
@@ -260,7 +260,7 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
     __syncthreads();
 
     // ---- U: update (kernel.cu:2606-2660 in Heaviside-Lorentz field units) ----------------------
-    const double kx = T_do / P.dx, ky = T_do / P.dy;
+    const double kx = T_do * P.inv_dx, ky = T_do * P.inv_dy;
     const bool axi = P.geometry == GD_AXISYM;
     bool any_active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
@@ -273,13 +273,9 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         const T r = c[0], p = c[PS], u = c[2 * PS], v = c[3 * PS];
         const T bx = c[4 * PS], by = c[5 * PS], bz = c[6 * PS];
         const long long k = (long long)gy * N + gx;
-        const double y = P.y0 + gy * P.dy;
-        if (P.frozen_radius > 0.0) {
-            const double x = P.x0 + gx * P.dx;
-            if (sqrt(x * x + y * y) < P.frozen_radius) {
-                if (!dt_only) copy_cell(in, out, k);
-                continue;
-            }
+        if (P.frozen && !cell_active(P, gx, gy)) {  // the faces' own test
+            if (!dt_only) copy_cell(in, out, k);
+            continue;
         }
         any_active = true;
         if (dt_only) continue;
@@ -296,7 +292,7 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         const T bxE = c[4 * PS + 1], bxW = c[4 * PS - 1];
         const T byN = c[5 * PS + SX], byS = c[5 * PS - SX];
         T divb = fma(0.5 * kx, bxE - bxW, 0.5 * ky * (byN - byS));  // T_do * div b
-        const double iy = axi ? rcp_fast(y) : 0.0;
+        const double iy = axi ? rcp_fast(P.y0 + gy * P.dy) : 0.0;
         if (axi) divb = fma(T_do * by, iy, divb);                 // kernel.cu:2615
         if constexpr (std::is_same<T, double>::value) {
             if (aux != nullptr) {
@@ -330,8 +326,8 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         const T u2 = mx2 * inv, v2 = my2 * inv;
         T p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2), fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
         if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
-        if (!isfinite(r2) || !isfinite(p2) || !isfinite(u2) || !isfinite(v2) || !isfinite(bx2) ||
-            !isfinite(by2) || !isfinite(bz2))
+        if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2) ||
+            !finite_bits(bx2) || !finite_bits(by2) || !finite_bits(bz2))
             ++nbad;
         store_state(out, k, 0, r2);
         store_state(out, k, 1, p2);

@@ -29,6 +29,7 @@ struct Params {
     double dx, dy, x0, y0;
     double gamma, krit;
     double frozen_radius;
+    int frozen;           // frozen_radius > 0 (tested on the integer pipe)
     int scheme;           // GD_SCHEME_*
     double x_max, y_max;  // domain extents of the Hancock schemes' cell coordinates
     // A launch of the fast step over a band of tile rows (gd_step_host): the band starts at
@@ -38,6 +39,7 @@ struct Params {
     unsigned int tile_nblocks;
     // derived
     double gm1, inv_gm1;
+    double inv_dx, inv_dy;  // 1/dx, 1/dy: the fast kernels scale fluxes by T_do * inv_dx
     double ambient_p;   // 1/gamma
     double krad_x;      // krit * rad used for faces with an x normal
     double krad_y;      // krit * rad used for faces with a y normal
@@ -177,7 +179,8 @@ __device__ __forceinline__ double rcp_fast(double x) {
 }
 
 __device__ __forceinline__ double rsqrt_fast(double x) {
-    if (!in_f32_range(x) || !(x > 0.0)) return 1.0 / sqrt(x);
+    // x > 0 on the integer pipe: NaN, +-0, negative and out-of-range values all fall back
+    if (!in_f32_range(x) || !gt_zero(x)) return 1.0 / sqrt(x);
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
     const double y = widen_f32(r);
@@ -186,8 +189,13 @@ __device__ __forceinline__ double rsqrt_fast(double x) {
 }
 
 __device__ __forceinline__ double sqrt_fast(double x) {
-    // sqrt(x) = x * rsqrt(x), exact zero preserved
-    return x == 0.0 ? 0.0 : x * rsqrt_fast(x);
+    // sqrt(x) = x * rsqrt(x), exact zero preserved (the +-0 test on the integer pipe)
+    return (bits(x) << 1) == 0 ? 0.0 : x * rsqrt_fast(x);
+}
+
+// isfinite(x) on the integer pipe: the exponent field is not all ones
+__device__ __forceinline__ bool finite_bits(double x) {
+    return (abs_bits(x) >> 52) != 0x7ffULL;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -255,9 +263,11 @@ __device__ __forceinline__ void fetch_cell(const Params& P, const CPlanes& in, i
 // Inside the grid and not frozen (kernel.cu:2205, 2218: dist = sqrt(x*x + y*y) < ddist).
 __device__ __forceinline__ bool cell_active(const Params& P, int gx, int gy) {
     if (gx < 0 || gx >= P.N || gy < 0 || gy >= P.M) return false;
-    if (P.frozen_radius <= 0.0) return true;
+    if (!P.frozen) return true;
     const double x = P.x0 + gx * P.dx, y = P.y0 + gy * P.dy;
-    return !(sqrt(x * x + y * y) < P.frozen_radius);
+    // explicit roundings: every build and every call site decides alike (the parity build,
+    // without contraction, computes the same sum)
+    return !(sqrt(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y))) < P.frozen_radius);
 }
 
 // ---------------------------------------------------------------------------------------

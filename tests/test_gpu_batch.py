@@ -1,8 +1,8 @@
 """Batched form: many independent grids of uneven sizes in one persistent launch per step.
 
-The persistent schedule, the looped schedule (one launch per grid) and CUDA-graph replay run
-the same kernel instantiation, so they must agree bit for bit, and each grid must agree bit
-for bit with the single-grid context and, to the fast path's tolerance, with the oracle.
+The persistent schedule, the looped schedule (one launch per grid), CUDA-graph replay and
+the single-grid context call the same compiled tile function (not inlined into the kernels),
+so they must agree bit for bit, and, to the fast path's tolerance, with the oracle.
 Different tile shapes are different instantiations that the compiler may fuse differently:
 they agree to rounding.  Autotuning itself must leave the state, dt and time untouched."""
 import numpy as np
