@@ -20,13 +20,13 @@
 // the forward kernel; adjoints w.r.t. the stored Gaussian field are converted at the ends.
 #include "gd_internal.cuh"
 #include "gd_kernels.h"
+#include "gd_mhd_flux.cuh"
 
 namespace gd {
 namespace {
 
 constexpr int NF = 7;
 constexpr int NT = 256;
-constexpr int ATX = 32, ATY = 8;
 
 // ---------------------------------------------------------------------------------------
 // Pass A: transpose of the cell update (Cartesian).
@@ -140,13 +140,17 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
 // ---------------------------------------------------------------------------------------
 // Reverse sweep of one HLLD face flux (method 3) in the local frame.
 // Inputs: the two face states A (low) and B (high) as (r, p, un, ut, bn, bt, bz) and the
-// adjoint of the flux (m, mn, mt, e, bn, bt, bz).  Adds the adjoints of A and B to Ab, Bb.
+// adjoint of the flux (m, mn, mt, e, bn, bt, bz).  Writes the adjoints of A and B to Ab, Bb.
 // The forward part repeats hlld_local<double> of gd_fast_mhd.cu operation for operation.
+// The reverse does per-side work only where the adjoint can be non-zero: the flux's base
+// terms and the energy enter through the upwind side K alone (the side whose state or star
+// state gives the flux), the fast speed through the side of max(cf) alone, and only K's
+// star energy and its sb term reach the flux; those chains run once, on the selected
+// side's values, and their results are added to that side.
 // ---------------------------------------------------------------------------------------
 struct SideV {
     double r, p, un, ut, bn, bt, bz;
-    double bn2, bb, pT, kin, E, gp, a, disc, rq, X, rs, cf;  // rq = 1 / sqrt(disc)
-    double F0, F1, F2, F4, F6, F7;
+    double bn2, bb, pT, gp, a, disc, rq, rs, cf;  // rq = 1 / sqrt(disc), rs = 1 / sqrt(X r)
     bool disc0;
 };
 
@@ -155,8 +159,6 @@ __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params
     S.bn2 = S.bn * S.bn;
     S.bb = fma(S.bz, S.bz, fma(S.bt, S.bt, S.bn2));
     S.pT = fma(0.5, S.bb, S.p);
-    S.kin = fma(S.r, fma(S.un, S.un, S.ut * S.ut), S.bb);
-    S.E = fma(S.p, P.inv_gm1, 0.5 * S.kin);
     S.gp = P.gamma * S.p;
     S.a = S.gp + S.bb;
     double disc = fma(S.a, S.a, -4.0 * S.gp * S.bn2);
@@ -164,111 +166,40 @@ __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params
     S.disc = S.disc0 ? 0.0 : disc;
     // sqrt_fast(disc) = disc * rsqrt_fast(disc), kept apart so the reverse reuses 1/sqrt
     S.rq = rsqrt_fast(S.disc);
-    const double sq = S.disc == 0.0 ? 0.0 : S.disc * S.rq;
-    S.X = 0.5 * (S.a + sq);
-    S.rs = rsqrt_fast(S.X * S.r);
-    S.cf = S.X * S.rs;
-    S.F0 = S.r * S.un;
-    S.F1 = fma(S.F0, S.un, S.pT - S.bn2);
-    S.F2 = fma(S.F0, S.ut, -S.bn * S.bt);
-    S.F4 = fma(S.E + S.pT, S.un, -S.bn * fma(S.ut, S.bt, S.un * S.bn));
-    S.F6 = fma(S.un, S.bt, -S.ut * S.bn);
-    S.F7 = S.un * S.bz;
+    const double sq = (bits(S.disc) << 1) == 0 ? 0.0 : S.disc * S.rq;
+    const double X = 0.5 * (S.a + sq);
+    S.rs = rsqrt_fast(X * S.r);
+    S.cf = X * S.rs;
 }
 
-// adjoints of the side's derived quantities -> adjoints of its inputs (qb[7], added)
+// per-side adjoint accumulators of the face state and of two derived quantities
 struct SideB {
-    double r, p, un, ut, bn, bt, bz, pT, E, cf, F0, F1, F2, F4, F6, F7;
+    double r, p, un, ut, bn, bt, bz, pT, bb, bn2;
 };
 
-__device__ __forceinline__ void side_rev(const SideV& S, SideB& b, const Params& P, double* qb) {
-    // F7 = un bz
-    b.un += b.F7 * S.bz;
-    b.bz += b.F7 * S.un;
-    // F6 = un bt - ut bn
-    b.un += b.F6 * S.bt;
-    b.bt += b.F6 * S.un;
-    b.ut -= b.F6 * S.bn;
-    b.bn -= b.F6 * S.ut;
-    // F4 = (E + pT) un - bn (ut bt + un bn)
-    {
-        const double w = fma(S.ut, S.bt, S.un * S.bn);
-        b.E += b.F4 * S.un;
-        b.pT += b.F4 * S.un;
-        b.un += b.F4 * (S.E + S.pT);
-        b.bn -= b.F4 * w;
-        const double wb = -b.F4 * S.bn;
-        b.ut += wb * S.bt;
-        b.bt += wb * S.ut;
-        b.un += wb * S.bn;
-        b.bn += wb * S.un;
-    }
-    // F2 = F0 ut - bn bt
-    b.F0 += b.F2 * S.ut;
-    b.ut += b.F2 * S.F0;
-    b.bn -= b.F2 * S.bt;
-    b.bt -= b.F2 * S.bn;
-    // F1 = F0 un + pT - bn^2
-    b.F0 += b.F1 * S.un;
-    b.un += b.F1 * S.F0;
-    b.pT += b.F1;
-    b.bn -= 2.0 * b.F1 * S.bn;
-    // F0 = r un
-    b.r += b.F0 * S.un;
-    b.un += b.F0 * S.r;
-    // cf = X * rsqrt(X r) = sqrt(X / r)
-    double Xb = 0.0, rb_cf = 0.0;
-    {
-        // d cf / dX = 0.5 / sqrt(X r) = 0.5 rs; d cf / dr = -0.5 cf / r = -0.5 X rs / r
-        Xb += b.cf * 0.5 * S.rs;
-        rb_cf = -b.cf * 0.5 * S.cf * rcp_fast(S.r);
-    }
-    b.r += rb_cf;
-    // X = 0.5 (a + sq)
-    double ab = 0.5 * Xb, sqb = 0.5 * Xb;
-    // sq = sqrt(disc), disc = a^2 - 4 gp bn^2 (clamped at 0)
-    double gpb = 0.0, bn2b = 0.0;
-    if (!S.disc0 && S.disc != 0.0) {
-        const double discb = sqb * 0.5 * S.rq;
-        ab += discb * 2.0 * S.a;
-        gpb -= discb * 4.0 * S.bn2;
-        bn2b -= discb * 4.0 * S.gp;
-    }
-    // a = gp + bb ; gp = gamma p
-    gpb += ab;
-    double bbb = ab;
-    b.p += gpb * P.gamma;
-    // E = p inv_gm1 + 0.5 kin ; kin = r (un^2 + ut^2) + bb
-    b.p += b.E * P.inv_gm1;
-    const double kinb = 0.5 * b.E;
-    b.r += kinb * fma(S.un, S.un, S.ut * S.ut);
-    b.un += kinb * 2.0 * S.r * S.un;
-    b.ut += kinb * 2.0 * S.r * S.ut;
-    bbb += kinb;
-    // pT = 0.5 bb + p
-    bbb += 0.5 * b.pT;
-    b.p += b.pT;
-    // bb = bz^2 + bt^2 + bn2 ; bn2 = bn^2
-    b.bz += 2.0 * bbb * S.bz;
-    b.bt += 2.0 * bbb * S.bt;
-    bn2b += bbb;
-    b.bn += 2.0 * bn2b * S.bn;
-    qb[0] += b.r;
-    qb[1] += b.p;
-    qb[2] += b.un;
-    qb[3] += b.ut;
-    qb[4] += b.bn;
-    qb[5] += b.bt;
-    qb[6] += b.bz;
+// adds k to the side the select names with one FP64 add (the other side is untouched)
+__device__ __forceinline__ void add_to(bool first, double& a, double& b, double k) {
+    const double s = (first ? a : b) + k;
+    a = first ? s : a;
+    b = first ? b : s;
 }
 
-__device__ __forceinline__ double isel(double v, int idbn) {
-    return idbn == 0 ? 0.0 : (idbn < 0 ? -v : v);
+// the side-generic tail: pT = 0.5 bb + p, bb = bz^2 + bt^2 + bn2, bn2 = bn^2
+__device__ __forceinline__ void side_tail(const SideV& S, SideB& b, double* qb) {
+    const double bbb = fma(0.5, b.pT, b.bb);
+    const double bn2b = b.bn2 + bbb;
+    qb[0] = b.r;
+    qb[1] = b.p + b.pT;
+    qb[2] = b.un;
+    qb[3] = b.ut;
+    qb[4] = fma(2.0 * bn2b, S.bn, b.bn);
+    qb[5] = fma(2.0 * bbb, S.bt, b.bt);
+    qb[6] = fma(2.0 * bbb, S.bz, b.bz);
 }
 
-// Fb = (m, mn, mt, e, bn, bt, bz); qa_b, qb_b accumulate (r, p, un, ut, bn, bt, bz).
-__device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
-                         const Params& P, double* qa_b, double* qb_b) {
+// Fb = (m, mn, mt, e, bn, bt, bz); qa_b, qb_b receive (r, p, un, ut, bn, bt, bz).
+__device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
+                                         const Params& P, double* qa_b, double* qb_b) {
     SideV A, B;
     side_fwd(A, qa, P);
     side_fwd(B, qb, P);
@@ -291,9 +222,7 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
     const double UU = UUR ? dabs(SR) : dabs(SL);
     const double iS = rcp_fast(SR - SL);
     const double bnn = fma(SR, B.bn, -SL * A.bn);
-    const double btn = fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6);
-    const double bzn = fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7);
-    const double bn = bnn * iS, bt = btn * iS, bz = bzn * iS;
+    const double bn = bnn * iS;
     const double iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
     const double rLL = mL * iL, rRR = mR * iR;
     const double bbn = bn * bn;
@@ -327,17 +256,10 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
         vRR = B.ut; wRR = 0.0; btR = 0.0; bzR = 0.0;
     }
     const double SMbn = SM * bn;
-    const double sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
-    const double sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
-    const double wA = fma(A.un, A.bn, A.ut * A.bt), wB = fma(B.un, B.bn, B.ut * B.bt);
-    const double eLLn = fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) + bn * (wA - sbLL);
-    const double eRRn = fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) + bn * (wB - sbRR);
-    const double eLL = eLLn * iL, eRR = eRRn * iR;
     const double isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
     const double sLL = rLL * isLL, sRR = rRR * isRR;
     const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
     const double abn = dabs(bn);
-    const double sgn_bn = gt_zero(bn) ? 1.0 : -1.0;
     const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
     const double SRR = bnz ? fma(abn, isRR, SM) : SM;
     const int idbn = bnz ? (gt_zero(bn) ? 1 : -1) : 0;
@@ -345,51 +267,57 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
     int level;
     if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
     else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
-    const SideV& Kf = takeL ? A : B;
+    // the upwind side K: its state, star state and energies
+    const double Kr = takeL ? A.r : B.r, Kp = takeL ? A.p : B.p;
+    const double Kun = takeL ? A.un : B.un, Kut = takeL ? A.ut : B.ut;
+    const double Kbn = takeL ? A.bn : B.bn, Kbt = takeL ? A.bt : B.bt;
+    const double Kbz = takeL ? A.bz : B.bz, KpT = takeL ? A.pT : B.pT;
+    const double Kbb = takeL ? A.bb : B.bb;
     const double S = takeL ? SL : SR;
+    const double su = takeL ? suL : suR;
+    const double iK = takeL ? iL : iR;
     const double rK = takeL ? rLL : rRR;
     const double vK = takeL ? vLL : vRR;
-    const double eK = takeL ? eLL : eRR;
+    const double wK = takeL ? wLL : wRR;
     const double btK = takeL ? btL : btR;
     const double bzK = takeL ? bzL : bzR;
+    const double vsq = fma(Kun, Kun, Kut * Kut);
+    const double KE = fma(Kp, P.inv_gm1, 0.5 * fma(Kr, vsq, Kbb));
+    const double sbK = fma(wK, bzK, fma(vK, btK, SMbn));
+    const double wKf = fma(Kun, Kbn, Kut * Kbt);
+    const double eKn = fma(KE, su, fma(PTT, SM, -KpT * Kun)) + bn * (wKf - sbK);
+    const double eK = eKn * iK;
     // double-star (only needed for level 2)
     double is = 0, vL3 = 0, wL3 = 0, s2 = 0, bt3 = 0, bz3 = 0, sb3 = 0, sK = 0, e3 = 0, S2 = 0;
     if (level == 2) {
         is = rcp_fast(sLL + sRR);
-        vL3 = (fma(sLL, vLL, sRR * vRR) + isel(btR - btL, idbn)) * is;
-        wL3 = (fma(sLL, wLL, sRR * wRR) + isel(bzR - bzL, idbn)) * is;
-        s2 = isel(sLL * sRR, idbn);
+        vL3 = (fma(sLL, vLL, sRR * vRR) + sgn_select(btR - btL, idbn)) * is;
+        wL3 = (fma(sLL, wLL, sRR * wRR) + sgn_select(bzR - bzL, idbn)) * is;
+        s2 = sgn_select(sLL * sRR, idbn);
         bt3 = fma(s2, vRR - vLL, fma(sLL, btR, sRR * btL)) * is;
         bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
         sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
         sK = takeL ? -sLL : sRR;
-        e3 = fma(isel(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
+        e3 = fma(sgn_select(sK, idbn), sbK - sb3, eK);
         S2 = takeL ? SLL : SRR;
     }
 
     // ---- reverse ------------------------------------------------------------------------
     SideB Ab = {}, Bb = {};
-    SideB& Kb = takeL ? Ab : Bb;
+    // adjoints of the K side's state and energy (added to its side at the end)
+    double kr = 0, kun = 0, kut = 0, kE = 0, kbt = 0, kbz = 0, kbn = 0, kpT = 0;
     // adjoints of intermediates
-    double SLb = 0, SRb = 0, SMb = 0, PTTb = 0, UUb = 0, bnb = 0, btb = 0, bzb = 0;
+    double SLb = 0, SRb = 0, SMb = 0, PTTb = 0, UUb = 0, bnb = 0;
     double rLLb = 0, rRRb = 0, iLb = 0, iRb = 0;
     double vLLb = 0, wLLb = 0, btLb = 0, bzLb = 0, vRRb = 0, wRRb = 0, btRb = 0, bzRb = 0;
-    double eLLb = 0, eRRb = 0, sLLb = 0, sRRb = 0, SLLb = 0, SRRb = 0, SMbnb = 0;
-    double sbLLb = 0, sbRRb = 0;
+    double sLLb = 0, sRRb = 0, SLLb = 0, SRRb = 0, SMbnb = 0;
     const double Fm = Fb[0], Fmn = Fb[1], Fmt = Fb[2], Fe = Fb[3], Fbn = Fb[4], Fbt = Fb[5],
                  Fbz = Fb[6];
     // F.bn = -UU (B.bn - A.bn)
-    UUb -= Fbn * (B.bn - A.bn);
-    Bb.bn -= Fbn * UU;
-    Ab.bn += Fbn * UU;
-    // base fluxes of side K
-    Kb.F0 += Fm;
-    Kb.F1 += Fmn;
-    Kb.F2 += Fmt;
-    Kb.F4 += Fe;
-    Kb.F6 += Fbt;
-    Kb.F7 += Fbz;
-    double Sb = 0, rKb = 0, vKb = 0, eKb = 0, btKb = 0, bzKb = 0;
+    UUb = -Fbn * (B.bn - A.bn);
+    Bb.bn = -Fbn * UU;
+    Ab.bn = Fbn * UU;
+    double Sb = 0, rKb = 0, vKb = 0, wKb = 0, eKb = 0, btKb = 0, bzKb = 0, sbKb = 0;
     if (level >= 1) {
         if (level == 2) {
             // F.mt += S2 rK (vL3 - vK); F.e += S2 (e3 - eK); F.bt += S2 (bt3 - btK);
@@ -406,14 +334,13 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
             double bz3b = Fbz * S2;
             bzKb -= Fbz * S2;
             if (takeL) SLLb += S2b; else SRRb += S2b;
-            // e3 = eK + isel(sK) (sbK - sb3)
+            // e3 = eK + sgn(sK) (sbK - sb3)
             eKb += e3b;
-            const double sKv = isel(sK, idbn);
-            const double sbK = takeL ? sbLL : sbRR;
+            const double sKv = sgn_select(sK, idbn);
             const double sKvb = e3b * (sbK - sb3);
-            if (takeL) sbLLb += e3b * sKv; else sbRRb += e3b * sKv;
+            sbKb += e3b * sKv;
             double sb3b = -e3b * sKv;
-            const double sKb = isel(sKvb, idbn);
+            const double sKb = sgn_select(sKvb, idbn);
             if (takeL) sLLb -= sKb; else sRRb += sKb;
             // sb3 = wL3 bz3 + vL3 bt3 + SMbn
             double wL3b = sb3b * bz3;
@@ -442,12 +369,12 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
                 btRb += mb * sLL;
                 sRRb += mb * btL;
                 btLb += mb * sRR;
-                // s2 = isel(sLL sRR)
-                const double pb = isel(s2b, idbn);
+                // s2 = sgn(sLL sRR)
+                const double pb = sgn_select(s2b, idbn);
                 sLLb += pb * sRR;
                 sRRb += pb * sLL;
             }
-            // wL3 = (sLL wLL + sRR wRR + isel(bzR - bzL)) is
+            // wL3 = (sLL wLL + sRR wRR + sgn(bzR - bzL)) is
             {
                 isb += wL3b * (wL3 * (sLL + sRR));
                 const double nb = wL3b * is;
@@ -455,11 +382,11 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
                 wLLb += nb * sLL;
                 sRRb += nb * wRR;
                 wRRb += nb * sRR;
-                const double tb = isel(nb, idbn);
+                const double tb = sgn_select(nb, idbn);
                 bzRb += tb;
                 bzLb -= tb;
             }
-            // vL3 = (sLL vLL + sRR vRR + isel(btR - btL)) is
+            // vL3 = (sLL vLL + sRR vRR + sgn(btR - btL)) is
             {
                 isb += vL3b * (vL3 * (sLL + sRR));
                 const double nb = vL3b * is;
@@ -467,7 +394,7 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
                 vLLb += nb * sLL;
                 sRRb += nb * vRR;
                 vRRb += nb * sRR;
-                const double tb = isel(nb, idbn);
+                const double tb = sgn_select(nb, idbn);
                 btRb += tb;
                 btLb -= tb;
             }
@@ -479,95 +406,71 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
         // level-1 terms: F.m += S (rK - K.r); F.mn += S (rK SM - K.r K.un);
         // F.mt += S (rK vK - K.r K.ut); F.e += S (eK - K.E); F.bt += S (btK - K.bt);
         // F.bz += S (bzK - K.bz)
-        Sb += Fm * (rK - Kf.r) + Fmn * fma(rK, SM, -Kf.r * Kf.un) +
-              Fmt * fma(rK, vK, -Kf.r * Kf.ut) + Fe * (eK - Kf.E) + Fbt * (btK - Kf.bt) +
-              Fbz * (bzK - Kf.bz);
+        Sb += Fm * (rK - Kr) + Fmn * fma(rK, SM, -Kr * Kun) + Fmt * fma(rK, vK, -Kr * Kut) +
+              Fe * (eK - KE) + Fbt * (btK - Kbt) + Fbz * (bzK - Kbz);
         rKb += S * (Fm + Fmn * SM + Fmt * vK);
         SMb += S * Fmn * rK;
         vKb += S * Fmt * rK;
         eKb += S * Fe;
         btKb += S * Fbt;
         bzKb += S * Fbz;
-        Kb.r -= S * (Fm + Fmn * Kf.un + Fmt * Kf.ut);
-        Kb.un -= S * Fmn * Kf.r;
-        Kb.ut -= S * Fmt * Kf.r;
-        Kb.E -= S * Fe;
-        Kb.bt -= S * Fbt;
-        Kb.bz -= S * Fbz;
+        kr = -S * (Fm + Fmn * Kun + Fmt * Kut);
+        kun = -S * Fmn * Kr;
+        kut = -S * Fmt * Kr;
+        kE = -S * Fe;
+        kbt = -S * Fbt;
+        kbz = -S * Fbz;
     }
+    // eK = eKn iK, eKn = K.E su + PTT SM - K.pT K.un + bn (wKf - sbK)
+    const double iKb = eKb * eKn;
+    {
+        const double nb = eKb * iK;
+        kE += nb * su;
+        const double sub = nb * KE;
+        PTTb += nb * SM;
+        SMb += nb * PTT;
+        kpT -= nb * Kun;
+        kun -= nb * KpT;
+        bnb += nb * (wKf - sbK);
+        const double wKfb = nb * bn;
+        sbKb -= nb * bn;
+        // wKf = K.un K.bn + K.ut K.bt
+        kun += wKfb * Kbn;
+        kbn += wKfb * Kun;
+        kut += wKfb * Kbt;
+        kbt += wKfb * Kut;
+        // su = S - K.un
+        Sb += sub;
+        kun -= sub;
+    }
+    // sbK = wK bzK + vK btK + SMbn
+    wKb += sbKb * bzK;
+    bzKb += sbKb * wK;
+    vKb += sbKb * btK;
+    btKb += sbKb * vK;
+    SMbnb += sbKb;
     // distribute the K-selected adjoints
     if (takeL) {
-        SLb += Sb; rLLb += rKb; vLLb += vKb; eLLb += eKb; btLb += btKb; bzLb += bzKb;
+        SLb += Sb; rLLb += rKb; vLLb += vKb; wLLb += wKb; btLb += btKb; bzLb += bzKb;
+        iLb += iKb;
     } else {
-        SRb += Sb; rRRb += rKb; vRRb += vKb; eRRb += eKb; btRb += btKb; bzRb += bzKb;
+        SRb += Sb; rRRb += rKb; vRRb += vKb; wRRb += wKb; btRb += btKb; bzRb += bzKb;
+        iRb += iKb;
     }
     // SLL = SM - abn isLL ; SRR = SM + abn isRR  (if bnz, else = SM)
-    double isLLb = 0, isRRb = 0, abnb = 0;
+    double isLLb = 0, isRRb = 0;
+    SMb += SLLb + SRRb;
     if (bnz) {
-        SMb += SLLb + SRRb;
-        abnb += -SLLb * isLL + SRRb * isRR;
-        isLLb += -SLLb * abn;
-        isRRb += SRRb * abn;
-    } else {
-        SMb += SLLb + SRRb;
+        const double abnb = fma(SRRb, isRR, -SLLb * isLL);
+        isLLb = -SLLb * abn;
+        isRRb = SRRb * abn;
+        bnb += sgn_select(abnb, idbn);
     }
-    bnb += abnb * sgn_bn;
     // sLL = rLL isLL, isLL = rsqrt(rLL)  =>  d sLL / d rLL = 0.5 isLL
     rLLb += sLLb * 0.5 * isLL;
     rRRb += sRRb * 0.5 * isRR;
     rLLb += isLLb * (-0.5) * isLL * isLL * isLL;
     rRRb += isRRb * (-0.5) * isRR * isRR * isRR;
-    // eLL = eLLn iL
-    iLb += eLLb * eLLn;
-    iRb += eRRb * eRRn;
-    {
-        const double nb = eLLb * iL;  // eLLn = A.E suL + PTT SM - A.pT A.un + bn (wA - sbLL)
-        Ab.E += nb * suL;
-        double suLb_e = nb * A.E;
-        PTTb += nb * SM;
-        SMb += nb * PTT;
-        Ab.pT -= nb * A.un;
-        Ab.un -= nb * A.pT;
-        bnb += nb * (wA - sbLL);
-        const double wAb = nb * bn;
-        sbLLb -= nb * bn;
-        Ab.un += wAb * A.bn;
-        Ab.bn += wAb * A.un;
-        Ab.ut += wAb * A.bt;
-        Ab.bt += wAb * A.ut;
-        // suL adjoint accumulated below
-        SLb += suLb_e;
-        Ab.un -= suLb_e;
-    }
-    {
-        const double nb = eRRb * iR;
-        Bb.E += nb * suR;
-        const double suRb_e = nb * B.E;
-        PTTb += nb * SM;
-        SMb += nb * PTT;
-        Bb.pT -= nb * B.un;
-        Bb.un -= nb * B.pT;
-        bnb += nb * (wB - sbRR);
-        const double wBb = nb * bn;
-        sbRRb -= nb * bn;
-        Bb.un += wBb * B.bn;
-        Bb.bn += wBb * B.un;
-        Bb.ut += wBb * B.bt;
-        Bb.bt += wBb * B.ut;
-        SRb += suRb_e;
-        Bb.un -= suRb_e;
-    }
-    // sbLL = wLL bzL + vLL btL + SMbn
-    wLLb += sbLLb * bzL;
-    bzLb += sbLLb * wLL;
-    vLLb += sbLLb * btL;
-    btLb += sbLLb * vLL;
-    SMbnb += sbLLb;
-    wRRb += sbRRb * bzR;
-    bzRb += sbRRb * wRR;
-    vRRb += sbRRb * btR;
-    btRb += sbRRb * vRR;
-    SMbnb += sbRRb;
     // SMbn = SM bn
     SMb += SMbnb * bn;
     bnb += SMbnb * SM;
@@ -576,7 +479,7 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
     if (gL) {
         // vLL = A.ut - cL A.bt ; wLL = -cL A.bz ; btL = A.bt dL ; bzL = A.bz dL
         Ab.ut += vLLb;
-        double cLb = -vLLb * A.bt - wLLb * A.bz;
+        const double cLb = -vLLb * A.bt - wLLb * A.bz;
         Ab.bt += -vLLb * cL + btLb * dL;
         Ab.bz += -wLLb * cL + bzLb * dL;
         const double dLb = btLb * A.bt + bzLb * A.bz;
@@ -606,7 +509,7 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
     }
     if (gR) {
         Bb.ut += vRRb;
-        double cRb = -vRRb * B.bt - wRRb * B.bz;
+        const double cRb = -vRRb * B.bt - wRRb * B.bz;
         Bb.bt += -vRRb * cR + btRb * dR;
         Bb.bz += -wRRb * cR + bzRb * dR;
         const double dRb = btRb * B.bt + bzRb * B.bz;
@@ -645,8 +548,8 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
         SRb += dRb;
         SMb -= dRb;
     }
-    // bn = bnn iS, bt = btn iS, bz = bzn iS
-    double iSb = bnb * bnn + btb * btn + bzb * bzn;
+    // bn = bnn iS (the star bt, bz of the HLLC-MHD branch are not used by HLLD)
+    const double iSb = bnb * bnn;
     {
         const double nb = bnb * iS;  // bnn = SR B.bn - SL A.bn
         SRb += nb * B.bn;
@@ -654,7 +557,6 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
         SLb -= nb * A.bn;
         Ab.bn -= nb * SL;
     }
-    // (bt, bz are not used by HLLD beyond the HLLC-MHD branch: btb = bzb = 0 here)
     // iS = 1 / (SR - SL)
     {
         const double db = -iSb * iS * iS;
@@ -662,10 +564,14 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
         SLb -= db;
     }
     // UU = max(|SL|, |SR|)
-    if (UUR) SRb += UUb * (lt_zero(SR) ? -1.0 : 1.0);
-    else SLb += UUb * (lt_zero(SL) ? -1.0 : 1.0);
+    {
+        const double Sx = UUR ? SR : SL;
+        const double t = lt_zero(Sx) ? from_bits(bits(UUb) ^ (long long)0x8000000000000000ULL)
+                                     : UUb;  // sign(Sx) UUb on the integer pipe
+        add_to(UUR, SRb, SLb, t);
+    }
     // PTT = PTTn iden ; SM = SMn iden
-    double idenb = PTTb * PTTn + SMb * SMn;
+    const double idenb = PTTb * PTTn + SMb * SMn;
     {
         const double nb = PTTb * iden;  // PTTn = mL mR (B.un - A.un) + mR A.pT - mL B.pT
         mLb += nb * (mR * (B.un - A.un) - B.pT);
@@ -692,20 +598,93 @@ __device__ void hlld_vjp(const double* qa, const double* qb, const double* Fb,
     }
     // mL = A.r suL, mR = B.r suR ; suL = SL - A.un ; suR = SR - B.un
     Ab.r += mLb * suL;
-    double suLb = mLb * A.r;
+    const double suLb = mLb * A.r;
     Bb.r += mRb * suR;
-    double suRb = mRb * B.r;
+    const double suRb = mRb * B.r;
     SLb += suLb;
     Ab.un -= suLb;
     SRb += suRb;
     Bb.un -= suRb;
     // SL = uminN - cmax ; SR = umaxN + cmax
-    double cmaxb = -SLb + SRb;
+    const double cmaxb = SRb - SLb;
     if (minA) Ab.un += SLb; else Bb.un += SLb;
     if (maxB) Bb.un += SRb; else Ab.un += SRb;
-    if (cfB) Bb.cf += cmaxb; else Ab.cf += cmaxb;
-    side_rev(A, Ab, P, qa_b);
-    side_rev(B, Bb, P, qb_b);
+
+    // ---- the K side's base flux and energy ----------------------------------------------
+    {
+        // F7 = un bz ; F6 = un bt - ut bn
+        kun += Fbz * Kbz;
+        kbz += Fbz * Kun;
+        kun += Fbt * Kbt;
+        kbt += Fbt * Kun;
+        kut -= Fbt * Kbn;
+        kbn -= Fbt * Kut;
+        // F4 = (E + pT) un - bn (ut bt + un bn)
+        const double w = fma(Kut, Kbt, Kun * Kbn);
+        kE += Fe * Kun;
+        kpT += Fe * Kun;
+        kun += Fe * (KE + KpT);
+        kbn -= Fe * w;
+        const double wb = -Fe * Kbn;
+        kut += wb * Kbt;
+        kbt += wb * Kut;
+        kun += wb * Kbn;
+        kbn += wb * Kun;
+        // F0 = r un ; F1 = F0 un + pT - bn^2 ; F2 = F0 ut - bn bt
+        const double F0 = Kr * Kun;
+        const double F0b = fma(Fmt, Kut, fma(Fmn, Kun, Fm));
+        kut += Fmt * F0;
+        kbn -= Fmt * Kbt;
+        kbt -= Fmt * Kbn;
+        kun += Fmn * F0;
+        kpT += Fmn;
+        kbn -= 2.0 * Fmn * Kbn;
+        kr += F0b * Kun;
+        kun += F0b * Kr;
+        // E = p inv_gm1 + 0.5 (r (un^2 + ut^2) + bb)
+        const double kinb = 0.5 * kE;
+        kr += kinb * vsq;
+        kun += kinb * 2.0 * Kr * Kun;
+        kut += kinb * 2.0 * Kr * Kut;
+        add_to(takeL, Ab.r, Bb.r, kr);
+        add_to(takeL, Ab.un, Bb.un, kun);
+        add_to(takeL, Ab.ut, Bb.ut, kut);
+        add_to(takeL, Ab.bn, Bb.bn, kbn);
+        add_to(takeL, Ab.bt, Bb.bt, kbt);
+        add_to(takeL, Ab.bz, Bb.bz, kbz);
+        add_to(takeL, Ab.pT, Bb.pT, kpT);
+        // the side's p and bb adjoints are still zero: assign
+        const double kp = kE * P.inv_gm1;
+        Ab.p = takeL ? kp : 0.0;
+        Bb.p = takeL ? 0.0 : kp;
+        Ab.bb = takeL ? kinb : 0.0;
+        Bb.bb = takeL ? 0.0 : kinb;
+    }
+    // ---- the fast speed of the side of max(cf) ------------------------------------------
+    {
+        const double Ccf = cfB ? B.cf : A.cf, Crs = cfB ? B.rs : A.rs;
+        const double Crq = cfB ? B.rq : A.rq, Ca = cfB ? B.a : A.a, Cgp = cfB ? B.gp : A.gp;
+        const double Cbn2 = cfB ? B.bn2 : A.bn2, Cdisc = cfB ? B.disc : A.disc;
+        // cf = X rsqrt(X r) = sqrt(X / r): d/dX = 0.5 rs, d/dr = -0.5 cf / r = -0.5 cf^2 rs
+        const double Xb = cmaxb * 0.5 * Crs;
+        const double rb = -0.5 * cmaxb * (Ccf * Ccf) * Crs;
+        // X = 0.5 (a + sq), sq = sqrt(disc), disc = a^2 - 4 gp bn2 (clamped at 0)
+        double ab = 0.5 * Xb, gpb = 0.0, bn2b = 0.0;
+        if ((bits(Cdisc) << 1) != 0) {
+            const double discb = (0.5 * Xb) * 0.5 * Crq;
+            ab = fma(discb * 2.0, Ca, ab);
+            gpb = -discb * 4.0 * Cbn2;
+            bn2b = -discb * 4.0 * Cgp;
+        }
+        gpb += ab;  // a = gp + bb
+        add_to(!cfB, Ab.r, Bb.r, rb);
+        add_to(!cfB, Ab.p, Bb.p, gpb * P.gamma);
+        add_to(!cfB, Ab.bb, Bb.bb, ab);
+        Ab.bn2 = cfB ? 0.0 : bn2b;
+        Bb.bn2 = cfB ? bn2b : 0.0;
+    }
+    side_tail(A, Ab, qa_b);
+    side_tail(B, Bb, qb_b);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -810,7 +789,7 @@ __global__ void __launch_bounds__(FBX * FBY) adj_face_kernel(Params P, CPlanes U
                           isx ? qa[4] : qa[5], isx ? qa[5] : qa[4], qa[6]};
     const double lb[7] = {qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2],
                           isx ? qb[4] : qb[5], isx ? qb[5] : qb[4], qb[6]};
-    double lab[7] = {0, 0, 0, 0, 0, 0, 0}, lbb[7] = {0, 0, 0, 0, 0, 0, 0};
+    double lab[7], lbb[7];
     hlld_vjp(la, lb, Fb, P, lab, lbb);
     // back to field order (rho, p, vx, vy, bx, by, bz)
     const double gab[7] = {lab[0], lab[1], isx ? lab[2] : lab[3], isx ? lab[3] : lab[2],

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
         side(B, qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], isx ? qb[4] : qb[5],
              isx ? qb[5] : qb[4], qb[6], P);
         double UU;
-        const FluxM<double> F = hlld_local(A, B, GD_METHOD_HLLD, UU);
+        const FluxM<double> F = hlld_local(A, B, GD_METHOD_HLLD, P, UU);
         if (isx) {
             double* fo = fx + ly * (TX + 1) + lx;
             fo[0 * NFX] = F.m;

@@ -232,7 +232,7 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         side(B, qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], isx ? qb[4] : qb[5],
              isx ? qb[5] : qb[4], qb[6], P);
         T UU;
-        const FluxM<T> F = hlld_local(A, B, P.method, UU);
+        const FluxM<T> F = hlld_local(A, B, P.method, P, UU);
         if (isx) {
             T* fo = fx + ly * (TX + 1) + lx;
             constexpr int st = TY * (TX + 1);

@@ -28,11 +28,11 @@ struct FluxM {
     T m, mn, mt, e, bn, bt, bz;  // mass, normal / tangential momentum, energy, field
 };
 
-// One side of the face in the local frame (un normal, ut in-plane tangential, uz = 0).
+// One side of the face in the local frame (un normal, ut in-plane tangential, uz = 0): what
+// the wave speeds and the star states need from both sides.
 template <class T>
 struct Side {
-    T r, p, un, ut, bn, bt, bz, bb, pT, E, cf;
-    T F0, F1, F2, F4, F6, F7;
+    T r, p, un, ut, bn, bt, bz, bb, pT, cf;
 };
 
 template <class T>
@@ -42,19 +42,47 @@ __device__ __forceinline__ void side(Side<T>& S, T r, T p, T un, T ut, T bn, T b
     const T bn2 = bn * bn;
     S.bb = fma(bz, bz, fma(bt, bt, bn2));
     S.pT = fma(0.5, S.bb, p);
-    S.E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(un, un, ut * ut), S.bb));
     const T gp = P.gamma * p;
     const T a = gp + S.bb;
     T disc = fma(a, a, -4.0 * gp * bn2);
     disc = le_zero(disc) ? cst<T>(0.0) : disc;
     const T X = 0.5 * (a + sqrt_fast(disc));  // rho cf^2
     S.cf = X * rsqrt_fast(X * r);              // sqrt(X / r)
-    S.F0 = r * un;
-    S.F1 = fma(S.F0, un, S.pT - bn2);
-    S.F2 = fma(S.F0, ut, -bn * bt);
-    S.F4 = fma(S.E + S.pT, un, -bn * fma(ut, bt, un * bn));
-    S.F6 = fma(un, bt, -ut * bn);
-    S.F7 = un * bz;
+}
+
+// a side's total energy and physical flux (mass, normal / tangential momentum, energy,
+// tangential and z field); HLLD needs them for the upwind side only
+template <class T>
+struct SideF {
+    T E, F0, F1, F2, F4, F6, F7;
+};
+
+template <class T>
+__device__ __forceinline__ void side_flux(SideF<T>& F, const Side<T>& S, const Params& P) {
+    F.E = fma(S.p, P.inv_gm1, 0.5 * fma(S.r, fma(S.un, S.un, S.ut * S.ut), S.bb));
+    F.F0 = S.r * S.un;
+    F.F1 = fma(F.F0, S.un, S.pT - S.bn * S.bn);
+    F.F2 = fma(F.F0, S.ut, -S.bn * S.bt);
+    F.F4 = fma(F.E + S.pT, S.un, -S.bn * fma(S.ut, S.bt, S.un * S.bn));
+    F.F6 = fma(S.un, S.bt, -S.ut * S.bn);
+    F.F7 = S.un * S.bz;
+}
+
+// field-by-field select of one side (selects, no arithmetic)
+template <class T>
+__device__ __forceinline__ Side<T> pick(bool first, const Side<T>& A, const Side<T>& B) {
+    Side<T> K;
+    K.r = first ? A.r : B.r;
+    K.p = first ? A.p : B.p;
+    K.un = first ? A.un : B.un;
+    K.ut = first ? A.ut : B.ut;
+    K.bn = first ? A.bn : B.bn;
+    K.bt = first ? A.bt : B.bt;
+    K.bz = first ? A.bz : B.bz;
+    K.bb = first ? A.bb : B.bb;
+    K.pT = first ? A.pT : B.pT;
+    K.cf = first ? A.cf : B.cf;
+    return K;
 }
 
 __device__ __forceinline__ double sgn_select(double v, int idbn) {
@@ -66,10 +94,12 @@ __device__ __forceinline__ Dual sgn_select(Dual v, int idbn) {
     return idbn == 0 ? Dual{0.0, 0.0} : (idbn < 0 ? -v : v);
 }
 
-// HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = max(|SL|, |SR|).
+// HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = max(|SL|, |SR|).  The energy and the
+// physical flux are formed for the sides that use them: both for HLLC-MHD (its HLL state of
+// the fan), the upwind side K alone for HLLD, whose star energy is likewise K's alone.
 template <class T>
 __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& B, int method,
-                                               T& UU) {
+                                               const Params& P, T& UU) {
     const T uminN = dmin(A.un, B.un);
     const T umaxN = dmax(A.un, B.un);
     const T cmax = max_nonneg(A.cf, B.cf);
@@ -82,23 +112,32 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
     UU = max_nonneg(dabs(SL), dabs(SR));
     const T iS = rcp_fast(SR - SL);
     const T bn = fma(SR, B.bn, -SL * A.bn) * iS;
-    const T bt = (fma(SR, B.bt, -SL * A.bt) + (A.F6 - B.F6)) * iS;
-    const T bz = (fma(SR, B.bz, -SL * A.bz) + (A.F7 - B.F7)) * iS;
     const T iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
     const T rLL = mL * iL, rRR = mR * iR;
 
     FluxM<T> F;
     if (method == GD_METHOD_HLLC_MHD) {
+        SideF<T> FA, FB;
+        side_flux(FA, A, P);
+        side_flux(FB, B, P);
+        const T bt = (fma(SR, B.bt, -SL * A.bt) + (FA.F6 - FB.F6)) * iS;
+        const T bz = (fma(SR, B.bz, -SL * A.bz) + (FA.F7 - FB.F7)) * iS;
         const bool takeL = ge_zero(SL) || ge_zero(SM);
-        const Side<T>& K = takeL ? A : B;
+        const Side<T> K = pick(takeL, A, B);
+        const T KE = takeL ? FA.E : FB.E;
         const T S = takeL ? SL : SR;
         const bool star = takeL ? lt_zero(SL) : gt_zero(SR);
-        F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
+        F.m = takeL ? FA.F0 : FB.F0;
+        F.mn = takeL ? FA.F1 : FB.F1;
+        F.mt = takeL ? FA.F2 : FB.F2;
+        F.e = takeL ? FA.F4 : FB.F4;
+        F.bt = takeL ? FA.F6 : FB.F6;
+        F.bz = takeL ? FA.F7 : FB.F7;
         if (star) {
             // HLL state of the fan (Gas_Dinamic.cu:1145-1149); mom_z: U = 0, F = -bn bz
-            const T UZ0 = (fma(SR, B.r, -SL * A.r) + (A.F0 - B.F0)) * iS;
-            const T UZ1 = (fma(SR, B.r * B.un, -SL * A.r * A.un) + (A.F1 - B.F1)) * iS;
-            const T UZ2 = (fma(SR, B.r * B.ut, -SL * A.r * A.ut) + (A.F2 - B.F2)) * iS;
+            const T UZ0 = (fma(SR, B.r, -SL * A.r) + (FA.F0 - FB.F0)) * iS;
+            const T UZ1 = (fma(SR, B.r * B.un, -SL * A.r * A.un) + (FA.F1 - FB.F1)) * iS;
+            const T UZ2 = (fma(SR, B.r * B.ut, -SL * A.r * A.ut) + (FA.F2 - FB.F2)) * iS;
             const T UZ3 = (B.bn * B.bz - A.bn * A.bz) * iS;
             const T iU0 = rcp_fast(UZ0);
             const T vS = UZ2 * iU0;
@@ -107,12 +146,12 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
             const T sbvK = fma(K.un, K.bn, K.ut * K.bt);
             const T iK = takeL ? iL : iR;
             const T suK = takeL ? suL : suR;
-            const T eK = (fma(K.E, suK, fma(ptz, SM, -K.pT * K.un)) + bn * (sbvK - sbvz)) * iK;
+            const T eK = (fma(KE, suK, fma(ptz, SM, -K.pT * K.un)) + bn * (sbvK - sbvz)) * iK;
             const T rK = takeL ? rLL : rRR;
             F.m = fma(S, rK - K.r, F.m);
             F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
             F.mt = fma(S, fma(rK, vS, -K.r * K.ut), F.mt);
-            F.e = fma(S, eK - K.E, F.e);
+            F.e = fma(S, eK - KE, F.e);
             F.bt = fma(S, bt - K.bt, F.bt);
             F.bz = fma(S, bz - K.bz, F.bz);
         }
@@ -149,12 +188,6 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
             }
         }
         const T SMbn = SM * bn;
-        const T sbLL = fma(wLL, bzL, fma(vLL, btL, SMbn));
-        const T sbRR = fma(wRR, bzR, fma(vRR, btR, SMbn));
-        const T eLL = (fma(A.E, suL, fma(PTT, SM, -A.pT * A.un)) +
-                       bn * (fma(A.un, A.bn, A.ut * A.bt) - sbLL)) * iL;
-        const T eRR = (fma(B.E, suR, fma(PTT, SM, -B.pT * B.un)) +
-                       bn * (fma(B.un, B.bn, B.ut * B.bt) - sbRR)) * iR;
         const T isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
         const T sLL = rLL * isLL, sRR = rRR * isRR;
         const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;  // |bn| > 1e-6
@@ -167,19 +200,26 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
         int level;
         if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
         else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
-        const Side<T>& K = takeL ? A : B;
-        F.m = K.F0; F.mn = K.F1; F.mt = K.F2; F.e = K.F4; F.bt = K.F6; F.bz = K.F7;
+        const Side<T> K = pick(takeL, A, B);
+        SideF<T> KF;
+        side_flux(KF, K, P);
+        F.m = KF.F0; F.mn = KF.F1; F.mt = KF.F2; F.e = KF.F4; F.bt = KF.F6; F.bz = KF.F7;
         if (level >= 1) {
             const T S = takeL ? SL : SR;
+            const T su = takeL ? suL : suR;
+            const T iK = takeL ? iL : iR;
             const T rK = takeL ? rLL : rRR;
             const T vK = takeL ? vLL : vRR;
-            const T eK = takeL ? eLL : eRR;
+            const T wK = takeL ? wLL : wRR;
             const T btK = takeL ? btL : btR;
             const T bzK = takeL ? bzL : bzR;
+            const T sbK = fma(wK, bzK, fma(vK, btK, SMbn));
+            const T eK = (fma(KF.E, su, fma(PTT, SM, -K.pT * K.un)) +
+                          bn * (fma(K.un, K.bn, K.ut * K.bt) - sbK)) * iK;
             F.m = fma(S, rK - K.r, F.m);
             F.mn = fma(S, fma(rK, SM, -K.r * K.un), F.mn);
             F.mt = fma(S, fma(rK, vK, -K.r * K.ut), F.mt);
-            F.e = fma(S, eK - K.E, F.e);
+            F.e = fma(S, eK - KF.E, F.e);
             F.bt = fma(S, btK - K.bt, F.bt);
             F.bz = fma(S, bzK - K.bz, F.bz);
             if (level == 2) {
@@ -192,7 +232,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
                 const T bz3 = fma(s2, wRR - wLL, fma(sLL, bzR, sRR * bzL)) * is;
                 const T sb3 = fma(wL3, bz3, fma(vL3, bt3, SMbn));
                 const T sK = takeL ? -sLL : sRR;
-                const T e3 = fma(sgn_select(sK, idbn), (takeL ? sbLL : sbRR) - sb3, eK);
+                const T e3 = fma(sgn_select(sK, idbn), sbK - sb3, eK);
                 const T S2 = takeL ? SLL : SRR;
                 F.mt = fma(S2, rK * (vL3 - vK), F.mt);
                 F.e = fma(S2, e3 - eK, F.e);
