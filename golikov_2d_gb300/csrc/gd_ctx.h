@@ -13,9 +13,11 @@ namespace gd {
 // work buffers of the reverse and tangent sweeps.
 // gd_step_host: the two copy streams, the events of the band pipeline and the AoS staging
 // of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
-constexpr int kMaxBands = 32;
+constexpr int kMaxBands = 64;
+constexpr int kCompStreams = 3;  // the caller's stream and two more
 struct HostPipe {
-    cudaStream_t up = nullptr, down = nullptr, comp = nullptr, edge = nullptr;
+    cudaStream_t up = nullptr, down = nullptr, edge = nullptr;
+    cudaStream_t comp[kCompStreams - 1] = {};
     cudaEvent_t start = nullptr, down_done = nullptr, comp_done = nullptr, edge_done = nullptr;
     cudaEvent_t ev_up[kMaxBands] = {}, ev_out[kMaxBands] = {};
     double* aos_in = nullptr;

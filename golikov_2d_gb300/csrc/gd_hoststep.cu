@@ -46,10 +46,16 @@ cudaError_t pipe_create(gd_ctx* ctx) {
     gd::HostPipe* p = new (std::nothrow) gd::HostPipe();
     if (!p) return cudaErrorMemoryAllocation;
     ctx->pipe = p;
-    HS_TRY(cudaStreamCreateWithFlags(&p->up, cudaStreamNonBlocking));
-    HS_TRY(cudaStreamCreateWithFlags(&p->down, cudaStreamNonBlocking));
-    HS_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
-    HS_TRY(cudaStreamCreateWithFlags(&p->edge, cudaStreamNonBlocking));
+    // The copy streams' conversion kernels and the Hancock edge launch are short and gate
+    // the next band's step or the downloads: at the highest priority their blocks are
+    // dispatched ahead of the queued blocks of the band steps (at equal priority the edge
+    // launch waited behind all of them and every download with it).
+    int prio_low = 0, prio_high = 0;
+    HS_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    HS_TRY(cudaStreamCreateWithPriority(&p->up, cudaStreamNonBlocking, prio_high));
+    HS_TRY(cudaStreamCreateWithPriority(&p->down, cudaStreamNonBlocking, prio_high));
+    HS_TRY(cudaStreamCreateWithPriority(&p->edge, cudaStreamNonBlocking, prio_high));
+    for (cudaStream_t& c : p->comp) HS_TRY(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done, &p->edge_done})
         HS_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int k = 0; k < gd::kMaxBands; ++k) {
@@ -125,12 +131,12 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     const int T = hk ? (M - 4 + TY - 1) / TY : (M + TY - 1) / TY;  // tile (block) rows
     const int nx = hk ? (N - 4 + TX - 1) / TX : (N + TX - 1) / TX;  // tiles per tile row
     // Smaller bands shorten the pipeline's fill (two bands up before the first step) and
-    // drain (one band down after the last); each band should still fill the GPU for a few
-    // waves: at least 2 waves of the two resident CTAs per SM the kernels have; 2 to
-    // kMaxBands bands of >= 2 block rows.
+    // drain (one band down after the last).  The bands are stepped on kCompStreams streams
+    // in turn, so a band of half a wave of the kernels' resident blocks (two per SM) keeps
+    // about one and a half waves in flight; 2 to kMaxBands bands of >= 2 block rows.
     int sms = 0;
     HS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    const long long per_band_min = (hk ? 4LL : 2LL) * 2 * (sms > 0 ? sms : 1);
+    const long long per_band_min = sms > 0 ? sms : 1;
     int B = (int)(((long long)nx * T) / per_band_min);
     if (B > gd::kMaxBands) B = gd::kMaxBands;
     if (B > T / 2) B = T / 2;
@@ -173,17 +179,33 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
                          cudaMemcpyHostToDevice, p->up));
         HS_TRY(to_planes(ctx, wrap_rows, p->up));
     }
-    for (int k = 0; k < B; ++k) {
-        const Rows r = band_rows_up(k);
-        HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, r, nf, cudaMemcpyHostToDevice,
-                         p->up));
-        HS_TRY(to_planes(ctx, r, p->up));
-        HS_TRY(cudaEventRecord(p->ev_up[k], p->up));
-    }
+    int n_up = 0;  // bands whose upload is enqueued
+    auto enqueue_up = [&](int upto) -> cudaError_t {
+        for (; n_up <= upto && n_up < B; ++n_up) {
+            const Rows r = band_rows_up(n_up);
+            HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, r, nf,
+                             cudaMemcpyHostToDevice, p->up));
+            HS_TRY(to_planes(ctx, r, p->up));
+            HS_TRY(cudaEventRecord(p->ev_up[n_up], p->up));
+        }
+        return cudaSuccess;
+    };
+    // down stream: band k's result to AoS and to the host while later bands are stepped
+    auto enqueue_down = [&](int k) -> cudaError_t {
+        HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
+        if (hk) HS_TRY(cudaStreamWaitEvent(p->down, p->edge_done, 0));
+        HS_TRY(from_planes(ctx, band_rows(k), p->down));
+        return copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
+                         cudaMemcpyDeviceToHost, p->down);
+    };
+    // The host enqueues in the order the GPU needs the work: two bands up, then per band the
+    // next upload, the step and the download, so the first step is queued after two bands'
+    // uploads rather than after all of them (each band is a dozen API calls).
+    HS_TRY(enqueue_up(1));
     // the step on band k once bands k and k + 1 are planes (band k - 1, and the seam rows,
-    // came before), bands alternating between the caller's stream and a second compute
-    // stream: the bands write disjoint rows and share one rotation ticket, so the next band's
-    // blocks may start while the last wave of this one drains
+    // came before), bands taken in turn by the caller's stream and kCompStreams - 1 more:
+    // the bands write disjoint rows and share one rotation ticket, so later bands' blocks
+    // may start while the last wave of this one drains
     Params P = ctx->P;
     unsigned int nblocks = (unsigned int)(nx * T);
     if (hk) {
@@ -192,18 +214,14 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         nblocks = gd::hancock_fast_blocks(P, 0, M, 1);
         for (int k = 0; k < B; ++k)
             nblocks += gd::hancock_fast_blocks(P, row_bound(k), row_bound(k + 1), 2);
-        HS_TRY(cudaStreamWaitEvent(p->edge, p->ev_up[B - 1], 0));
-        HS_TRY(gd::launch_hancock_fast_rows(P, gd_ctx::cplanes(ctx->planes(ctx->cur)),
-                                            ctx->planes(1 - ctx->cur), &ctx->sc->T_do,
-                                            &ctx->sc->T_bits, ctx->sc, ctx->sc, 0, M, nblocks, 1,
-                                            p->edge));
-        HS_TRY(cudaEventRecord(p->edge_done, p->edge));
     }
     P.tile_nblocks = nblocks;
     const CPlanes in = gd_ctx::cplanes(ctx->planes(ctx->cur));
     const Planes out = ctx->planes(1 - ctx->cur);
     for (int k = 0; k < B; ++k) {
-        const cudaStream_t cs = (k & 1) ? p->comp : st;
+        HS_TRY(enqueue_up(k + 2));
+        const int si = k % gd::kCompStreams;
+        const cudaStream_t cs = si == 0 ? st : p->comp[si - 1];
         HS_TRY(cudaStreamWaitEvent(cs, p->ev_up[k + 1 < B ? k + 1 : k], 0));
         int t0, t1;
         band_tiles(k, &t0, &t1);
@@ -226,15 +244,21 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         else
             HS_TRY(gd::launch_mhd_fast(P, in, out, &ctx->sc->T_do, Tb, ctx->sc, ctx->sc, 0, cs));
         HS_TRY(cudaEventRecord(p->ev_out[k], cs));
-        // down stream: band k's result to AoS and to the host while later bands are stepped
-        HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
-        if (hk) HS_TRY(cudaStreamWaitEvent(p->down, p->edge_done, 0));
-        HS_TRY(from_planes(ctx, band_rows(k), p->down));
-        HS_TRY(copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
-                         cudaMemcpyDeviceToHost, p->down));
+        if (!hk) HS_TRY(enqueue_down(k));
     }
-    HS_TRY(cudaEventRecord(p->comp_done, p->comp));
-    HS_TRY(cudaStreamWaitEvent(st, p->comp_done, 0));
+    if (hk) {
+        // every upload is enqueued: the edge launch (it reads all of them), then the
+        // downloads, each of which waits for it
+        HS_TRY(cudaStreamWaitEvent(p->edge, p->ev_up[B - 1], 0));
+        HS_TRY(gd::launch_hancock_fast_rows(P, in, out, &ctx->sc->T_do, &ctx->sc->T_bits,
+                                            ctx->sc, ctx->sc, 0, M, nblocks, 1, p->edge));
+        HS_TRY(cudaEventRecord(p->edge_done, p->edge));
+        for (int k = 0; k < B; ++k) HS_TRY(enqueue_down(k));
+    }
+    for (cudaStream_t c : p->comp) {
+        HS_TRY(cudaEventRecord(p->comp_done, c));
+        HS_TRY(cudaStreamWaitEvent(st, p->comp_done, 0));
+    }
     if (hk) HS_TRY(cudaStreamWaitEvent(st, p->edge_done, 0));
     HS_TRY(cudaEventRecord(p->down_done, p->down));
     HS_TRY(cudaStreamWaitEvent(st, p->down_done, 0));
@@ -257,7 +281,8 @@ void pipe_free(gd_ctx* ctx) {
     }
     if (p->up) cudaStreamDestroy(p->up);
     if (p->down) cudaStreamDestroy(p->down);
-    if (p->comp) cudaStreamDestroy(p->comp);
+    for (cudaStream_t c : p->comp)
+        if (c) cudaStreamDestroy(c);
     if (p->edge) cudaStreamDestroy(p->edge);
     delete p;
     ctx->pipe = nullptr;

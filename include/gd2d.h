@@ -200,8 +200,9 @@ gd_status gd_advance_to(gd_ctx* ctx, double t_end, long long max_steps, int use_
  * layout (as gd_import / gd_export with is_host = 1).  Same result, dt and time as
  * gd_import + gd_advance(1) + gd_export.  With the lagged dt and pinned (page-locked) host
  * buffers the grid is moved in bands of tile rows, each band's upload, step and download
- * overlapping the others' on two copy streams and `stream`; otherwise (GD_DT_CURRENT,
- * pageable buffers, grids of fewer than four tile rows) the three calls run in turn.
+ * overlapping the others' on two copy streams, `stream` and two more compute streams;
+ * otherwise (GD_DT_CURRENT, pageable buffers, grids of fewer than four tile rows) the three
+ * calls run in turn.
  * Returns after the result is in s2, u2, b2. */
 gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u, const double* b,
                        double* s2, double* u2, double* b2, gd_stream stream);
