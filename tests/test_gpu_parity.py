@@ -136,3 +136,40 @@ def test_parity_tiny_grids(cuda, oracle_lib, N, M, physics):
         assert np.array_equal(sg, so) and np.array_equal(ug, uo), bc
         if b is not None:
             assert np.array_equal(bg, bo), bc
+
+
+@pytest.mark.parametrize("case", ["sod256", "ot128", "kh256"])
+def test_run_checksums(cuda, case):
+    """Whole runs against the committed checksums (tests/golden/checksums.npz, from the
+    oracle): parity mode reproduces the state hash, dt and time after 1, 10 and N steps bit
+    for bit; fast mode reproduces every field's sum and L1 norm, and dt and time, to 1e-9
+    relative (the bound on N steps of the full protocol)."""
+    from golden.make_checksums import case_state, digest, field_sums
+    gz = golden("checksums.npz")
+    steps = [int(k) for k in gz[f"{case}_steps"]]
+    for mode in (g.MODE_PARITY, g.MODE_FAST):
+        cfg, s, u, b, n = case_state(case, gz)
+        cfg.mode = mode
+        sol = g.Solver(cfg)
+        sol.import_state(s, u, b)
+        sol.set_time(0.0, 0.0)
+        sol.init_dt()
+        done = 0
+        for i, k in enumerate(steps):
+            sol.advance(k - done)
+            done = k
+            s2, u2 = np.zeros_like(s), np.zeros_like(u)
+            b2 = None if b is None else np.zeros_like(b)
+            sol.export_state(s2, u2, b2)
+            st = sol.stats()
+            T_do, TT = gz[f"{case}_Tdo"][i], gz[f"{case}_TT"][i]
+            if mode == g.MODE_PARITY:
+                assert digest(s2, u2, b2) == str(gz[f"{case}_sha"][i]), k
+                assert st.dt == T_do and st.t == TT, k
+            else:
+                sm, l1 = field_sums(s2, u2, b2)
+                ref_l1 = gz[f"{case}_l1"][i]
+                assert np.all(np.abs(sm - gz[f"{case}_sum"][i]) <= 1e-9 * ref_l1), k
+                assert np.all(np.abs(l1 - ref_l1) <= 1e-9 * ref_l1), k
+                assert abs(st.dt - T_do) <= 1e-9 * T_do and abs(st.t - TT) <= 1e-9 * TT, k
+        sol.close()

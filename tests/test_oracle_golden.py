@@ -204,3 +204,20 @@ def test_hancock_schemes_differ_only_in_vy_slopes(oracle_lib):
     r2 = oracle_lib.step(gkr_grid(N, M, xmax, ymax, scheme=2), s, u, b, 2e-3)
     assert not np.array_equal(r1[1], r2[1])
 
+
+
+@pytest.mark.parametrize("case", ["sod256", "ot128", "kh256"])
+def test_benchmark_run_checksums(oracle_lib, case):
+    """Whole runs of the benchmark problems at reduced size (Sod 256^2 200 steps,
+    Orszag-Tang 128^2 and KH 256^2 100 steps): the oracle reproduces the committed state
+    hashes, field sums, L1 norms, dt and time after 1, 10 and N steps (checksums.npz,
+    written by tests/golden/make_checksums.py)."""
+    from golden.make_checksums import case_state, run_case
+    gz = golden("checksums.npz")
+    cfg, s, u, b, n = case_state(case, gz)
+    recs = run_case(oracle_lib, cfg, s, u, b, n)
+    assert [r[0] for r in recs] == list(gz[f"{case}_steps"])
+    for i, (k, sha, sm, l1, T_do, TT) in enumerate(recs):
+        assert sha == str(gz[f"{case}_sha"][i]), k
+        assert np.array_equal(sm, gz[f"{case}_sum"][i]) and np.array_equal(l1, gz[f"{case}_l1"][i])
+        assert T_do == gz[f"{case}_Tdo"][i] and TT == gz[f"{case}_TT"][i], k
