@@ -82,6 +82,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# FP64 operations per cell-update from one ncu capture of the kernel: FP64 pipe utilisation
+# (sm__pipe_fp64_cycles_active) x 2 ops/clk/SM x elapsed cycles x 152 SMs / cells
+OPS_SOURCE = ("ncu FP64 pipe utilisation x 2 ops/clk/SM x cycles x SMs / cells, "
+              "profiles/ncu_traffic.txt")
+
+
 def ncu_traffic(workload):
     """DRAM bytes per launch of the step kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
@@ -209,7 +215,7 @@ def fp64_roofline(g, workload, cells_per_s, torch):
         ach = per_cell * cells_per_s
         out.update({"ops_per_cell": per_cell, "achieved": ach, "frac": ach / pipe_peak_ops,
                     "frac_of_dfma_loop": ach / (probe / 2.0),
-                    "ops_source": "ncu sm__inst_executed_pipe_fp64, profiles/ncu_traffic.txt"})
+                    "ops_source": OPS_SOURCE})
     return out
 
 
@@ -668,8 +674,7 @@ def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792
                 pipe = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07e9
                 entry["fp64"] = {"ops_per_cell": ops, "achieved": ops * entry["value"],
                                  "pipe_peak": pipe, "frac": ops * entry["value"] / pipe,
-                                 "ops_source": "ncu sm__inst_executed_pipe_fp64, "
-                                               "profiles/ncu_traffic.txt"}
+                                 "ops_source": OPS_SOURCE}
             peak_gbs, kind = measured_peaks()
             ach = N * M * 7 * 16 / (ms * 1e-3) / 1e9
             entry["hbm"] = {"achieved": ach, "peak": peak_gbs, "unit": "GB/s",
