@@ -30,7 +30,8 @@ typedef enum {
     GD_ERR_INVALID_ARG = 1,  /* bad configuration or argument; nothing was launched      */
     GD_ERR_CUDA = 2,         /* a CUDA call failed; see gd_last_cuda_error()              */
     GD_ERR_NONPHYSICAL = 3,  /* non-finite state detected (gd_stats.nonfinite > 0)        */
-    GD_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up                        */
+    GD_ERR_TIMEOUT = 4,      /* reserved for a bounded device-side wait that gives up; no
+                                kernel here waits on another block, so none returns it    */
     GD_ERR_UNSUPPORTED = 5   /* combination not implemented                               */
 } gd_status;
 
