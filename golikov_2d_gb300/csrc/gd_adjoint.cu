@@ -168,7 +168,8 @@ __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params
     S.rq = rsqrt_fast(S.disc);
     const double sq = (bits(S.disc) << 1) == 0 ? 0.0 : S.disc * S.rq;
     const double X = 0.5 * (S.a + sq);
-    S.rs = rsqrt_fast(X * S.r);
+    // cf = sqrt_over(X, r) of the forward, keeping its 1/sqrt(X r) for the reverse
+    S.rs = rsqrt_times(X, S.r);
     S.cf = X * S.rs;
 }
 
@@ -256,8 +257,9 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
         vRR = B.ut; wRR = 0.0; btR = 0.0; bzR = 0.0;
     }
     const double SMbn = SM * bn;
-    const double isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
-    const double sLL = rLL * isLL, sRR = rRR * isRR;
+    double isLL, isRR, sLL, sRR;
+    rsqrt_and_sqrt(rLL, isLL, sLL);
+    rsqrt_and_sqrt(rRR, isRR, sRR);
     const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
     const double abn = dabs(bn);
     const double SLL = bnz ? fma(-abn, isLL, SM) : SM;

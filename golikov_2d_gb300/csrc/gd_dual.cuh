@@ -63,6 +63,19 @@ __device__ __forceinline__ Dual sqrt_fast(Dual x) {
 }
 
 // value-only predicates and selections (derivative follows the selected branch)
+// values exactly as the double versions (the tangent takes the forward's branches)
+__device__ __forceinline__ void rsqrt_and_sqrt(Dual x, Dual& ix, Dual& sx) {
+    double i, s;
+    rsqrt_and_sqrt(x.v, i, s);
+    ix = {i, -0.5 * x.d * i * i * i};
+    sx = {s, 0.5 * x.d * i};
+}
+__device__ __forceinline__ Dual sqrt_over(Dual a, Dual r) {
+    // d sqrt(a / r) = sqrt(a / r) / 2 (da / a - dr / r); 0 at a = 0
+    const double v = sqrt_over(a.v, r.v);
+    if ((bits(a.v) << 1) == 0) return {v, 0.0};
+    return {v, 0.5 * v * (a.d / a.v - r.d / r.v)};
+}
 __device__ __forceinline__ unsigned long long abs_bits(Dual x) { return abs_bits(x.v); }
 __device__ __forceinline__ bool le_zero(Dual x) { return le_zero(x.v); }
 __device__ __forceinline__ bool gt_zero(Dual x) { return gt_zero(x.v); }

@@ -47,8 +47,8 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
                                             const Params& P, double& UU) {
     const double g = P.gamma;
     const double gpL = g * pL, gpR = g * pR;
-    const double cL = gpL * rsqrt_fast(gpL * rL);  // sqrt(g p / rho)
-    const double cR = gpR * rsqrt_fast(gpR * rR);
+    const double cL = sqrt_over(gpL, rL);  // sqrt(g p / rho)
+    const double cR = sqrt_over(gpR, rR);
     const double aL = unL - cL, aR = unR - cR;
     const double bL = unL + cL, bR = unR + cR;
     const double SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
@@ -98,8 +98,8 @@ __device__ __forceinline__ FluxE hll_local(double rL, double pL, double unL, dou
                                            const Params& P, double& UU) {
     const double g = P.gamma;
     const double gpL = g * pL, gpR = g * pR;
-    const double cL = le_zero(rL) ? 0.0 : gpL * rsqrt_fast(gpL * rL);  // sqrt(g p / rho)
-    const double cR = le_zero(rR) ? 0.0 : gpR * rsqrt_fast(gpR * rR);
+    const double cL = le_zero(rL) ? 0.0 : sqrt_over(gpL, rL);  // sqrt(g p / rho)
+    const double cR = le_zero(rR) ? 0.0 : sqrt_over(gpR, rR);
     const double cm = max_nonneg(cL, cR);
     const double DL = dmin(unL, unR) - cm;
     const double DR = dmax(unL, unR) + cm;

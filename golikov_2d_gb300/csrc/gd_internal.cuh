@@ -178,9 +178,12 @@ __device__ __forceinline__ double rcp_fast(double x) {
     return fma(y, fma(e, e, e), y);
 }
 
-__device__ __forceinline__ double rsqrt_fast(double x) {
-    // x > 0 on the integer pipe: NaN, +-0, negative and out-of-range values all fall back
-    if (!in_f32_range(x) || !gt_zero(x)) return 1.0 / sqrt(x);
+// The fast reciprocal square root applies to x > 0 in the seeded range (tested on the
+// integer pipe); NaN, +-0, negative and out-of-range values take the correctly rounded path.
+__device__ __forceinline__ bool rsqrt_ok(double x) { return in_f32_range(x) && gt_zero(x); }
+
+// the seeded FP32 estimate of 1/sqrt(x) and one third-order Newton step; x as rsqrt_ok
+__device__ __forceinline__ double rsqrt_newton(double x) {
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
     const double y = widen_f32(r);
@@ -188,10 +191,40 @@ __device__ __forceinline__ double rsqrt_fast(double x) {
     return fma(y, e * fma(0.375, e, 0.5), y);
 }
 
+__device__ __forceinline__ double rsqrt_fast(double x) {
+    if (!rsqrt_ok(x)) return 1.0 / sqrt(x);
+    return rsqrt_newton(x);
+}
+
 __device__ __forceinline__ double sqrt_fast(double x) {
     // sqrt(x) = x * rsqrt(x), exact zero preserved (the +-0 test on the integer pipe)
     return (bits(x) << 1) == 0 ? 0.0 : x * rsqrt_fast(x);
 }
+
+// 1/sqrt(x) and sqrt(x) = x / sqrt(x) together; where the fast path does not apply, the
+// correctly rounded pair (x = 0: sqrt 0 and 1/sqrt inf, as the reference's sqrt(x))
+__device__ __forceinline__ void rsqrt_and_sqrt(double x, double& ix, double& sx) {
+    if (!rsqrt_ok(x)) {
+        sx = sqrt(x);
+        ix = 1.0 / sx;
+        return;
+    }
+    ix = rsqrt_newton(x);
+    sx = x * ix;
+}
+
+// 1/sqrt(a r), except 0 where a = +-0, for the product a * rsqrt(a r) = sqrt(a / r): the
+// zero test sits in the slow branch only, so the fast path is rsqrt_fast's
+__device__ __forceinline__ double rsqrt_times(double a, double r) {
+    const double x = a * r;
+    if (!rsqrt_ok(x)) return (bits(a) << 1) == 0 ? 0.0 : 1.0 / sqrt(x);
+    return rsqrt_newton(x);
+}
+
+// sqrt(a / r) (a sound or fast magnetosonic speed, a >= 0) as a * rsqrt(a r): a = 0 gives 0,
+// as the reference's sqrt(a / r) (the plain product would be 0 * inf); r = 0 gives inf and
+// r < 0 NaN, as there
+__device__ __forceinline__ double sqrt_over(double a, double r) { return a * rsqrt_times(a, r); }
 
 // isfinite(x) on the integer pipe: the exponent field is not all ones
 __device__ __forceinline__ bool finite_bits(double x) {

@@ -47,7 +47,7 @@ __device__ __forceinline__ void side(Side<T>& S, T r, T p, T un, T ut, T bn, T b
     T disc = fma(a, a, -4.0 * gp * bn2);
     disc = le_zero(disc) ? cst<T>(0.0) : disc;
     const T X = 0.5 * (a + sqrt_fast(disc));  // rho cf^2
-    S.cf = X * rsqrt_fast(X * r);              // sqrt(X / r)
+    S.cf = sqrt_over(X, r);                    // sqrt(X / r)
 }
 
 // a side's total energy and physical flux (mass, normal / tangential momentum, energy,
@@ -188,8 +188,9 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
             }
         }
         const T SMbn = SM * bn;
-        const T isLL = rsqrt_fast(rLL), isRR = rsqrt_fast(rRR);
-        const T sLL = rLL * isLL, sRR = rRR * isRR;
+        T isLL, isRR, sLL, sRR;
+        rsqrt_and_sqrt(rLL, isLL, sLL);
+        rsqrt_and_sqrt(rRR, isRR, sRR);
         const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;  // |bn| > 1e-6
         const T abn = dabs(bn);
         const T SLL = bnz ? fma(-abn, isLL, SM) : SM;
