@@ -46,7 +46,7 @@ EXPORTS = (
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
     "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
-    "gd_probe_fp64_peak", "gd_step_ref_static",
+    "gd_probe_fp64_peak", "gd_probe_faces", "gd_step_ref_static",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
@@ -141,6 +141,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_launch_count.restype = ll
     L.gd_launch_count.argtypes = [vp]
     L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
+    L.gd_probe_faces.argtypes = [i, i, d, i, ll, vp, vp, vp, vp, vp]
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
@@ -170,7 +171,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     for name in ("gd_create", "gd_destroy", "gd_get_config", "gd_step_ref", "gd_funk_time",
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
                  "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
-                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_step_ref_static",
+                 "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_probe_faces",
+                 "gd_step_ref_static",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
@@ -482,6 +484,20 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(self.lib.gd_batch_launch_count(self.handle))
+
+
+def probe_faces(physics: int, method: int, gamma: float, axis: int, L, R, stream=None):
+    """gd_probe_faces: the fast step's face solver on n faces.  L, R: contiguous float64 CUDA
+    tensors of shape (n, 4) for EULER or (n, 8) for MHD in the reference's face layouts;
+    returns (flux, speed) CUDA tensors of shape (n, 4 | 8) and (n,)."""
+    import torch
+    n = int(L.shape[0])
+    flux = torch.empty((n, L.shape[1]), dtype=torch.float64, device=L.device)
+    speed = torch.empty(n, dtype=torch.float64, device=L.device)
+    _check(load().gd_probe_faces(int(physics), int(method), float(gamma), int(axis), n,
+                                 L.data_ptr(), R.data_ptr(), flux.data_ptr(), speed.data_ptr(),
+                                 _stream_handle(stream)), "gd_probe_faces")
+    return flux, speed
 
 
 def probe_fp64_peak() -> float:

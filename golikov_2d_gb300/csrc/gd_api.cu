@@ -503,4 +503,27 @@ gd_status gd_probe_fp64_peak(double* flops_out) {
     return GD_OK;
 }
 
+gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long long n,
+                         const double* L, const double* R, double* flux, double* speed,
+                         gd_stream stream) {
+    if (physics != GD_EULER && physics != GD_MHD) return GD_ERR_INVALID_ARG;
+    if (physics == GD_EULER && method != GD_METHOD_HLL && method != GD_METHOD_HLLC)
+        return GD_ERR_INVALID_ARG;
+    if (physics == GD_MHD && method != GD_METHOD_HLLC_MHD && method != GD_METHOD_HLLD)
+        return GD_ERR_INVALID_ARG;
+    if (!(std::isfinite(gamma) && gamma > 1.0)) return GD_ERR_INVALID_ARG;
+    if ((axis != 0 && axis != 1) || n < 0 || n > (1LL << 36)) return GD_ERR_INVALID_ARG;
+    if (n > 0 && (!L || !R || !flux || !speed)) return GD_ERR_INVALID_ARG;
+    Params P{};
+    P.physics = physics;
+    P.method = method;
+    P.gamma = gamma;
+    P.gm1 = gamma - 1.0;
+    P.inv_gm1 = 1.0 / (gamma - 1.0);
+    const cudaStream_t st = (cudaStream_t)stream;
+    GD_CUDA(physics == GD_EULER ? gd::launch_euler_face_probe(P, n, axis, L, R, flux, speed, st)
+                                : gd::launch_mhd_face_probe(P, n, axis, L, R, flux, speed, st));
+    return GD_OK;
+}
+
 }  // extern "C"

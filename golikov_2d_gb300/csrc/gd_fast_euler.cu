@@ -518,4 +518,43 @@ cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, c
                       (grids, items, nitems, cur, dt_only, sc_override, ctas, st));
 }
 
+
+namespace {
+// One face per thread through the step's own face solver (hllc_local / hll_local): L, R are
+// n x 4 (rho, p, vx, vy); flux n x 4 (mass, energy, x momentum, y momentum), the reference's
+// HLLC_Aleksashov output order; speed n values max(|S_L|, |S_R|).  axis 0: normal +x.
+__global__ void euler_face_probe_kernel(Params P, long long n, int axis,
+                                        const double* __restrict__ L,
+                                        const double* __restrict__ R, double* flux,
+                                        double* speed) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = L + 4 * i;
+    const double* b = R + 4 * i;
+    const bool isx = axis == 0;
+    double UU;
+    const FluxE F =
+        P.method == GD_METHOD_HLL
+            ? hll_local(a[0], a[1], isx ? a[2] : a[3], isx ? a[3] : a[2], b[0], b[1],
+                        isx ? b[2] : b[3], isx ? b[3] : b[2], P, UU)
+            : hllc_local(a[0], a[1], isx ? a[2] : a[3], isx ? a[3] : a[2], b[0], b[1],
+                         isx ? b[2] : b[3], isx ? b[3] : b[2], P, UU);
+    double* o = flux + 4 * i;
+    o[0] = F.m;
+    o[1] = F.e;
+    o[2] = isx ? F.mn : F.mt;
+    o[3] = isx ? F.mt : F.mn;
+    speed[i] = UU;
+}
+}  // namespace
+
+cudaError_t launch_euler_face_probe(const Params& P, long long n, int axis, const double* L,
+                                    const double* R, double* flux, double* speed,
+                                    cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long long blocks = (n + 255) / 256;
+    euler_face_probe_kernel<<<(unsigned int)blocks, 256, 0, st>>>(P, n, axis, L, R, flux, speed);
+    return cudaGetLastError();
+}
+
 }  // namespace gd

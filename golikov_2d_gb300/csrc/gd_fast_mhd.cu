@@ -445,4 +445,58 @@ cudaError_t launch_mhd_tangent(const Params& P, const CPlanes& in, const CPlanes
     return launch_tangent_t<2>(P, in, din, out, dout, T_do, st);
 }
 
+
+namespace {
+// One face per thread through the step's own face solver (side + hlld_local): L, R are n x 8
+// in the reference's HLLDQ_Korolkov layout (rho, p, vx, vy, vz, Bx, By, Bz; Gaussian B, vz
+// taken as 0 as the 2-D step does); flux n x 8 in its output order and units (mass, x, y, z
+// momentum, Bx, By, Bz, energy; the z-momentum flux is not formed by the 2-D step: 0);
+// speed n values max(|S_L|, |S_R|).  The field goes to Heaviside-Lorentz units by the
+// rounded product the tile load uses.  axis 0: normal +x.
+__global__ void mhd_face_probe_kernel(Params P, long long n, int axis,
+                                      const double* __restrict__ L,
+                                      const double* __restrict__ R, double* flux,
+                                      double* speed) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = L + 8 * i;
+    const double* b = R + 8 * i;
+    const bool isx = axis == 0;
+    double qa[NF], qb[NF];
+    qa[0] = a[0]; qa[1] = a[1]; qa[2] = a[2]; qa[3] = a[3];
+    qb[0] = b[0]; qb[1] = b[1]; qb[2] = b[2]; qb[3] = b[3];
+#pragma unroll
+    for (int f = 4; f < NF; ++f) {
+        qa[f] = __dmul_rn(a[f + 1], kInvSpi4);
+        qb[f] = __dmul_rn(b[f + 1], kInvSpi4);
+    }
+    Side<double> A, B;
+    side(A, qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], isx ? qa[4] : qa[5],
+         isx ? qa[5] : qa[4], qa[6], P);
+    side(B, qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], isx ? qb[4] : qb[5],
+         isx ? qb[5] : qb[4], qb[6], P);
+    double UU;
+    const FluxM<double> F = hlld_local(A, B, P.method, P, UU);
+    double* o = flux + 8 * i;
+    o[0] = F.m;
+    o[1] = isx ? F.mn : F.mt;
+    o[2] = isx ? F.mt : F.mn;
+    o[3] = 0.0;
+    o[4] = (isx ? F.bn : F.bt) * kSpi4;
+    o[5] = (isx ? F.bt : F.bn) * kSpi4;
+    o[6] = F.bz * kSpi4;
+    o[7] = F.e;
+    speed[i] = UU;
+}
+}  // namespace
+
+cudaError_t launch_mhd_face_probe(const Params& P, long long n, int axis, const double* L,
+                                  const double* R, double* flux, double* speed,
+                                  cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long long blocks = (n + 255) / 256;
+    mhd_face_probe_kernel<<<(unsigned int)blocks, 256, 0, st>>>(P, n, axis, L, R, flux, speed);
+    return cudaGetLastError();
+}
+
 }  // namespace gd

@@ -15,6 +15,13 @@ cudaError_t prepare_mhd_fast();
 // Fast face-once step.  `rot` (may be null) receives the fused funk_time rotation by the
 // last block; `ctr` (may be null) receives floor / non-finite counters.  dt_only != 0
 // computes only the dt minimum.
+// The step's face solvers on n independent faces (gd_probe_faces).
+cudaError_t launch_euler_face_probe(const Params& P, long long n, int axis, const double* L,
+                                    const double* R, double* flux, double* speed,
+                                    cudaStream_t st);
+cudaError_t launch_mhd_face_probe(const Params& P, long long n, int axis, const double* L,
+                                  const double* R, double* flux, double* speed,
+                                  cudaStream_t st);
 cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& out,
                               const double* T_do, unsigned long long* T_bits, Scalars* rot,
                               Scalars* ctr, int dt_only, cudaStream_t st);

@@ -355,6 +355,22 @@ long long gd_launch_count(const gd_ctx* ctx);
  * DFMA loop on every SM; blocking, ~50 ms. */
 gd_status gd_probe_fp64_peak(double* flops_out);
 
+/* Test entry point (no reference counterpart): the fast step's own face solver on n
+ * independent faces, for per-face checks against the reference's HLLC_Aleksashov /
+ * HLL (kernel.cu:853-1165, 1485-1609) and HLLDQ_Korolkov (Gas_Dinamic.cu:964-1510).
+ * Device pointers; axis 0: the face normal is +x, 1: +y.
+ *   physics GD_EULER, method GD_METHOD_HLL or GD_METHOD_HLLC: L, R n x 4 (rho, p, vx, vy);
+ *     flux n x 4 (mass, energy, x momentum, y momentum).
+ *   physics GD_MHD, method GD_METHOD_HLLC_MHD or GD_METHOD_HLLD: L, R n x 8 (rho, p, vx, vy,
+ *     vz, Bx, By, Bz; Gaussian B; vz is taken as 0, as the 2-D step does); flux n x 8 (mass,
+ *     x, y, z momentum, Bx, By, Bz, energy; Gaussian field fluxes; the z-momentum flux is not
+ *     formed by the 2-D step and is written as 0).
+ * speed: n values max(|S_L|, |S_R|) (the reference's dt estimate is krit * rad / speed).
+ * Asynchronous on stream. */
+gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long long n,
+                         const double* L, const double* R, double* flux, double* speed,
+                         gd_stream stream);
+
 #ifdef __cplusplus
 }
 #endif
