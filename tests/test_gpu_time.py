@@ -124,3 +124,37 @@ def test_advance_to_respects_max_steps_and_rejects_past_times(cuda):
     with pytest.raises(g.GdError):
         sol.set_dt_policy(5)
     sol.close()
+
+
+# Fast mode against the oracle at t = 0.5 on Orszag-Tang 128^2 (416 steps): measured 4.9e-8
+# (relative L1 per conserved field, the largest).  The differences are rounding grown
+# through minmod near-ties; at 1024^2, where the reference's p <= 0 clamp is reached, they
+# grow to 2.8e-2 by t = 0.5 (test_gpu_fullsize.py).  The bound leaves a factor of ~10.
+OT128_T05_BOUND = 5e-7
+
+
+def test_orszag_tang_128_to_t05(cuda, oracle_lib):
+    """Orszag-Tang at reduced size run to t = 0.5 as the configuration states: parity mode
+    equals the oracle bit for bit (state, time, step count); fast mode is within the stated
+    L1 bound of it."""
+    from gpu_util import max_rel_l1
+    cfg, s, u, b = problems.orszag_tang(128, 128)
+    so, uo, bo, to, no, _ = oracle_to(oracle_lib, cfg, s, u, b, 0.5)
+    for mode in (g.MODE_PARITY, g.MODE_FAST):
+        cfg.mode = mode
+        sol = g.Solver(cfg)
+        sol.import_state(s, u, b)
+        sol.set_time(0.0, 0.0)
+        sol.init_dt()
+        n = sol.advance_to(0.5, use_graph=True)
+        st = sol.stats()
+        s2, u2, b2 = export(sol, s, u, b)
+        sol.close()
+        assert abs(st.t_state - 0.5) <= 1e-14 * 0.5
+        if mode == g.MODE_PARITY:
+            assert n == no and st.t_state == to
+            assert np.array_equal(s2, so) and np.array_equal(u2, uo) and np.array_equal(b2, bo)
+        else:
+            err = max_rel_l1(cfg, (s2, u2, b2), (so, uo, bo))
+            print(f"OT 128^2 t = 0.5: fast vs oracle {err:.3e} after {n} steps (oracle {no})")
+            assert err <= OT128_T05_BOUND, err
