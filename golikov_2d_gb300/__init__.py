@@ -54,7 +54,7 @@ EXPORTS = (
     "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text", "gd_write_binary",
     "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot",
 )
-BATCH_PERSISTENT, BATCH_LOOPED = 0, 1
+BATCH_PERSISTENT, BATCH_LOOPED, BATCH_LOOPED_SYNC = 0, 1, 2
 
 
 class GdError(RuntimeError):

@@ -82,21 +82,25 @@ gd_status step_persistent(gd_batch* b, int variant, int dt_only, Scalars* sc_ove
     return GD_OK;
 }
 
-gd_status step_looped(gd_batch* b, cudaStream_t st) {
+// One plain launch per grid; with `sync` the host waits for each launch before the next, as
+// the reference's main loop does after each of its launches (kernel.cu:4113-4137).
+gd_status step_looped(gd_batch* b, bool sync, cudaStream_t st) {
     for (int g = 0; g < b->ngrids; ++g) {
         Scalars* sc = b->sc + g;
         GD_TRY(gd::launch_euler_fast_v(b->variant, b->params[g], as_const(b->planes(g, b->cur)),
                                        b->planes(g, b->cur ^ 1), &sc->T_do, &sc->T_bits, sc, sc,
                                        0, st));
         b->launches += 1;
+        if (sync) GD_TRY(cudaStreamSynchronize(st));
     }
     return GD_OK;
 }
 
 gd_status advance_plain(gd_batch* b, int nsteps, int schedule, cudaStream_t st) {
     for (int s = 0; s < nsteps; ++s) {
-        gd_status r = schedule == GD_BATCH_LOOPED ? step_looped(b, st)
-                                                  : step_persistent(b, b->variant, 0, nullptr, st);
+        gd_status r = schedule == GD_BATCH_PERSISTENT
+                          ? step_persistent(b, b->variant, 0, nullptr, st)
+                          : step_looped(b, schedule == GD_BATCH_LOOPED_SYNC, st);
         if (r != GD_OK) return r;
         b->cur ^= 1;
     }
@@ -269,8 +273,11 @@ gd_status gd_batch_init_dt(gd_batch* b, gd_stream stream) {
 
 gd_status gd_batch_advance(gd_batch* b, int nsteps, int schedule, int use_graph,
                            gd_stream stream) {
-    if (!b || nsteps < 0 || (schedule != GD_BATCH_PERSISTENT && schedule != GD_BATCH_LOOPED))
+    if (!b || nsteps < 0 ||
+        (schedule != GD_BATCH_PERSISTENT && schedule != GD_BATCH_LOOPED &&
+         schedule != GD_BATCH_LOOPED_SYNC))
         return GD_ERR_INVALID_ARG;
+    if (schedule == GD_BATCH_LOOPED_SYNC && use_graph) return GD_ERR_INVALID_ARG;
     if (nsteps == 0) return GD_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (!use_graph) return advance_plain(b, nsteps, schedule, st);
@@ -304,7 +311,7 @@ gd_status gd_batch_advance(gd_batch* b, int nsteps, int schedule, int use_graph,
         it = b->graphs.emplace(key, ge).first;
     }
     GD_TRY(cudaGraphLaunch(it->second, st));
-    b->launches += (long long)nsteps * (schedule == GD_BATCH_LOOPED ? b->ngrids : 1);
+    b->launches += (long long)nsteps * (schedule == GD_BATCH_PERSISTENT ? 1 : b->ngrids);
     if (nsteps & 1) b->cur ^= 1;
     return GD_OK;
 }

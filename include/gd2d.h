@@ -250,10 +250,13 @@ gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const dou
  * each with its own boundaries, dt reduction, dt rotation and time.  Schedules:
  *   GD_BATCH_PERSISTENT  one persistent launch per step walks the tiles of every grid
  *   GD_BATCH_LOOPED      one plain launch per grid per step (the baseline)
+ *   GD_BATCH_LOOPED_SYNC as GD_BATCH_LOOPED, the host waiting for each launch to finish
+ *                        before the next, as the reference's main loop synchronises after
+ *                        each of its launches (kernel.cu:4113-4137); no graph (use_graph 0)
  * gd_batch_autotune times every compiled tile shape (32x16, 32x8, 16x16, 64x8; the halo
  * width is the stencil's, 2 cells for order 2) on the batch's own grids without changing
  * their state or time, and keeps the fastest for GD_BATCH_PERSISTENT. */
-enum { GD_BATCH_PERSISTENT = 0, GD_BATCH_LOOPED = 1 };
+enum { GD_BATCH_PERSISTENT = 0, GD_BATCH_LOOPED = 1, GD_BATCH_LOOPED_SYNC = 2 };
 typedef struct gd_batch gd_batch;
 typedef struct gd_batch_info {
     int ngrids;

@@ -85,3 +85,16 @@ def test_batch_against_oracle(cuda, oracle_lib):
         so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 10)
         assert max_rel_l1(cfg, (s2, u2, None), (so, uo, None)) <= 1e-10
         assert abs(st.t - TT) <= 1e-11 * TT
+
+
+def test_looped_sync_equals_looped(cuda):
+    """GD_BATCH_LOOPED_SYNC (the host waiting for each launch, as the reference's main loop)
+    steps every grid exactly as GD_BATCH_LOOPED; it cannot be captured in a graph."""
+    grids = small_batch(6)
+    a, _ = run_batch(grids, 5, schedule=g.BATCH_LOOPED)
+    c, _ = run_batch(grids, 5, schedule=g.BATCH_LOOPED_SYNC)
+    for (s1, u1, st1), (s2, u2, st2) in zip(a, c):
+        assert np.array_equal(s1, s2) and np.array_equal(u1, u2)
+        assert st1.t == st2.t and st1.dt == st2.dt
+    with pytest.raises(g.GdError):
+        run_batch(grids, 1, schedule=g.BATCH_LOOPED_SYNC, use_graph=True)
