@@ -117,6 +117,24 @@ def ncu_fp64_per_cell(workload):
     return None
 
 
+def ncu_l2_hit_pct(workload):
+    """L2 sector hit rate of the step kernel (lts__t_sector_hit_rate) where the committed ncu
+    summary records one, as an `l2hit=<percent>` token of the workload's line."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if parts and parts[0] == workload:
+            for tok in parts[3:]:
+                if tok.startswith("l2hit="):
+                    try:
+                        return float(tok[len("l2hit="):])
+                    except ValueError:
+                        return None
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -961,7 +979,8 @@ def run_gb300(args):
                                  "unit": "cell-updates/s", "ms_per_step": ms2,
                                  "roofline": {"bound": "hbm", "achieved": ach2, "peak": peak_gbs,
                                               "unit": "GB/s", "frac": ach2 / peak_gbs,
-                                              "traffic": ncu_traffic("ot1024")},
+                                              "traffic": ncu_traffic("ot1024"),
+                                              "l2_hit_pct": ncu_l2_hit_pct("ot1024")},
                                  "fp64": fp64_roofline(g, "ot1024", K2 / (ms2 * 1e-3), torch),
                                  "l2": "flushed before every timed step",
                                  "gpu_launches": l2,
