@@ -346,7 +346,8 @@ class Solver:
                                        _stream_handle(stream)), "gd_adj_forward")
 
     def _vec_call(self, fn, what, ins, outs, stream):
-        p = [t.data_ptr() for t in ins] + [t.data_ptr() for t in outs]
+        ptr = lambda t: None if t is None else t.data_ptr()  # Euler: no field tensors
+        p = [ptr(t) for t in ins] + [ptr(t) for t in outs]
         _check(fn(self.handle, *p, _stream_handle(stream)), what)
 
     def adj_backward(self, gs, gu, gb, os_, ou, ob, stream=None) -> None:

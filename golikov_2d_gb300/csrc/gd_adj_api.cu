@@ -49,9 +49,30 @@ bool adj_supported(const gd_ctx* ctx) {
     const gd_config& c = ctx->cfg;
     for (int s = 0; s < 4; ++s)
         if (c.bc[s] != GD_BC_PERIODIC) return false;
-    return c.scheme == GD_SCHEME_TVD && c.physics == GD_MHD && c.method == GD_METHOD_HLLD &&
-           c.order == 2 &&
-           c.geometry == GD_CARTESIAN && c.mode == GD_MODE_FAST && c.frozen_radius == 0.0;
+    const bool flux = (c.physics == GD_MHD && c.method == GD_METHOD_HLLD) ||
+                      (c.physics == GD_EULER && c.method == GD_METHOD_HLLC);
+    return c.scheme == GD_SCHEME_TVD && flux && c.order == 2 && c.geometry == GD_CARTESIAN &&
+           c.mode == GD_MODE_FAST && c.frozen_radius == 0.0;
+}
+
+// planes of update terms stored per recorded step: MHD d[0..6] and the Powell term, Euler
+// d[0..3]
+int aux_planes(const gd_ctx* ctx) { return ctx->nf == 7 ? 8 : 4; }
+
+// the fast step writing its update terms to `aux` (null: not stored)
+cudaError_t step_aux(const gd_ctx* ctx, const Params& P, const CPlanes& in, const Planes& out,
+                     const double* T_do, unsigned long long* T_bits, Scalars* rot, Scalars* ctr,
+                     double* aux, cudaStream_t st) {
+    return ctx->nf == 7 ? gd::launch_mhd_fast_aux(P, in, out, T_do, T_bits, rot, ctr, aux, st)
+                        : gd::launch_euler_fast_aux(P, in, out, T_do, T_bits, rot, ctr, aux, st);
+}
+
+cudaError_t reverse_step(const gd_ctx* ctx, const Params& P, const CPlanes& U, const double* aux,
+                         const CPlanes& lam_out, const Planes& lam_in, double* scratch,
+                         const double* T_do, cudaStream_t st) {
+    return ctx->nf == 7
+               ? gd::launch_adjoint_step(P, U, aux, lam_out, lam_in, scratch, T_do, st)
+               : gd::launch_adjoint_step_euler(P, U, aux, lam_out, lam_in, scratch, T_do, st);
 }
 
 // (Re)allocates the recording store for nsteps steps with a checkpoint every `every`
@@ -68,13 +89,15 @@ gd_status alloc_store(gd_ctx* ctx, int nsteps, int every, size_t state) {
     GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
     GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
     GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
-    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * 8 * (size_t)K * every));
+    const int naux = aux_planes(ctx);
+    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * naux * (size_t)K * every));
     GD_TRY(cudaMalloc(&a->lam, 2 * state));
-    GD_TRY(cudaMalloc(&a->scratch,
-                      sizeof(double) * (size_t)gd::adjoint_scratch_planes() * (size_t)K));
+    const int nscr = ctx->nf == 7 ? gd::adjoint_scratch_planes()
+                                  : gd::adjoint_euler_scratch_planes();
+    GD_TRY(cudaMalloc(&a->scratch, sizeof(double) * (size_t)nscr * (size_t)K));
     GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
     GD_TRY(cudaMalloc(&a->seg2, state * (every + 1)));
-    GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * 8 * (size_t)K * every));
+    GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * naux * (size_t)K * every));
     GD_TRY(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&a->ev_start, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0],
                            &a->ev_rev[1]})
@@ -144,10 +167,10 @@ gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stre
         if (j == 0)
             GD_TRY(cudaMemcpyAsync(seg, ctx->state[ctx->cur], state, cudaMemcpyDeviceToDevice,
                                    st));
-        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(seg + (size_t)j * nf * K, nf, K),
-                                       planes_at(seg + (size_t)(j + 1) * nf * K, nf, K),
-                                       &ctx->sc->T_do, &ctx->sc->T_bits, ctx->sc, ctx->sc,
-                                       aux + (size_t)j * 8 * K, st));
+        GD_TRY(step_aux(ctx, ctx->P, cplanes_at(seg + (size_t)j * nf * K, nf, K),
+                        planes_at(seg + (size_t)(j + 1) * nf * K, nf, K), &ctx->sc->T_do,
+                        &ctx->sc->T_bits, ctx->sc, ctx->sc,
+                        aux + (size_t)j * aux_planes(ctx) * K, st));
         ctx->launches += 1;
         // the segment's last output is the context's state for what follows
         if (j + 1 == (last ? nsteps - k_last : every))
@@ -161,7 +184,8 @@ gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stre
 
 gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const double* gb,
                           double* os, double* ou, double* ob, gd_stream stream) {
-    if (!ctx || !ctx->adj || !gs || !gu || !gb || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    if (!ctx || !ctx->adj || !gs || !gu || !os || !ou) return GD_ERR_INVALID_ARG;
+    if (ctx->nf == 7 && (!gb || !ob)) return GD_ERR_INVALID_ARG;
     gd::AdjStore* a = ctx->adj;
     const long long K = ctx->K;
     const int nf = ctx->nf;
@@ -185,10 +209,10 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
         GD_TRY(cudaMemcpyAsync(segb[b], a->ckpt + (size_t)sg * nf * K, state,
                                cudaMemcpyDeviceToDevice, s));
         for (int j = 0; j < len; ++j) {
-            GD_TRY(gd::launch_mhd_fast_aux(P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
-                                           planes_at(segb[b] + (size_t)(j + 1) * nf * K, nf, K),
-                                           a->dts + k0 + j, (unsigned long long*)a->tbits,
-                                           nullptr, nullptr, auxb[b] + (size_t)j * 8 * K, s));
+            GD_TRY(step_aux(ctx, P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
+                            planes_at(segb[b] + (size_t)(j + 1) * nf * K, nf, K),
+                            a->dts + k0 + j, (unsigned long long*)a->tbits, nullptr, nullptr,
+                            auxb[b] + (size_t)j * aux_planes(ctx) * K, s));
             ctx->launches += 1;
         }
         return GD_OK;
@@ -221,10 +245,10 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
         int k0, len;
         seg_range(sg, &k0, &len);
         for (int j = len - 1; j >= 0; --j) {
-            GD_TRY(gd::launch_adjoint_step(P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
-                                           auxb[b] + (size_t)j * 8 * K, cplanes_at(lam[c], nf, K),
-                                           planes_at(lam[c ^ 1], nf, K), a->scratch,
-                                           a->dts + k0 + j, st));
+            GD_TRY(reverse_step(ctx, P, cplanes_at(segb[b] + (size_t)j * nf * K, nf, K),
+                                auxb[b] + (size_t)j * aux_planes(ctx) * K,
+                                cplanes_at(lam[c], nf, K), planes_at(lam[c ^ 1], nf, K),
+                                a->scratch, a->dts + k0 + j, st));
             ctx->launches += 3;
             c ^= 1;
         }
@@ -244,7 +268,9 @@ gd_status gd_adj_backward(gd_ctx* ctx, const double* gs, const double* gu, const
 
 gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const double* vb,
                      double* os, double* ou, double* ob, gd_stream stream) {
-    if (!ctx || !ctx->adj || !vs || !vu || !vb || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    if (!ctx || !ctx->adj || !vs || !vu || !os || !ou) return GD_ERR_INVALID_ARG;
+    if (ctx->nf == 7 && (!vb || !ob)) return GD_ERR_INVALID_ARG;
+    if (ctx->nf != 7) return GD_ERR_UNSUPPORTED;  // the tangent kernel is the MHD tile's
     gd::AdjStore* a = ctx->adj;
     const long long K = ctx->K;
     const int nf = ctx->nf;
@@ -269,7 +295,8 @@ gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const doub
 
 gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const double* b,
                         double* os, double* ou, double* ob, gd_stream stream) {
-    if (!ctx || !ctx->adj || !s || !u || !b || !os || !ou || !ob) return GD_ERR_INVALID_ARG;
+    if (!ctx || !ctx->adj || !s || !u || !os || !ou) return GD_ERR_INVALID_ARG;
+    if (ctx->nf == 7 && (!b || !ob)) return GD_ERR_INVALID_ARG;
     gd::AdjStore* a = ctx->adj;
     const long long K = ctx->K;
     const int nf = ctx->nf;
@@ -279,9 +306,9 @@ gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const dou
     GD_TRY(gd::launch_aos_to_soa(s, u, b, planes_at(w[0], nf, K), K, nf, st));
     int c = 0;
     for (int k = 0; k < a->nsteps; ++k) {
-        GD_TRY(gd::launch_mhd_fast_aux(ctx->P, cplanes_at(w[c], nf, K), planes_at(w[c ^ 1], nf, K),
-                                       a->dts + k, (unsigned long long*)a->tbits, nullptr,
-                                       nullptr, nullptr, st));
+        GD_TRY(step_aux(ctx, ctx->P, cplanes_at(w[c], nf, K), planes_at(w[c ^ 1], nf, K),
+                        a->dts + k, (unsigned long long*)a->tbits, nullptr, nullptr, nullptr,
+                        st));
         ctx->launches += 1;
         c ^= 1;
     }

@@ -150,13 +150,15 @@ struct TileResult {
 
 // One TX x TY tile whose lower-left cell is (tx0, ty0).  Reads `in`, writes `out`, returns
 // the per-thread wave-speed maxima and counters.  Every thread of the block must call it.
+// `aux` (may be null): per cell, the flux differences d[0..3] of the update, planes of N*M
+// (the adjoint's recording).
 // Not inlined: the single-grid kernel and the persistent batch kernel call one compiled
 // function per tile shape, so a grid's arithmetic, and its bits, do not depend on which
 // schedule advanced it (inlined into each, the compiler may fuse the two differently).
 template <int ORDER, int TX, int TY>
 __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, const Planes& out,
                                            int tx0, int ty0, double T_do, int dt_only,
-                                           double* smem, TileResult& res) {
+                                           double* smem, TileResult& res, double* aux) {
     using S = Shape<ORDER, TX, TY>;
     constexpr int H = S::H, SX = S::SX, SY = S::SY;
     double* prim = smem;                 // [NF][SY][SX]
@@ -311,6 +313,11 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
             const double* b = fyc + f * (TY + 1) * TX;
             d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
         }
+        if (aux != nullptr) {  // the recording of the adjoint: the flux differences used
+            const long long KK = (long long)N * M;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) aux[f * KK + k] = d[f];
+        }
         double r2 = r - d[0];
         if (le_zero(r2)) { r2 = 0.0001; ++nfl_r; }
         const double E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
@@ -345,11 +352,12 @@ template <int ORDER, int TX, int TY>
 __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Planes out,
                                                         const double* __restrict__ T_do_ptr,
                                                         unsigned long long* T_bits, Scalars* rot,
-                                                        Scalars* ctr, int dt_only) {
+                                                        Scalars* ctr, int dt_only,
+                                                        double* aux) {
     extern __shared__ double smem[];
     TileResult r;
     euler_tile<ORDER, TX, TY>(P, in, out, blockIdx.x * TX, (blockIdx.y + P.tile_row0) * TY,
-                              *T_do_ptr, dt_only, smem, r);
+                              *T_do_ptr, dt_only, smem, r, aux);
     add_counters(ctr, r);
     block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot, P.tile_nblocks);
 }
@@ -387,7 +395,7 @@ __global__ void __launch_bounds__(NT) euler_batch_kernel(const BatchGrid* __rest
         const int tx0 = (tile % g.tiles_x) * TX, ty0 = (tile / g.tiles_x) * TY;
         const double T_do = g.sc->T_do;
         TileResult r;
-        euler_tile<ORDER, TX, TY>(g.P, in, out, tx0, ty0, T_do, dt_only, smem, r);
+        euler_tile<ORDER, TX, TY>(g.P, in, out, tx0, ty0, T_do, dt_only, smem, r, nullptr);
         add_counters(dt_only ? nullptr : g.sc, r);
         block_dt_and_rotate<NT>(g.P, r.umax_x, r.umax_y, r.any_active, &g.sc->T_bits,
                                 dt_only ? nullptr : g.sc, (unsigned int)g.ntiles);
@@ -408,10 +416,10 @@ cudaError_t set_attrs() {
 template <int ORDER, int TX, int TY>
 cudaError_t launch_single(const Params& P, const CPlanes& in, const Planes& out,
                           const double* T_do, unsigned long long* T_bits, Scalars* rot,
-                          Scalars* ctr, int dt_only, cudaStream_t st) {
+                          Scalars* ctr, int dt_only, cudaStream_t st, double* aux = nullptr) {
     dim3 grid((P.N + TX - 1) / TX, P.tile_rows ? P.tile_rows : (P.M + TY - 1) / TY);
     euler_fast_kernel<ORDER, TX, TY><<<grid, NT, Shape<ORDER, TX, TY>::bytes, st>>>(
-        P, in, out, T_do, T_bits, rot, ctr, dt_only);
+        P, in, out, T_do, T_bits, rot, ctr, dt_only, aux);
     return cudaGetLastError();
 }
 
@@ -505,6 +513,15 @@ cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& 
                               const double* T_do, unsigned long long* T_bits, Scalars* rot,
                               Scalars* ctr, int dt_only, cudaStream_t st) {
     return launch_euler_fast_v(0, P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
+                                  const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                  Scalars* ctr, double* aux, cudaStream_t st) {
+    // variant 0, the launch gd_advance makes: the recorded step is the plain step
+    if (P.order == 1)
+        return launch_single<1, 32, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
+    return launch_single<2, 32, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
 }
 
 cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, const int2* items,

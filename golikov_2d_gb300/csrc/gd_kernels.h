@@ -15,6 +15,10 @@ cudaError_t prepare_mhd_fast();
 // Fast face-once step.  `rot` (may be null) receives the fused funk_time rotation by the
 // last block; `ctr` (may be null) receives floor / non-finite counters.  dt_only != 0
 // computes only the dt minimum.
+// The Euler step (variant 0) writing its flux differences d[0..3] per cell to `aux`.
+cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
+                                  const double* T_do, unsigned long long* T_bits, Scalars* rot,
+                                  Scalars* ctr, double* aux, cudaStream_t st);
 // The step's face solvers on n independent faces (gd_probe_faces).
 cudaError_t launch_euler_face_probe(const Params& P, long long n, int axis, const double* L,
                                     const double* R, double* flux, double* speed,
@@ -71,6 +75,12 @@ cudaError_t launch_mhd_fast_aux(const Params& P, const CPlanes& in, const Planes
 // lam_in = S'(U)^T lam_out, with U, aux of the forward step and the dt *T_do.
 // `scratch` holds adjoint_scratch_planes() planes of N*M.
 int adjoint_scratch_planes();
+// The Euler (HLLC) reverse step, the same roles as launch_adjoint_step with four fields and
+// aux d[0..3] per cell; its scratch holds adjoint_euler_scratch_planes() planes.
+int adjoint_euler_scratch_planes();
+cudaError_t launch_adjoint_step_euler(const Params& P, const CPlanes& U, const double* aux,
+                                      const CPlanes& lam_out, const Planes& lam_in,
+                                      double* scratch, const double* T_do, cudaStream_t st);
 cudaError_t prepare_adjoint();
 cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
                                 const CPlanes& lam_out, const Planes& lam_in, double* scratch,

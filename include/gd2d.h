@@ -224,11 +224,13 @@ gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
 /* ---- differentiation: discrete adjoint and tangent ------------------------------------
  * No counterpart in the reference.  The map differentiated is n steps of the fast step
  * with the dt sequence of a recorded forward run held fixed (the CFL minimum is not
- * differentiated); minmod, wave-speed min/max, HLLD region and guard choices and floors
- * are differentiated along the branch the forward values take.  Supported: MHD, HLLD,
- * order 2, Cartesian, periodic on all sides, fast mode, no frozen cells (the Orszag-Tang
- * configuration); other configurations return GD_ERR_UNSUPPORTED.  All vectors are device
- * pointers in the reference AoS layout (d/ds: K x 2, d/du: K x 2, d/dB: K x 3, Gaussian B).
+ * differentiated); minmod, wave-speed min/max, HLLC / HLLD region and guard choices and
+ * floors are differentiated along the branch the forward values take.  Supported: MHD with
+ * HLLD or Euler with HLLC, order 2, Cartesian, periodic on all sides, fast mode, no frozen
+ * cells (the Orszag-Tang and Kelvin-Helmholtz configurations); other configurations return
+ * GD_ERR_UNSUPPORTED, and so does gd_tangent for Euler.  All vectors are device pointers in
+ * the reference AoS layout (d/ds: K x 2, d/du: K x 2, d/dB: K x 3, Gaussian B; for Euler
+ * the d/dB pointers may be null).
  *
  * gd_adj_forward: advance nsteps from the current state (as gd_advance), recording the dt
  *   of every step and a checkpoint of the state every ckpt_every steps.
