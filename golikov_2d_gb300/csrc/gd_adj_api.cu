@@ -270,7 +270,6 @@ gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const doub
                      double* os, double* ou, double* ob, gd_stream stream) {
     if (!ctx || !ctx->adj || !vs || !vu || !os || !ou) return GD_ERR_INVALID_ARG;
     if (ctx->nf == 7 && (!vb || !ob)) return GD_ERR_INVALID_ARG;
-    if (ctx->nf != 7) return GD_ERR_UNSUPPORTED;  // the tangent kernel is the MHD tile's
     gd::AdjStore* a = ctx->adj;
     const long long K = ctx->K;
     const int nf = ctx->nf;
@@ -283,9 +282,10 @@ gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const doub
     GD_TRY(cudaMemcpyAsync(u[0], a->ckpt, state, cudaMemcpyDeviceToDevice, st));
     int c = 0;
     for (int k = 0; k < a->nsteps; ++k) {
-        GD_TRY(gd::launch_mhd_tangent(ctx->P, cplanes_at(u[c], nf, K), cplanes_at(t[c], nf, K),
-                                      planes_at(u[c ^ 1], nf, K), planes_at(t[c ^ 1], nf, K),
-                                      a->dts + k, st));
+        const CPlanes ui = cplanes_at(u[c], nf, K), ti = cplanes_at(t[c], nf, K);
+        const Planes uo = planes_at(u[c ^ 1], nf, K), to = planes_at(t[c ^ 1], nf, K);
+        GD_TRY(nf == 7 ? gd::launch_mhd_tangent(ctx->P, ui, ti, uo, to, a->dts + k, st)
+                       : gd::launch_euler_tangent(ctx->P, ui, ti, uo, to, a->dts + k, st));
         ctx->launches += 1;
         c ^= 1;
     }

@@ -26,8 +26,12 @@
 // for method 0, the Ker_Dekard update and floors
 // rho <= 0 -> 1e-4, p <= 0 -> 1e-6 (kernel.cu:1849-1874), dt = min over faces of
 // krit*rad/max(|SL|,|SR|) with rad = dy on x-faces (kernel.cu:1811).
+#include <type_traits>
+
+#include "gd_dual.cuh"
 #include "gd_internal.cuh"
 #include "gd_kernels.h"
+#include "gd_mhd_flux.cuh"  // cst<T>
 
 namespace gd {
 namespace {
@@ -35,52 +39,54 @@ namespace {
 constexpr int NT = 256;
 constexpr int NF = 4;
 
+template <class T>
 struct FluxE {
-    double m, mn, mt, e;
+    T m, mn, mt, e;
 };
 
 // HLLC flux in a local frame: un = normal velocity, ut = in-plane tangential velocity.
 // Returns the flux (mass, normal momentum, tangential momentum, energy) and, in UU,
-// max(|SL|, |SR|).
-__device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, double utL,
-                                            double rR, double pR, double unR, double utR,
-                                            const Params& P, double& UU) {
+// max(|SL|, |SR|).  T is double, or Dual for the tangent (value and derivative, the branch
+// choices taken on the value).
+template <class T>
+__device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
+                                               T utR, const Params& P, T& UU) {
     const double g = P.gamma;
-    const double gpL = g * pL, gpR = g * pR;
-    const double cL = sqrt_over(gpL, rL);  // sqrt(g p / rho)
-    const double cR = sqrt_over(gpR, rR);
-    const double aL = unL - cL, aR = unR - cR;
-    const double bL = unL + cL, bR = unR + cR;
-    const double SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
-    const double SR = dmax(bL, bR);
-    const double suL = SL - unL, suR = SR - unR;
-    const double mL = rL * suL, mR = rR * suR;
-    const double SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
+    const T gpL = g * pL, gpR = g * pR;
+    const T cL = sqrt_over(gpL, rL);  // sqrt(g p / rho)
+    const T cR = sqrt_over(gpR, rR);
+    const T aL = unL - cL, aR = unR - cR;
+    const T bL = unL + cL, bR = unR + cR;
+    const T SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
+    const T SR = dmax(bL, bR);
+    const T suL = SL - unL, suR = SR - unR;
+    const T mL = rL * suL, mR = rR * suR;
+    const T SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
     UU = max_nonneg(dabs(SL), dabs(SR));
 
     // Side whose state (or star state) gives the flux at x/t = 0 (kernel.cu:1119-1158).
     const bool takeL = gt_zero(SL) || ge_zero(SM);
-    const double r = takeL ? rL : rR;
-    const double p = takeL ? pL : pR;
-    const double un = takeL ? unL : unR;
-    const double ut = takeL ? utL : utR;
-    const double S = takeL ? SL : SR;
-    const double su = takeL ? suL : suR;
-    const double mm = takeL ? mL : mR;
+    const T r = takeL ? rL : rR;
+    const T p = takeL ? pL : pR;
+    const T un = takeL ? unL : unR;
+    const T ut = takeL ? utL : utR;
+    const T S = takeL ? SL : SR;
+    const T su = takeL ? suL : suR;
+    const T mm = takeL ? mL : mR;
     const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
 
-    FluxE F;
+    FluxE<T> F;
     F.m = r * un;
     F.mn = fma(F.m, un, p);
     F.mt = F.m * ut;
-    const double E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
+    const T E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
     F.e = (E + p) * un;
     if (star) {
-        const double inv = rcp_fast(S - SM);
-        const double rz = r * (su * inv);
-        const double pst = fma(mm, SM - un, p);
-        const double ez = fma(-p, un, fma(E, su, pst * SM)) * inv;
-        const double drz = rz - r;
+        const T inv = rcp_fast(S - SM);
+        const T rz = r * (su * inv);
+        const T pst = fma(mm, SM - un, p);
+        const T ez = fma(-p, un, fma(E, su, pst * SM)) * inv;
+        const T drz = rz - r;
         F.mn = fma(S, fma(rz, SM, -F.m), F.mn);
         F.m = fma(S, drz, F.m);
         F.mt = fma(S, ut * drz, F.mt);
@@ -93,34 +99,34 @@ __device__ __forceinline__ FluxE hllc_local(double rL, double pL, double unL, do
 // hllc_local): sound speed 0 where rho <= 0, D_L = min(un) - max(c), D_R = max(un) + max(c),
 // the upwind physical flux when the fan lies on one side of the face (strict tests against
 // Omega = 0, kernel.cu:11), else (D_R F_L - D_L F_R + D_L D_R (U_R - U_L)) / (D_R - D_L).
-__device__ __forceinline__ FluxE hll_local(double rL, double pL, double unL, double utL,
-                                           double rR, double pR, double unR, double utR,
-                                           const Params& P, double& UU) {
+template <class T>
+__device__ __forceinline__ FluxE<T> hll_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
+                                              T utR, const Params& P, T& UU) {
     const double g = P.gamma;
-    const double gpL = g * pL, gpR = g * pR;
-    const double cL = le_zero(rL) ? 0.0 : sqrt_over(gpL, rL);  // sqrt(g p / rho)
-    const double cR = le_zero(rR) ? 0.0 : sqrt_over(gpR, rR);
-    const double cm = max_nonneg(cL, cR);
-    const double DL = dmin(unL, unR) - cm;
-    const double DR = dmax(unL, unR) + cm;
+    const T gpL = g * pL, gpR = g * pR;
+    const T cL = le_zero(rL) ? cst<T>(0.0) : sqrt_over(gpL, rL);  // sqrt(g p / rho)
+    const T cR = le_zero(rR) ? cst<T>(0.0) : sqrt_over(gpR, rR);
+    const T cm = max_nonneg(cL, cR);
+    const T DL = dmin(unL, unR) - cm;
+    const T DR = dmax(unL, unR) + cm;
     UU = max_nonneg(dabs(DL), dabs(DR));
     const bool left = gt_zero(DL), right = !left && lt_zero(DR);
-    FluxE F;
+    FluxE<T> F;
     if (left || right) {  // one side's physical flux
-        const double r = left ? rL : rR, p = left ? pL : pR;
-        const double un = left ? unL : unR, ut = left ? utL : utR;
+        const T r = left ? rL : rR, p = left ? pL : pR;
+        const T un = left ? unL : unR, ut = left ? utL : utR;
         F.m = r * un;
         F.mn = fma(F.m, un, p);
         F.mt = F.m * ut;
-        const double E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
+        const T E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
         F.e = (E + p) * un;
         return F;
     }
-    const double mL = rL * unL, mR = rR * unR;
-    const double EL = fma(pL, P.inv_gm1, 0.5 * rL * fma(unL, unL, utL * utL));
-    const double ER = fma(pR, P.inv_gm1, 0.5 * rR * fma(unR, unR, utR * utR));
-    const double inv = rcp_fast(DR - DL);
-    const double dd = DL * DR;
+    const T mL = rL * unL, mR = rR * unR;
+    const T EL = fma(pL, P.inv_gm1, 0.5 * rL * fma(unL, unL, utL * utL));
+    const T ER = fma(pR, P.inv_gm1, 0.5 * rR * fma(unR, unR, utR * utR));
+    const T inv = rcp_fast(DR - DL);
+    const T dd = DL * DR;
     // (D_R F_L - D_L F_R + D_L D_R dU) / (D_R - D_L), component by component
     F.m = fma(dd, rR - rL, fma(DR, mL, -DL * mR)) * inv;
     F.mn = fma(dd, mR - mL, fma(DR, fma(mL, unL, pL), -DL * fma(mR, unR, pR))) * inv;
@@ -142,6 +148,36 @@ struct Shape {
     static constexpr size_t bytes = sizeof(double) * (kPrim + kSlx + kSly + kFx + kFy);
 };
 
+// Value and tangent planes (the tangent step of the adjoint checks).
+struct DualIn {
+    CPlanes v, d;
+};
+struct DualOut {
+    Planes v, d;
+};
+
+__device__ __forceinline__ void load_cell(const Params& P, const CPlanes& in, int gx, int gy,
+                                          double* v) {
+    fetch_cell<NF>(P, in, gx, gy, v);
+}
+// The tangent of a ghost value: the same copy (the tangent runs on periodic grids only, where
+// a ghost is a copy of a cell).
+__device__ __forceinline__ void load_cell(const Params& P, const DualIn& in, int gx, int gy,
+                                          Dual* v) {
+    double a[NF], b[NF];
+    fetch_cell<NF>(P, in.v, gx, gy, a);
+    fetch_cell<NF>(P, in.d, gx, gy, b);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) v[f] = Dual{a[f], b[f]};
+}
+__device__ __forceinline__ void store_cell(const Planes& out, long long k, int f, double x) {
+    out.f[f][k] = x;
+}
+__device__ __forceinline__ void store_cell(const DualOut& out, long long k, int f, Dual x) {
+    out.v.f[f][k] = x.v;
+    out.d.f[f][k] = x.d;
+}
+
 struct TileResult {
     double umax_x, umax_y;
     bool any_active;
@@ -155,17 +191,17 @@ struct TileResult {
 // Not inlined: the single-grid kernel and the persistent batch kernel call one compiled
 // function per tile shape, so a grid's arithmetic, and its bits, do not depend on which
 // schedule advanced it (inlined into each, the compiler may fuse the two differently).
-template <int ORDER, int TX, int TY>
-__device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, const Planes& out,
-                                           int tx0, int ty0, double T_do, int dt_only,
-                                           double* smem, TileResult& res, double* aux) {
+template <class T, int ORDER, int TX, int TY, class IN, class OUT>
+__device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT& out, int tx0,
+                                        int ty0, double T_do, int dt_only, T* smem,
+                                        TileResult& res, double* aux) {
     using S = Shape<ORDER, TX, TY>;
     constexpr int H = S::H, SX = S::SX, SY = S::SY;
-    double* prim = smem;                 // [NF][SY][SX]
-    double* slx = prim + S::kPrim;       // [NF][TY][TX+2]   cells x in [-1, TX]
-    double* sly = slx + S::kSlx;         // [NF][TY+2][TX]   cells y in [-1, TY]
-    double* fx = sly + S::kSly;          // [NF][TY][TX+1]   face between x-1 and x
-    double* fy = fx + S::kFx;            // [NF][TY+1][TX]   face between y-1 and y
+    T* prim = smem;                 // [NF][SY][SX]
+    T* slx = prim + S::kPrim;       // [NF][TY][TX+2]   cells x in [-1, TX]
+    T* sly = slx + S::kSlx;         // [NF][TY+2][TX]   cells y in [-1, TY]
+    T* fx = sly + S::kSly;          // [NF][TY][TX+1]   face between x-1 and x
+    T* fy = fx + S::kFx;            // [NF][TY+1][TX]   face between y-1 and y
 
     const int tid = threadIdx.x;
     const int N = P.N, M = P.M;
@@ -176,13 +212,13 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
         const bool xh = lx < H || lx >= TX + H, yh = ly < H || ly >= TY + H;
         if (xh && yh) continue;  // corners are never read
         const int gx = tx0 + lx - H, gy = ty0 + ly - H;
-        double v[NF];
+        T v[NF];
         if (gx >= -2 && gx < N + 2 && gy >= -2 && gy < M + 2 &&
             !((gx < 0 || gx >= N) && (gy < 0 || gy >= M))) {
-            fetch_cell<NF>(P, in, gx, gy, v);
+            load_cell(P, in, gx, gy, v);
         } else {
 #pragma unroll
-            for (int f = 0; f < NF; ++f) v[f] = 1.0;  // outside the grid, never used
+            for (int f = 0; f < NF; ++f) v[f] = cst<T>(1.0);  // outside the grid, never used
         }
 #pragma unroll
         for (int f = 0; f < NF; ++f) prim[(f * SY + ly) * SX + lx] = v[f];
@@ -193,19 +229,19 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
     if (ORDER == 2) {
         for (int i = tid; i < TY * (TX + 2); i += NT) {
             const int ly = i / (TX + 2), c = i - ly * (TX + 2);  // cell x = c - 1
-            const double* row = prim + (ly + H) * SX + (c - 1 + H);
+            const T* row = prim + (ly + H) * SX + (c - 1 + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                const double* q = row + f * SY * SX;
+                const T* q = row + f * SY * SX;
                 slx[(f * TY + ly) * (TX + 2) + c] = minmod(q[0] - q[-1], q[1] - q[0]);
             }
         }
         for (int i = tid; i < (TY + 2) * TX; i += NT) {
             const int r = i / TX, lx = i - r * TX;  // cell y = r - 1
-            const double* col = prim + (r - 1 + H) * SX + (lx + H);
+            const T* col = prim + (r - 1 + H) * SX + (lx + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                const double* q = col + f * SY * SX;
+                const T* q = col + f * SY * SX;
                 sly[(f * (TY + 2) + r) * TX + lx] = minmod(q[0] - q[-SX], q[SX] - q[0]);
             }
         }
@@ -233,14 +269,14 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
         if (P.frozen && !cell_active(P, tx0 + ax, ty0 + ay) &&
             !cell_active(P, tx0 + lx, ty0 + ly))
             continue;  // no updated cell uses this face
-        const double* pa = prim + (ay + H) * SX + (ax + H);
-        const double* pb = pa + (isx ? 1 : SX);
-        double qa[NF], qb[NF];
+        const T* pa = prim + (ay + H) * SX + (ax + H);
+        const T* pb = pa + (isx ? 1 : SX);
+        T qa[NF], qb[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            const double ca = pa[f * SY * SX], cb = pb[f * SY * SX];
+            const T ca = pa[f * SY * SX], cb = pb[f * SY * SX];
             if (ORDER == 2) {
-                double da, db;
+                T da, db;
                 if (isx) {
                     da = slx[(f * TY + ly) * (TX + 2) + lx];
                     db = slx[(f * TY + ly) * (TX + 2) + lx + 1];
@@ -248,7 +284,7 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
                     da = sly[(f * (TY + 2) + ly) * TX + lx];
                     db = sly[(f * (TY + 2) + ly + 1) * TX + lx];
                 }
-                double a = fma(0.5, da, ca), b = fma(-0.5, db, cb);
+                T a = fma(0.5, da, ca), b = fma(-0.5, db, cb);
                 if (f < 2) {  // rho, p fall back to the cell value (kernel.cu:3436-3470)
                     a = le_zero(a) ? ca : a;
                     b = le_zero(b) ? cb : b;
@@ -260,27 +296,27 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
                 qb[f] = cb;
             }
         }
-        double UU;
-        const FluxE F =
+        T UU;
+        const FluxE<T> F =
             P.method == GD_METHOD_HLL
                 ? hll_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], qb[0], qb[1],
                             isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU)
                 : hllc_local(qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2], qb[0], qb[1],
                              isx ? qb[2] : qb[3], isx ? qb[3] : qb[2], P, UU);
         if (isx) {
-            double* fo = fx + ly * (TX + 1) + lx;
+            T* fo = fx + ly * (TX + 1) + lx;
             fo[0 * TY * (TX + 1)] = F.m;
             fo[1 * TY * (TX + 1)] = F.e;
             fo[2 * TY * (TX + 1)] = F.mn;  // x momentum
             fo[3 * TY * (TX + 1)] = F.mt;  // y momentum
-            umax_x = max_nonneg(umax_x, UU);
+            umax_x = max_nonneg(umax_x, value_of(UU));
         } else {
-            double* fo = fy + ly * TX + lx;
+            T* fo = fy + ly * TX + lx;
             fo[0 * (TY + 1) * TX] = F.m;
             fo[1 * (TY + 1) * TX] = F.e;
             fo[2 * (TY + 1) * TX] = F.mt;  // x momentum
             fo[3 * (TY + 1) * TX] = F.mn;  // y momentum
-            umax_y = max_nonneg(umax_y, UU);
+            umax_y = max_nonneg(umax_y, value_of(UU));
         }
     }
     __syncthreads();
@@ -293,44 +329,47 @@ __device__ __noinline__ void euler_tile(const Params& P, const CPlanes& in, cons
         const int ly = i / TX, lx = i - ly * TX;
         const int gx = tx0 + lx, gy = ty0 + ly;
         if (gx >= N || gy >= M) continue;
-        const double* c = prim + (ly + H) * SX + (lx + H);
-        const double r = c[0], p = c[SY * SX], u = c[2 * SY * SX], v = c[3 * SY * SX];
+        const T* c = prim + (ly + H) * SX + (lx + H);
+        const T r = c[0], p = c[SY * SX], u = c[2 * SY * SX], v = c[3 * SY * SX];
         const long long k = (long long)gy * N + gx;
         if (P.frozen && !cell_active(P, gx, gy)) {  // the faces' own test
             if (!dt_only) {
-                out.f[0][k] = r; out.f[1][k] = p; out.f[2][k] = u; out.f[3][k] = v;
+                store_cell(out, k, 0, r); store_cell(out, k, 1, p);
+                store_cell(out, k, 2, u); store_cell(out, k, 3, v);
             }
             continue;
         }
         any_active = true;
         if (dt_only) continue;
-        const double* fxc = fx + ly * (TX + 1) + lx;
-        const double* fyc = fy + ly * TX + lx;
-        double d[NF];
+        const T* fxc = fx + ly * (TX + 1) + lx;
+        const T* fyc = fy + ly * TX + lx;
+        T d[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            const double* a = fxc + f * TY * (TX + 1);
-            const double* b = fyc + f * (TY + 1) * TX;
+            const T* a = fxc + f * TY * (TX + 1);
+            const T* b = fyc + f * (TY + 1) * TX;
             d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
         }
-        if (aux != nullptr) {  // the recording of the adjoint: the flux differences used
-            const long long KK = (long long)N * M;
+        if constexpr (std::is_same<T, double>::value) {
+            if (aux != nullptr) {  // the recording of the adjoint: the flux differences used
+                const long long KK = (long long)N * M;
 #pragma unroll
-            for (int f = 0; f < NF; ++f) aux[f * KK + k] = d[f];
+                for (int f = 0; f < NF; ++f) aux[f * KK + k] = d[f];
+            }
         }
-        double r2 = r - d[0];
-        if (le_zero(r2)) { r2 = 0.0001; ++nfl_r; }
-        const double E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
-        const double inv = rcp_fast(r2);
-        const double u2 = fma(r, u, -d[2]) * inv;
-        const double v2 = fma(r, v, -d[3]) * inv;
-        double p2 = fma(-0.5 * r2, fma(u2, u2, v2 * v2), E - d[1]) * P.gm1;
-        if (le_zero(p2)) { p2 = 0.000001; ++nfl_p; }
+        T r2 = r - d[0];
+        if (le_zero(r2)) { r2 = cst<T>(0.0001); ++nfl_r; }
+        const T E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
+        const T inv = rcp_fast(r2);
+        const T u2 = fma(r, u, -d[2]) * inv;
+        const T v2 = fma(r, v, -d[3]) * inv;
+        T p2 = fma(-0.5 * r2, fma(u2, u2, v2 * v2), E - d[1]) * P.gm1;
+        if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
         if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2)) ++nbad;
-        out.f[0][k] = r2;
-        out.f[1][k] = p2;
-        out.f[2][k] = u2;
-        out.f[3][k] = v2;
+        store_cell(out, k, 0, r2);
+        store_cell(out, k, 1, p2);
+        store_cell(out, k, 2, u2);
+        store_cell(out, k, 3, v2);
     }
     res.umax_x = umax_x;
     res.umax_y = umax_y;
@@ -356,10 +395,25 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
                                                         double* aux) {
     extern __shared__ double smem[];
     TileResult r;
-    euler_tile<ORDER, TX, TY>(P, in, out, blockIdx.x * TX, (blockIdx.y + P.tile_row0) * TY,
-                              *T_do_ptr, dt_only, smem, r, aux);
+    euler_tile<double, ORDER, TX, TY>(P, in, out, blockIdx.x * TX,
+                                      (blockIdx.y + P.tile_row0) * TY, *T_do_ptr, dt_only, smem,
+                                      r, aux);
     add_counters(ctr, r);
     block_dt_and_rotate<NT>(P, r.umax_x, r.umax_y, r.any_active, T_bits, rot, P.tile_nblocks);
+}
+
+// Tangent of one step: (U, dU) -> (U', dU') with the dt read from *T_do_ptr (held fixed):
+// the same tile instantiated with Dual values, on the forward step's 32 x 16 tiles.
+template <int ORDER>
+__global__ void __launch_bounds__(NT) euler_tangent_kernel(Params P, CPlanes in, CPlanes din,
+                                                           Planes out, Planes dout,
+                                                           const double* __restrict__ T_do_ptr) {
+    extern __shared__ __align__(16) double smem[];
+    TileResult r;
+    const DualIn I{in, din};
+    const DualOut O{out, dout};
+    euler_tile<Dual, ORDER, 32, 16>(P, I, O, blockIdx.x * 32, blockIdx.y * 16, *T_do_ptr, 0,
+                                    reinterpret_cast<Dual*>(smem), r, nullptr);
 }
 
 // Persistent batched step: CTAs stride over the flattened (grid, tile) work list; each tile
@@ -395,7 +449,8 @@ __global__ void __launch_bounds__(NT) euler_batch_kernel(const BatchGrid* __rest
         const int tx0 = (tile % g.tiles_x) * TX, ty0 = (tile / g.tiles_x) * TY;
         const double T_do = g.sc->T_do;
         TileResult r;
-        euler_tile<ORDER, TX, TY>(g.P, in, out, tx0, ty0, T_do, dt_only, smem, r, nullptr);
+        euler_tile<double, ORDER, TX, TY>(g.P, in, out, tx0, ty0, T_do, dt_only, smem, r,
+                                          nullptr);
         add_counters(dt_only ? nullptr : g.sc, r);
         block_dt_and_rotate<NT>(g.P, r.umax_x, r.umax_y, r.any_active, &g.sc->T_bits,
                                 dt_only ? nullptr : g.sc, (unsigned int)g.ntiles);
@@ -488,6 +543,14 @@ int euler_batch_blocks_per_sm(int order, int variant) {
 
 cudaError_t prepare_euler_fast() {
     cudaError_t e = set_attrs<1, 32, 16>();
+    if (e == cudaSuccess)  // Dual tiles: twice the bytes of the double ones
+        e = cudaFuncSetAttribute(euler_tangent_kernel<1>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(2 * Shape<1, 32, 16>::bytes));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(euler_tangent_kernel<2>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(2 * Shape<2, 32, 16>::bytes));
     if (e == cudaSuccess) e = set_attrs<2, 32, 16>();
     if (e == cudaSuccess) e = set_attrs<1, 32, 8>();
     if (e == cudaSuccess) e = set_attrs<2, 32, 8>();
@@ -513,6 +576,19 @@ cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& 
                               const double* T_do, unsigned long long* T_bits, Scalars* rot,
                               Scalars* ctr, int dt_only, cudaStream_t st) {
     return launch_euler_fast_v(0, P, in, out, T_do, T_bits, rot, ctr, dt_only, st);
+}
+
+cudaError_t launch_euler_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
+                                 const Planes& out, const Planes& dout, const double* T_do,
+                                 cudaStream_t st) {
+    const dim3 grid((P.N + 31) / 32, (P.M + 15) / 16);
+    if (P.order == 1)
+        euler_tangent_kernel<1><<<grid, NT, 2 * Shape<1, 32, 16>::bytes, st>>>(P, in, din, out,
+                                                                              dout, T_do);
+    else
+        euler_tangent_kernel<2><<<grid, NT, 2 * Shape<2, 32, 16>::bytes, st>>>(P, in, din, out,
+                                                                              dout, T_do);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
@@ -550,7 +626,7 @@ __global__ void euler_face_probe_kernel(Params P, long long n, int axis,
     const double* b = R + 4 * i;
     const bool isx = axis == 0;
     double UU;
-    const FluxE F =
+    const FluxE<double> F =
         P.method == GD_METHOD_HLL
             ? hll_local(a[0], a[1], isx ? a[2] : a[3], isx ? a[3] : a[2], b[0], b[1],
                         isx ? b[2] : b[3], isx ? b[3] : b[2], P, UU)

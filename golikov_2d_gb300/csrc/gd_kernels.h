@@ -15,6 +15,10 @@ cudaError_t prepare_mhd_fast();
 // Fast face-once step.  `rot` (may be null) receives the fused funk_time rotation by the
 // last block; `ctr` (may be null) receives floor / non-finite counters.  dt_only != 0
 // computes only the dt minimum.
+// Tangent of one Euler step (value and derivative planes), dt read from *T_do.
+cudaError_t launch_euler_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
+                                 const Planes& out, const Planes& dout, const double* T_do,
+                                 cudaStream_t st);
 // The Euler step (variant 0) writing its flux differences d[0..3] per cell to `aux`.
 cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
                                   const double* T_do, unsigned long long* T_bits, Scalars* rot,

@@ -228,7 +228,7 @@ gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
  * floors are differentiated along the branch the forward values take.  Supported: MHD with
  * HLLD or Euler with HLLC, order 2, Cartesian, periodic on all sides, fast mode, no frozen
  * cells (the Orszag-Tang and Kelvin-Helmholtz configurations); other configurations return
- * GD_ERR_UNSUPPORTED, and so does gd_tangent for Euler.  All vectors are device pointers in
+ * GD_ERR_UNSUPPORTED.  All vectors are device pointers in
  * the reference AoS layout (d/ds: K x 2, d/du: K x 2, d/dB: K x 3, Gaussian B; for Euler
  * the d/dB pointers may be null).
  *

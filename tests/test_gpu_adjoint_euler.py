@@ -1,7 +1,9 @@
 """Discrete adjoint of the fast Euler step (HLLC, minmod TVD, periodic): the recording is the
 plain run, the replay reproduces it, the gradient is the same for any checkpoint interval and
-for repeated sweeps, and it agrees with FP64 central finite differences (relative difference
-<= 1e-6) on a smooth periodic state, the Euler counterpart of tests/test_gpu_adjoint.py.  The
+for repeated sweeps, it satisfies the dot-product identity with the forward-mode tangent
+(relative 1e-10, also at exact minmod and wave-speed ties), and it
+agrees with FP64 central finite differences (relative difference <= 1e-6) on a smooth
+periodic state: the Euler counterpart of tests/test_gpu_adjoint.py.  The
 map is only piecewise smooth (minmod choices, wave-speed min / max, star regions): a direction
 over the bound at eps = 1e-7 is retaken at 1e-8, keeping the closer quotient, as there."""
 import numpy as np
@@ -147,11 +149,46 @@ def test_gradient_matches_central_differences(cuda):
     sol.close()
 
 
-def test_euler_tangent_is_unsupported(cuda):
+def jvp(sol, vs, vu):
     import torch
-    cfg, sol, U0, _ = setup(16, 3, 3)
-    z = [torch.zeros_like(dev(x)) for x in U0]
-    with pytest.raises(g.GdError) as e:
-        sol.tangent(z[0], z[1], None, z[0].clone(), z[1].clone(), None)
-    assert e.value.status == 5
+    o = [torch.zeros_like(dev(x)) for x in (vs, vu)]
+    sol.tangent(dev(vs), dev(vu), None, o[0], o[1], None)
+    torch.cuda.synchronize()
+    return [x.cpu().numpy() for x in o]
+
+
+def test_tangent_adjoint_dot_product(cuda):
+    """<lam, J v> = <J^T lam, v> between the forward-mode tangent (the Euler tile instantiated
+    with Dual values) and the reverse sweep, both hand-written: relative 1e-10."""
+    cfg, sol, U0, _ = setup(48, 12, 5)
+    rng = np.random.default_rng(1)
+    lam = [rng.standard_normal(x.shape) for x in U0]
+    v = [rng.standard_normal(x.shape) for x in U0]
+    a, b = dot(lam, jvp(sol, *v)), dot(vjp(sol, *lam), v)
+    assert abs(a - b) <= 1e-10 * max(abs(a), abs(b)), (a, b)
+    sol.close()
+
+
+def test_tangent_adjoint_dot_product_at_ties(cuda):
+    """The Kelvin-Helmholtz shear layer without its perturbation (v_y = 0): a contact at
+    rest, which the HLLC step keeps exactly, so every minmod choice (minmod(0, 0)) and every
+    wave-speed min / max (equal left and right states) stays an exact tie; the tangent and
+    the adjoint break them the same way, so the identity holds there too.  (Near ties are
+    another matter: the tangent computes its values in the Dual instantiation of the tile,
+    which may round an intermediate value differently from the forward step's, and a choice
+    within that rounding can then go the other way: on the perturbed layer after 4 steps,
+    40 of its 16384 input columns, in 3 x 3 patches at the interfaces.)"""
+    cfg, s, u, _ = problems.kelvin_helmholtz(64, 64)
+    u = u.copy()
+    u[:, 1] = 0.0
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, None)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.adj_forward(4, 2)
+    rng = np.random.default_rng(2)
+    lam = [rng.standard_normal(x.shape) for x in (s, u)]
+    v = [rng.standard_normal(x.shape) for x in (s, u)]
+    a, b = dot(lam, jvp(sol, *v)), dot(vjp(sol, *lam), v)
+    assert abs(a - b) <= 1e-10 * max(abs(a), abs(b)), (a, b)
     sol.close()
