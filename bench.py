@@ -648,6 +648,50 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
     return res
 
 
+def measure_adjoint_euler(g, torch, N=512, nsteps=100, every=10):
+    """The Euler (HLLC) adjoint's cost: Kelvin-Helmholtz N x N, `nsteps` steps with
+    checkpoints every `every`, one gradient (checkpointed forward + backward) against the
+    plain forward run of the same steps."""
+    from golikov_2d_gb300 import problems
+    stream = torch.cuda.current_stream()
+    cfg, s, u, _ = problems.kelvin_helmholtz(N, N)
+    sol = g.Solver(cfg)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+    def start():
+        sol.import_state(s, u, None)
+        sol.set_time(0.0, 0.0)
+        sol.init_dt()
+
+    def timed(fn):
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        fn()
+        z.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(z)
+
+    rng = np.random.default_rng(11)
+    lam = [dev(rng.standard_normal(x.shape)) for x in (s, u)]
+    out = [torch.zeros_like(x) for x in lam]
+    start()
+    sol.advance(3)
+    start()
+    ms_fwd = timed(lambda: sol.advance(nsteps))
+    start()
+    sol.adj_forward(nsteps, every)
+    sol.adj_backward(lam[0], lam[1], None, out[0], out[1], None)  # warm-up
+    start()
+    ms_rec = timed(lambda: sol.adj_forward(nsteps, every))
+    ms_bwd = timed(lambda: sol.adj_backward(lam[0], lam[1], None, out[0], out[1], None))
+    sol.close()
+    return {"workload": f"Kelvin-Helmholtz Euler {N}x{N}, HLLC + minmod, FP64, {nsteps} steps, "
+                        f"checkpoints every {every}",
+            "forward_ms": ms_fwd, "record_ms": ms_rec, "backward_ms": ms_bwd,
+            "gradient_cost_vs_forward": (ms_rec + ms_bwd) / ms_fwd}
+
+
 HANCOCK_WORKLOAD = ("MUSCL-Hancock step of Kernel_GKR (scheme as written), axisymmetric MHD, "
                     "HLLD, wind in ambient medium, 3226x1792 (the reference's production grid), "
                     "CFL 0.25, FP64")
@@ -1000,6 +1044,7 @@ def run_gb300(args):
     if args.adjoint:
         try:
             line["adjoint"] = measure_adjoint(g, torch)
+            line["adjoint"]["euler"] = measure_adjoint_euler(g, torch)
         except Exception as e:
             line["adjoint"] = {"unavailable": str(e)}
     if args.io:
