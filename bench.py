@@ -456,6 +456,31 @@ def adjoint_step_case(g, torch, N=512):
     return 0 if ok else 1
 
 
+def adjoint_step_euler_case(g, torch, N=512):
+    """The Euler counterpart for kernel profiles: Kelvin-Helmholtz N x N, 20 plain steps, a
+    10-step recording, one backward sweep and one tangent sweep."""
+    from golikov_2d_gb300 import problems
+    cfg, s, u, _ = problems.kelvin_helmholtz(N, N)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, None)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.advance(20)
+    sol.adj_forward(10, 10)
+    rng = np.random.default_rng(1)
+    lam = [torch.from_numpy(rng.standard_normal(x.shape)).cuda() for x in (s, u)]
+    out = [torch.zeros_like(x) for x in lam]
+    sol.adj_backward(lam[0], lam[1], None, out[0], out[1], None)
+    tan = [torch.zeros_like(x) for x in lam]
+    sol.tangent(lam[0], lam[1], None, tan[0], tan[1], None)
+    torch.cuda.synchronize()
+    ok = all(bool(torch.isfinite(x).all()) for x in out + tan)
+    sol.close()
+    print(json.dumps({"case": "adjoint-step-euler", "grid": f"{N}x{N}", "finite": ok}),
+          flush=True)
+    return 0 if ok else 1
+
+
 class AdjointHarness:
     """One Orszag-Tang grid with its solver and the device-side helpers of the gradient
     checks (device tensors in the reference AoS layout)."""
@@ -1079,8 +1104,9 @@ def main():
     ap.add_argument("--io", type=int, default=1)
     ap.add_argument("--hancock", type=int, default=1)
     ap.add_argument("--case", default="bench",
-                    choices=["bench", "adjoint-step", "io", "hancock"],
-                    help="adjoint-step: a short differentiation run for kernel profiles; "
+                    choices=["bench", "adjoint-step", "adjoint-step-euler", "io", "hancock"],
+                    help="adjoint-step (-euler): a short differentiation run of the MHD (Euler) "
+                         "step for kernel profiles; "
                          "io: the state-file measurement alone; hancock: the MUSCL-Hancock "
                          "measurement alone")
     args = ap.parse_args()
@@ -1092,6 +1118,10 @@ def main():
         import torch
         import golikov_2d_gb300 as g
         return adjoint_step_case(g, torch)
+    if args.case == "adjoint-step-euler":
+        import torch
+        import golikov_2d_gb300 as g
+        return adjoint_step_euler_case(g, torch)
     if args.case == "io":
         import torch
         import golikov_2d_gb300 as g
