@@ -403,7 +403,10 @@ __global__ void __launch_bounds__(NT) euler_fast_kernel(Params P, CPlanes in, Pl
 }
 
 // Tangent of one step: (U, dU) -> (U', dU') with the dt read from *T_do_ptr (held fixed):
-// the same tile instantiated with Dual values, on the forward step's 32 x 16 tiles.
+// the same tile instantiated with Dual values.  32 x 8 tiles: a Dual tile holds twice the
+// bytes of a double one (101 KB at second order), so two CTAs fit on an SM (at 32 x 16, 186 KB,
+// one).
+constexpr int kTanTX = 32, kTanTY = 8;
 template <int ORDER>
 __global__ void __launch_bounds__(NT) euler_tangent_kernel(Params P, CPlanes in, CPlanes din,
                                                            Planes out, Planes dout,
@@ -412,8 +415,9 @@ __global__ void __launch_bounds__(NT) euler_tangent_kernel(Params P, CPlanes in,
     TileResult r;
     const DualIn I{in, din};
     const DualOut O{out, dout};
-    euler_tile<Dual, ORDER, 32, 16>(P, I, O, blockIdx.x * 32, blockIdx.y * 16, *T_do_ptr, 0,
-                                    reinterpret_cast<Dual*>(smem), r, nullptr);
+    euler_tile<Dual, ORDER, kTanTX, kTanTY>(P, I, O, blockIdx.x * kTanTX, blockIdx.y * kTanTY,
+                                            *T_do_ptr, 0, reinterpret_cast<Dual*>(smem), r,
+                                            nullptr);
 }
 
 // Persistent batched step: CTAs stride over the flattened (grid, tile) work list; each tile
@@ -546,11 +550,11 @@ cudaError_t prepare_euler_fast() {
     if (e == cudaSuccess)  // Dual tiles: twice the bytes of the double ones
         e = cudaFuncSetAttribute(euler_tangent_kernel<1>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(2 * Shape<1, 32, 16>::bytes));
+                                 (int)(2 * Shape<1, kTanTX, kTanTY>::bytes));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(euler_tangent_kernel<2>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(2 * Shape<2, 32, 16>::bytes));
+                                 (int)(2 * Shape<2, kTanTX, kTanTY>::bytes));
     if (e == cudaSuccess) e = set_attrs<2, 32, 16>();
     if (e == cudaSuccess) e = set_attrs<1, 32, 8>();
     if (e == cudaSuccess) e = set_attrs<2, 32, 8>();
@@ -581,13 +585,13 @@ cudaError_t launch_euler_fast(const Params& P, const CPlanes& in, const Planes& 
 cudaError_t launch_euler_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
                                  const Planes& out, const Planes& dout, const double* T_do,
                                  cudaStream_t st) {
-    const dim3 grid((P.N + 31) / 32, (P.M + 15) / 16);
+    const dim3 grid((P.N + kTanTX - 1) / kTanTX, (P.M + kTanTY - 1) / kTanTY);
     if (P.order == 1)
-        euler_tangent_kernel<1><<<grid, NT, 2 * Shape<1, 32, 16>::bytes, st>>>(P, in, din, out,
-                                                                              dout, T_do);
+        euler_tangent_kernel<1><<<grid, NT, 2 * Shape<1, kTanTX, kTanTY>::bytes, st>>>(
+            P, in, din, out, dout, T_do);
     else
-        euler_tangent_kernel<2><<<grid, NT, 2 * Shape<2, 32, 16>::bytes, st>>>(P, in, din, out,
-                                                                              dout, T_do);
+        euler_tangent_kernel<2><<<grid, NT, 2 * Shape<2, kTanTX, kTanTY>::bytes, st>>>(
+            P, in, din, out, dout, T_do);
     return cudaGetLastError();
 }
 
