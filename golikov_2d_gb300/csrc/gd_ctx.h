@@ -13,15 +13,29 @@ namespace gd {
 // work buffers of the reverse and tangent sweeps.
 // gd_step_host: the two copy streams, the events of the band pipeline and the AoS staging
 // of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
+// The banded step is captured once per (host buffers, current plane set) into a CUDA graph
+// and replayed: a graph launch puts all of a step's copies and launches on the GPU at once,
+// where enqueuing them one API call at a time (a dozen per band) paces a short step.
 constexpr int kMaxBands = 64;
 constexpr int kCompStreams = 3;  // the caller's stream and two more
+constexpr int kStepGraphs = 4;   // cached step graphs (two per ping-pong pair of host buffers)
+struct StepGraph {
+    const void* buf[6] = {};  // s, u, b, s2, u2, b2
+    int cur = -1;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;  // kernel launches one replay makes
+};
 struct HostPipe {
     cudaStream_t up = nullptr, down = nullptr, edge = nullptr;
     cudaStream_t comp[kCompStreams - 1] = {};
+    cudaStream_t cap = nullptr;  // the origin stream of the captures
     cudaEvent_t start = nullptr, down_done = nullptr, comp_done = nullptr, edge_done = nullptr;
+    cudaEvent_t up_done = nullptr;
     cudaEvent_t ev_up[kMaxBands] = {}, ev_out[kMaxBands] = {};
     double* aos_in = nullptr;
     double* aos_out = nullptr;
+    StepGraph graphs[kStepGraphs];
+    int next_graph = 0;  // slot the next capture replaces
 };
 
 struct AdjStore {

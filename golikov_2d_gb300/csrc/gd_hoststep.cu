@@ -9,7 +9,9 @@
 // the caller's stream band k is stepped as soon as its neighbours' rows (the stencil's halo)
 // are there; its output is converted back and goes down on a second copy stream while later
 // bands are stepped.  The two copy directions and the SMs work at once, so a step costs
-// about the step itself plus one band of each copy.  The step is the same kernel with the
+// about the step itself plus one band of each copy.  The whole banded step is captured into
+// a CUDA graph per (host buffers, plane set) and replayed, so its few hundred copies and
+// launches reach the GPU in one submission.  The step is the same kernel with the
 // same arithmetic, launched once per band (Params::tile_row0 / tile_rows); the bands' blocks
 // share one dt rotation ticket, so dt, time and counters are those of gd_advance(1).
 #include <cstring>
@@ -56,7 +58,8 @@ cudaError_t pipe_create(gd_ctx* ctx) {
     HS_TRY(cudaStreamCreateWithPriority(&p->down, cudaStreamNonBlocking, prio_high));
     HS_TRY(cudaStreamCreateWithPriority(&p->edge, cudaStreamNonBlocking, prio_high));
     for (cudaStream_t& c : p->comp) HS_TRY(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done, &p->edge_done})
+    HS_TRY(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&p->start, &p->down_done, &p->comp_done, &p->edge_done, &p->up_done})
         HS_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int k = 0; k < gd::kMaxBands; ++k) {
         HS_TRY(cudaEventCreateWithFlags(&p->ev_up[k], cudaEventDisableTiming));
@@ -255,13 +258,59 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
         HS_TRY(cudaEventRecord(p->edge_done, p->edge));
         for (int k = 0; k < B; ++k) HS_TRY(enqueue_down(k));
     }
-    for (cudaStream_t c : p->comp) {
-        HS_TRY(cudaEventRecord(p->comp_done, c));
+    // the caller's stream joins every stream the step used (a capture must end with all
+    // of them joined; a stream no band used never joined it)
+    for (int c = 1; c < B && c < gd::kCompStreams; ++c) {
+        HS_TRY(cudaEventRecord(p->comp_done, p->comp[c - 1]));
         HS_TRY(cudaStreamWaitEvent(st, p->comp_done, 0));
     }
     if (hk) HS_TRY(cudaStreamWaitEvent(st, p->edge_done, 0));
+    HS_TRY(cudaEventRecord(p->up_done, p->up));
+    HS_TRY(cudaStreamWaitEvent(st, p->up_done, 0));
     HS_TRY(cudaEventRecord(p->down_done, p->down));
     HS_TRY(cudaStreamWaitEvent(st, p->down_done, 0));
+    return cudaSuccess;
+}
+
+// The graph of the banded step for these host buffers and the current plane set: a cached
+// one, or a new capture of banded_step (replacing the oldest).  Capturing executes nothing.
+cudaError_t step_graph(gd_ctx* ctx, const double* s, const double* u, const double* b,
+                       double* s2, double* u2, double* b2, int TX, int TY, gd::StepGraph** out) {
+    gd::HostPipe* p = ctx->pipe;
+    const void* buf[6] = {s, u, b, s2, u2, b2};
+    for (gd::StepGraph& g : p->graphs) {
+        if (!g.exec || g.cur != ctx->cur) continue;
+        bool same = true;
+        for (int i = 0; i < 6; ++i) same = same && g.buf[i] == buf[i];
+        if (same) {
+            *out = &g;
+            return cudaSuccess;
+        }
+    }
+    gd::StepGraph& g = p->graphs[p->next_graph];
+    p->next_graph = (p->next_graph + 1) % gd::kStepGraphs;
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = gd::StepGraph{};
+    const long long l0 = ctx->launches;
+    HS_TRY(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = banded_step(ctx, s, u, b, s2, u2, b2, TX, TY, p->cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(p->cap, &graph);
+    const long long n = ctx->launches - l0;
+    ctx->launches = l0;  // counted when a replay runs
+    if (e == cudaSuccess) e = ee;
+    // the kernel nodes keep the priorities of the streams they were captured on
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        g.exec = nullptr;
+        return e;
+    }
+    for (int i = 0; i < 6; ++i) g.buf[i] = buf[i];
+    g.cur = ctx->cur;
+    g.launches = n;
+    *out = &g;
     return cudaSuccess;
 }
 
@@ -271,9 +320,11 @@ namespace gd {
 void pipe_free(gd_ctx* ctx) {
     HostPipe* p = ctx->pipe;
     if (!p) return;
+    for (StepGraph& g : p->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     cudaFree(p->aos_in);
     cudaFree(p->aos_out);
-    for (cudaEvent_t e : {p->start, p->down_done, p->comp_done, p->edge_done})
+    for (cudaEvent_t e : {p->start, p->down_done, p->comp_done, p->edge_done, p->up_done})
         if (e) cudaEventDestroy(e);
     for (int k = 0; k < kMaxBands; ++k) {
         if (p->ev_up[k]) cudaEventDestroy(p->ev_up[k]);
@@ -284,6 +335,7 @@ void pipe_free(gd_ctx* ctx) {
     for (cudaStream_t c : p->comp)
         if (c) cudaStreamDestroy(c);
     if (p->edge) cudaStreamDestroy(p->edge);
+    if (p->cap) cudaStreamDestroy(p->cap);
     delete p;
     ctx->pipe = nullptr;
 }
@@ -318,7 +370,10 @@ extern "C" gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u,
         return r;
     }
     cudaError_t e = pipe_init(ctx);
-    if (e == cudaSuccess) e = banded_step(ctx, s, u, b, s2, u2, b2, TX, TY, st);
+    gd::StepGraph* g = nullptr;
+    if (e == cudaSuccess) e = step_graph(ctx, s, u, b, s2, u2, b2, TX, TY, &g);
+    if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, st);
+    if (e == cudaSuccess) ctx->launches += g->launches;
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return gd::cuda_error(e);
     ctx->cur ^= 1;

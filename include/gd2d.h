@@ -203,7 +203,10 @@ gd_status gd_advance_to(gd_ctx* ctx, double t_end, long long max_steps, int use_
  * buffers the grid is moved in bands of tile rows, each band's upload, step and download
  * overlapping the others' on two copy streams, `stream` and two more compute streams;
  * otherwise (GD_DT_CURRENT, pageable buffers, grids of fewer than four tile rows) the three
- * calls run in turn.
+ * calls run in turn.  The banded step is captured into a CUDA graph the first time a set
+ * of buffer addresses is used with each of the two internal state buffers, and replayed
+ * after that (the last four such graphs are kept): the buffers are checked to be pinned
+ * at every call.
  * Returns after the result is in s2, u2, b2. */
 gd_status gd_step_host(gd_ctx* ctx, const double* s, const double* u, const double* b,
                        double* s2, double* u2, double* b2, gd_stream stream);

@@ -71,3 +71,66 @@ def test_step_host_equals_import_advance_export(cuda, case, pin):
         # the next step starts from this result, as the reference loop does
         hs, hu, hb = (conv(np.asarray(x)) if x is not None else None for x in (os_, ou, ob))
     sol.close()
+
+
+def run_reference(case, n):
+    cfg, s, u, b = CASES[case]()
+    return cfg, s, u, b, reference_steps(cfg, s, u, b, n)
+
+
+def check_step(sol, out, r, mhd, tag):
+    got = [np.asarray(x) for x in out[:2]] + ([np.asarray(out[2])] if mhd else [])
+    want = [r[0], r[1]] + ([r[2]] if mhd else [])
+    for x, y in zip(got, want):
+        assert np.array_equal(x, y), tag
+    st = sol.stats()
+    assert st.dt == r[3] and st.t_state == r[4], tag
+
+
+@pytest.mark.parametrize("case", ["kh512_periodic", "ot256_mhd_periodic", "wind_native",
+                                  "hancock_fast", "sod256_parity"])
+def test_step_host_graph_replays(cuda, case):
+    """The step graphs are replayed when the same host buffers come back: ping-pong between
+    two buffer sets (the reference loop's s -> s2 -> s) for 7 steps, then the same input
+    and output buffers every step (the input refilled on the host) for 6 more; every step
+    equals gd_advance(1), and each step counts the launches of a directly enqueued one."""
+    cfg, s, u, b, ref = run_reference(case, 13)
+    mhd = b is not None
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(1e-4, 0.0)
+    A = [pinned(x) for x in (s, u, b)]
+    B = [pinned(np.zeros_like(x)) if x is not None else None for x in (s, u, b)]
+    per_step = None
+    for k in range(7):
+        src, dst = (A, B) if k % 2 == 0 else (B, A)
+        l0 = sol.launch_count()
+        sol.step_host(*src, *dst)
+        n = sol.launch_count() - l0
+        assert per_step is None or n == per_step, (case, k, n, per_step)
+        per_step = n
+        check_step(sol, dst, ref[k], mhd, (case, k))
+    # B holds the result of the last step (k = 6): step from B into A, then copy A into B
+    for k in range(7, 13):
+        sol.step_host(*B, *A)
+        check_step(sol, A, ref[k], mhd, (case, k))
+        for x, y in zip(A, B):
+            if x is not None:
+                y.copy_(x)
+    sol.close()
+
+
+def test_step_host_graph_cache_eviction(cuda):
+    """Five buffer sets in rotation (more than the cached graphs): captures replace the
+    oldest graphs and every step still equals gd_advance(1)."""
+    cfg, s, u, b, ref = run_reference("kh512_periodic", 11)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(1e-4, 0.0)
+    sets = [[pinned(s), pinned(u)]] + [[pinned(np.zeros_like(s)), pinned(np.zeros_like(u))]
+                                      for _ in range(4)]
+    for k in range(11):
+        src, dst = sets[k % 5], sets[(k + 1) % 5]
+        sol.step_host(src[0], src[1], None, dst[0], dst[1], None)
+        check_step(sol, dst, ref[k], False, k)
+    sol.close()
