@@ -23,6 +23,11 @@ CASES = {
     "hancock_parity": lambda: problems.hancock_wind(160, 96, mode=g.MODE_PARITY),
     "hancock_fast": lambda: problems.hancock_wind(160, 96),
     "hancock_fast_ragged": lambda: problems.hancock_wind(131, 77, scheme=g.SCHEME_HANCOCK),
+    # grids of many bands (16 to 53)
+    "kh2048x1024_many_bands": lambda: problems.kelvin_helmholtz(2048, 1024),
+    "ot1024_many_bands": lambda: problems.orszag_tang(1024, 1024),
+    "hancock_fast_many_bands": lambda: problems.hancock_wind(1024, 640),
+    "sod1024_parity_many_bands": lambda: problems.sod(1024, 1024, mode=g.MODE_PARITY),
 }
 
 
@@ -88,7 +93,7 @@ def check_step(sol, out, r, mhd, tag):
 
 
 @pytest.mark.parametrize("case", ["kh512_periodic", "ot256_mhd_periodic", "wind_native",
-                                  "hancock_fast", "sod256_parity"])
+                                  "hancock_fast", "sod256_parity", "ot1024_many_bands"])
 def test_step_host_graph_replays(cuda, case):
     """The step graphs are replayed when the same host buffers come back: ping-pong between
     two buffer sets (the reference loop's s -> s2 -> s) for 7 steps, then the same input
