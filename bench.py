@@ -215,18 +215,25 @@ def dist_info():
     return ws, rank, local
 
 
-def fp64_roofline(g, workload, cells_per_s, torch):
+def fp64_pipe_peak(torch, sm_mhz):
+    """FP64 pipe peak (ops/s, FMA = 1) at the SM clock sampled during the timed region: 2 FP64
+    operations per clock per SM; the maximum clock (2070 MHz) where no sample was taken."""
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = float(sm_mhz) if sm_mhz else 2070.0
+    src = "median SM clock sampled in the timed region" if sm_mhz else "maximum SM clock"
+    return 2.0 * sms * mhz * 1e6, f"2 ops/clk/SM x {sms} SMs x {mhz:.0f} MHz ({src})"
+
+
+def fp64_roofline(g, workload, cells_per_s, torch, sm_mhz=None):
     """FP64 roofline of the step kernel.  The pipe peak is 2 FP64 operations per clock per
-    SM (FMA counted once), i.e. 2 x SMs x SM clock; `gd_probe_fp64_peak` gives what a
-    register-resident DFMA loop reaches on the same GPU.  FP64 operations per cell come from
-    the committed ncu capture (profiles/ncu_traffic.txt)."""
-    props = torch.cuda.get_device_properties(torch.cuda.current_device())
-    sms = props.multi_processor_count
+    SM (FMA counted once), i.e. 2 x SMs x the SM clock sampled while the step was timed;
+    `gd_probe_fp64_peak` gives what a register-resident DFMA loop reaches on the same GPU.
+    FP64 operations per cell come from the committed ncu capture (profiles/ncu_traffic.txt)."""
     probe = g.probe_fp64_peak()                       # FLOP/s, FMA = 2
-    pipe_peak_ops = 2.0 * sms * 2.07e9                # FP64 ops/s at the max SM clock
+    pipe_peak_ops, src = fp64_pipe_peak(torch, sm_mhz)
     out = {"unit": "FP64 ops/s (FMA = 1 op)", "pipe_peak": pipe_peak_ops,
            "dfma_loop_peak": probe / 2.0,
-           "pipe_peak_source": f"2 ops/clk/SM x {sms} SMs x 2070 MHz",
+           "pipe_peak_source": src,
            "dfma_loop_source": "gd_probe_fp64_peak in this run"}
     per_cell = ncu_fp64_per_cell(workload)
     if per_cell is not None:
@@ -740,15 +747,17 @@ def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792
         torch.cuda.synchronize()
         l0 = sol.launch_count()
         a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        sol.advance(k)
-        z.record(stream)
-        torch.cuda.synchronize()
+        with ClockSampler() as clk:
+            a.record(stream)
+            sol.advance(k)
+            z.record(stream)
+            torch.cuda.synchronize()
         ms = a.elapsed_time(z) / k
         st = sol.stats(allow_nonfinite=True)
         entry = {"value": N * M / (ms * 1e-3), "ms_per_step": ms, "steps": k,
                  "gpu_launches": sol.launch_count() - l0, "nonfinite": st.nonfinite,
-                 "rho_floor_hits": st.rho_floor_hits, "p_floor_hits": st.p_floor_hits}
+                 "rho_floor_hits": st.rho_floor_hits, "p_floor_hits": st.p_floor_hits,
+                 "clocks": clk.summary()}
         if mode == g.MODE_FAST:
             hs, hu, hb = (torch.from_numpy(x).pin_memory() for x in (s, u, b))
             hs2, hu2, hb2 = (torch.empty_like(x).pin_memory() for x in (hs, hu, hb))
@@ -766,10 +775,10 @@ def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792
                             "d2h_bytes_per_step": io_bytes}
             ops = ncu_fp64_per_cell("hancock3226")
             if ops is not None:
-                pipe = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07e9
+                pipe, src = fp64_pipe_peak(torch, entry["clocks"]["sm_mhz"])
                 entry["fp64"] = {"ops_per_cell": ops, "achieved": ops * entry["value"],
                                  "pipe_peak": pipe, "frac": ops * entry["value"] / pipe,
-                                 "ops_source": OPS_SOURCE}
+                                 "pipe_peak_source": src, "ops_source": OPS_SOURCE}
             peak_gbs, kind = measured_peaks()
             ach = N * M * 7 * 16 / (ms * 1e-3) / 1e9
             entry["hbm"] = {"achieved": ach, "peak": peak_gbs, "unit": "GB/s",
@@ -820,7 +829,19 @@ def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
     return {"value": cfg.N * cfg.M * nsteps / dt, "unit": "cell-updates/s", "cores": threads,
             "kind": "port",
             "sample": f"{nsteps} full steps of {workload} ({cfg.N}x{cfg.M}) on {threads} host "
-                      f"threads, oracle/gd_oracle.c -O2 OpenMP, {dt:.2f} s"}
+                      f"threads, oracle/gd_oracle.c -O3 OpenMP, {dt:.2f} s"}
+
+
+def workload_config(workload, cfg, ws):
+    """The `config` object of both arms' lines: the same workload, the same dict."""
+    K = cfg.N * cfg.M
+    state_bytes = K * cfg.nfields * 8
+    flush_l2 = 2 * state_bytes <= 2 * L2_BYTES
+    return {"workload": WORKLOADS[workload], "cells": K, "fields": cfg.nfields,
+            "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "flushed before every timed step" if flush_l2 else
+                  f"state {2 * state_bytes / 2**20:.0f} MiB > L2 (129 MiB), no flush",
+            "steps_per_launch": 1, "dt": "lagged reference protocol, dt-only pre-pass"}
 
 
 def run_reference(args):
@@ -849,12 +870,13 @@ def run_reference(args):
         "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "cells": K, "parallelism": "replicas"},
+        "config": workload_config(args.workload, cfg, ws),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
                          "kind": "port",
                          "sample": f"{args.steps} full steps of {args.workload} after "
-                                   f"{args.warmup} warm-up steps, oracle/gd_oracle.c "
-                                   f"(restatement of the reference step) on {threads} threads"},
+                                   f"{args.warmup} warm-up steps, oracle/gd_oracle.c -O3 "
+                                   f"(restatement of the reference step, bit-identical to "
+                                   f"it) on {threads} threads"},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -1018,17 +1040,14 @@ def run_gb300(args):
     alg_bytes = K * bytes_per_cell(cfg)
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
     traffic = ncu_traffic(args.workload)
-    fp64 = fp64_roofline(g, args.workload, K / (ms_step * 1e-3), torch)
+    clocks = clk.summary()
+    fp64 = fp64_roofline(g, args.workload, K / (ms_step * 1e-3), torch, clocks["sm_mhz"])
     line = {
         "metric": "FP64 cell-updates/s", "value": value, "unit": "cell-updates/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "cells": K, "fields": cfg.nfields,
-                   "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed before every timed step" if flush_l2 else
-                         f"state {2 * state_bytes / 2**20:.0f} MiB > L2 (129 MiB), no flush",
-                   "steps_per_launch": 1, "dt": "lagged reference protocol, dt-only pre-pass"},
+        "config": workload_config(args.workload, cfg, ws),
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": achieved / peak_gbs,
@@ -1036,7 +1055,7 @@ def run_gb300(args):
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "FP64-issue bound on GB300; see fp64"},
         "fp64": fp64,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "e2e": e2e,
         "sim": {"t": stats.t, "dt": stats.dt, "steps": stats.steps,
                 "rho_floor_hits": stats.rho_floor_hits, "p_floor_hits": stats.p_floor_hits,
@@ -1044,7 +1063,10 @@ def run_gb300(args):
     }
     if args.secondary and args.workload != "ot1024":
         try:
-            c2, ms2, l2, st2 = time_workload("ot1024", args.steps, args.warmup, torch, g, True)
+            with ClockSampler(bus) as clk2:
+                c2, ms2, l2, st2 = time_workload("ot1024", args.steps, args.warmup, torch, g,
+                                                 True)
+            clocks2 = clk2.summary()
             K2 = c2.N * c2.M
             ach2 = K2 * bytes_per_cell(c2) / (ms2 * 1e-3) / 1e9
             line["secondary"] = {"workload": WORKLOADS["ot1024"], "value": K2 / (ms2 * 1e-3),
@@ -1053,7 +1075,9 @@ def run_gb300(args):
                                               "unit": "GB/s", "frac": ach2 / peak_gbs,
                                               "traffic": ncu_traffic("ot1024"),
                                               "l2_hit_pct": ncu_l2_hit_pct("ot1024")},
-                                 "fp64": fp64_roofline(g, "ot1024", K2 / (ms2 * 1e-3), torch),
+                                 "fp64": fp64_roofline(g, "ot1024", K2 / (ms2 * 1e-3), torch,
+                                                       clocks2["sm_mhz"]),
+                                 "clocks": clocks2,
                                  "l2": "flushed before every timed step",
                                  "gpu_launches": l2,
                                  "e2e": measure_e2e(g, torch, *make_problem("ot1024"))}

@@ -46,7 +46,7 @@ EXPORTS = (
     "gd_abi_version", "gd_step_ref", "gd_funk_time", "gd_import", "gd_export", "gd_set_time",
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
     "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
-    "gd_probe_fp64_peak", "gd_probe_faces", "gd_step_ref_static",
+    "gd_probe_fp64_peak", "gd_probe_faces", "gd_step_ref_static", "gd_alloc_counts",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
@@ -143,6 +143,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_probe_fp64_peak.argtypes = [ctypes.POINTER(d)]
     L.gd_probe_faces.argtypes = [i, i, d, i, ll, vp, vp, vp, vp, vp]
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
+    L.gd_alloc_counts.argtypes = [ctypes.POINTER(ll), ctypes.POINTER(ll)]
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
@@ -172,7 +173,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
                  "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_probe_faces",
-                 "gd_step_ref_static",
+                 "gd_step_ref_static", "gd_alloc_counts",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
@@ -507,3 +508,12 @@ def probe_fp64_peak() -> float:
     v = ctypes.c_double()
     _check(L.gd_probe_fp64_peak(ctypes.byref(v)), "gd_probe_fp64_peak")
     return v.value
+
+
+def alloc_counts() -> tuple[int, int]:
+    """(allocations, releases) of device and pinned-host memory the library has made in
+    this process (gd_alloc_counts)."""
+    L = load()
+    a, f = ctypes.c_longlong(), ctypes.c_longlong()
+    _check(L.gd_alloc_counts(ctypes.byref(a), ctypes.byref(f)), "gd_alloc_counts")
+    return a.value, f.value

@@ -19,15 +19,15 @@ namespace gd {
 void adj_free(gd_ctx* ctx) {
     AdjStore* a = ctx->adj;
     if (!a) return;
-    cudaFree(a->dts);
-    cudaFree(a->ckpt);
-    cudaFree(a->seg);
-    cudaFree(a->aux);
-    cudaFree(a->lam);
-    cudaFree(a->scratch);
-    cudaFree(a->tbits);
-    cudaFree(a->seg2);
-    cudaFree(a->aux2);
+    gd::dev_free(a->dts);
+    gd::dev_free(a->ckpt);
+    gd::dev_free(a->seg);
+    gd::dev_free(a->aux);
+    gd::dev_free(a->lam);
+    gd::dev_free(a->scratch);
+    gd::dev_free(a->tbits);
+    gd::dev_free(a->seg2);
+    gd::dev_free(a->aux2);
     for (cudaEvent_t e : {a->ev_start, a->ev_rec[0], a->ev_rec[1], a->ev_rev[0], a->ev_rev[1]})
         if (e) cudaEventDestroy(e);
     if (a->side) cudaStreamDestroy(a->side);
@@ -86,18 +86,18 @@ gd_status alloc_store(gd_ctx* ctx, int nsteps, int every, size_t state) {
     a->nsteps = nsteps;
     a->every = every;
     a->nckpt = (nsteps + every - 1) / every;
-    GD_TRY(cudaMalloc(&a->dts, sizeof(double) * nsteps));
-    GD_TRY(cudaMalloc(&a->ckpt, state * a->nckpt));
-    GD_TRY(cudaMalloc(&a->seg, state * (every + 1)));
+    GD_TRY(gd::dev_alloc(&a->dts, sizeof(double) * nsteps));
+    GD_TRY(gd::dev_alloc(&a->ckpt, state * a->nckpt));
+    GD_TRY(gd::dev_alloc(&a->seg, state * (every + 1)));
     const int naux = aux_planes(ctx);
-    GD_TRY(cudaMalloc(&a->aux, sizeof(double) * naux * (size_t)K * every));
-    GD_TRY(cudaMalloc(&a->lam, 2 * state));
+    GD_TRY(gd::dev_alloc(&a->aux, sizeof(double) * naux * (size_t)K * every));
+    GD_TRY(gd::dev_alloc(&a->lam, 2 * state));
     const int nscr = ctx->nf == 7 ? gd::adjoint_scratch_planes()
                                   : gd::adjoint_euler_scratch_planes();
-    GD_TRY(cudaMalloc(&a->scratch, sizeof(double) * (size_t)nscr * (size_t)K));
-    GD_TRY(cudaMalloc(&a->tbits, sizeof(double)));
-    GD_TRY(cudaMalloc(&a->seg2, state * (every + 1)));
-    GD_TRY(cudaMalloc(&a->aux2, sizeof(double) * naux * (size_t)K * every));
+    GD_TRY(gd::dev_alloc(&a->scratch, sizeof(double) * (size_t)nscr * (size_t)K));
+    GD_TRY(gd::dev_alloc(&a->tbits, sizeof(double)));
+    GD_TRY(gd::dev_alloc(&a->seg2, state * (every + 1)));
+    GD_TRY(gd::dev_alloc(&a->aux2, sizeof(double) * naux * (size_t)K * every));
     GD_TRY(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&a->ev_start, &a->ev_rec[0], &a->ev_rec[1], &a->ev_rev[0],
                            &a->ev_rev[1]})
@@ -125,6 +125,9 @@ extern "C" {
 gd_status gd_adj_forward(gd_ctx* ctx, int nsteps, int ckpt_every, gd_stream stream) {
     if (!ctx || nsteps < 1 || ckpt_every < 1) return GD_ERR_INVALID_ARG;
     if (!adj_supported(ctx)) return GD_ERR_UNSUPPORTED;
+    // the recording steps and the recomputed segments use the dt rotated by the previous
+    // step (GD_DT_LAGGED); under GD_DT_CURRENT the steps taken would not be the recorded map
+    if (ctx->dt_policy != GD_DT_LAGGED) return GD_ERR_UNSUPPORTED;
     const long long K = ctx->K;
     const int nf = ctx->nf;
     const int every = ckpt_every < nsteps ? ckpt_every : nsteps;

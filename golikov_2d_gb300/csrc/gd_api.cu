@@ -24,6 +24,8 @@ using gd::Scalars;
 
 namespace {
 std::atomic<int> g_last_cuda_error{0};
+// device / pinned-host allocations and releases made through the helpers below
+std::atomic<long long> g_allocs{0}, g_frees{0};
 
 gd_status cuda_fail(cudaError_t e) {
     g_last_cuda_error.store((int)e);
@@ -136,6 +138,25 @@ cudaError_t launch_step(gd_ctx* ctx, const Params& P, const CPlanes& in, const P
 
 namespace gd {
 gd_status cuda_error(cudaError_t e) { return cuda_fail(e); }
+
+cudaError_t dev_alloc_bytes(void** p, size_t bytes) {
+    g_allocs.fetch_add(1);
+    return cudaMalloc(p, bytes);
+}
+cudaError_t host_alloc_bytes(void** p, size_t bytes) {
+    g_allocs.fetch_add(1);
+    return cudaMallocHost(p, bytes);
+}
+cudaError_t dev_free(void* p) {
+    if (p == nullptr) return cudaSuccess;
+    g_frees.fetch_add(1);
+    return cudaFree(p);
+}
+cudaError_t host_free(void* p) {
+    if (p == nullptr) return cudaSuccess;
+    g_frees.fetch_add(1);
+    return cudaFreeHost(p);
+}
 // Configuration checks and launch parameters for entry points that have no context.
 gd_status validate_config(const gd_config* c) { return validate(c); }
 Params params_from_config(const gd_config& c) { return make_params(c); }
@@ -146,6 +167,13 @@ extern "C" {
 int gd_abi_version(void) { return GD_ABI_VERSION; }
 
 int gd_last_cuda_error(void) { return g_last_cuda_error.load(); }
+
+gd_status gd_alloc_counts(long long* allocs, long long* frees) {
+    if (!allocs || !frees) return GD_ERR_INVALID_ARG;
+    *allocs = g_allocs.load();
+    *frees = g_frees.load();
+    return GD_OK;
+}
 
 const char* gd_status_string(gd_status s) {
     switch (s) {
@@ -172,9 +200,9 @@ gd_status gd_create(const gd_config* cfg, gd_ctx** out) {
     ctx->K = (long long)cfg->N * cfg->M;
     cudaError_t e = cudaGetDevice(&ctx->device);
     const size_t plane_bytes = sizeof(double) * (size_t)ctx->K * ctx->nf;
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->state[0], plane_bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->state[1], plane_bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->sc, sizeof(Scalars));
+    if (e == cudaSuccess) e = gd::dev_alloc(&ctx->state[0], plane_bytes);
+    if (e == cudaSuccess) e = gd::dev_alloc(&ctx->state[1], plane_bytes);
+    if (e == cudaSuccess) e = gd::dev_alloc(&ctx->sc, sizeof(Scalars));
     if (e == cudaSuccess) e = cudaMemset(ctx->sc, 0, sizeof(Scalars));
     if (e == cudaSuccess) {
         Scalars h{};
@@ -214,11 +242,11 @@ gd_status gd_create(const gd_config* cfg, gd_ctx** out) {
 gd_status gd_destroy(gd_ctx* ctx) {
     if (!ctx) return GD_ERR_INVALID_ARG;
     for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
-    cudaFree(ctx->state[0]);
-    cudaFree(ctx->state[1]);
-    cudaFree(ctx->sc);
-    cudaFree(ctx->ref_planes);
-    cudaFree(ctx->aos);
+    gd::dev_free(ctx->state[0]);
+    gd::dev_free(ctx->state[1]);
+    gd::dev_free(ctx->sc);
+    gd::dev_free(ctx->ref_planes);
+    gd::dev_free(ctx->aos);
     gd::adj_free(ctx);
     gd::io_free(ctx);
     gd::pipe_free(ctx);
@@ -256,7 +284,7 @@ gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const doubl
     }
     cudaStream_t st = (cudaStream_t)stream;
     if (!ctx->ref_planes)
-        GD_CUDA(cudaMalloc(&ctx->ref_planes, sizeof(double) * 2 * (size_t)ctx->nf * ctx->K));
+        GD_CUDA(gd::dev_alloc(&ctx->ref_planes, sizeof(double) * 2 * (size_t)ctx->nf * ctx->K));
     const Planes pin = ctx->ref_plane_set(0), pout = ctx->ref_plane_set(1);
     GD_CUDA(gd::launch_aos_to_soa(s, u, b, pin, ctx->K, ctx->nf, st));
     ctx->launches += 1;
@@ -281,7 +309,7 @@ gd_status gd_import(gd_ctx* ctx, const double* s, const double* u, const double*
     cudaStream_t st = (cudaStream_t)stream;
     const double *ds = s, *du = u, *db = b;
     if (is_host) {
-        if (!ctx->aos) GD_CUDA(cudaMalloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
+        if (!ctx->aos) GD_CUDA(gd::dev_alloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
         double* hs = ctx->aos;
         double* hu = hs + 2 * ctx->K;
         double* hb = hu + 2 * ctx->K;
@@ -303,7 +331,7 @@ gd_status gd_export(gd_ctx* ctx, double* s, double* u, double* b, int is_host, g
     cudaStream_t st = (cudaStream_t)stream;
     double *ds = s, *du = u, *db = b;
     if (is_host) {
-        if (!ctx->aos) GD_CUDA(cudaMalloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
+        if (!ctx->aos) GD_CUDA(gd::dev_alloc(&ctx->aos, sizeof(double) * 7 * (size_t)ctx->K));
         ds = ctx->aos;
         du = ds + 2 * ctx->K;
         db = du + 2 * ctx->K;

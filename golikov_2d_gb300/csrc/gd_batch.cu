@@ -137,12 +137,12 @@ gd_status gd_batch_create(const gd_config* cfgs, int ngrids, gd_batch** out) {
     }
     b->pool_doubles = off;
     cudaError_t e = gd::prepare_euler_fast();
-    if (e == cudaSuccess) e = cudaMalloc(&b->pool[0], sizeof(double) * off);
-    if (e == cudaSuccess) e = cudaMalloc(&b->pool[1], sizeof(double) * off);
+    if (e == cudaSuccess) e = gd::dev_alloc(&b->pool[0], sizeof(double) * off);
+    if (e == cudaSuccess) e = gd::dev_alloc(&b->pool[1], sizeof(double) * off);
     if (e == cudaSuccess) e = cudaMemset(b->pool[0], 0, sizeof(double) * off);
     if (e == cudaSuccess) e = cudaMemset(b->pool[1], 0, sizeof(double) * off);
-    if (e == cudaSuccess) e = cudaMalloc(&b->sc, sizeof(Scalars) * ngrids);
-    if (e == cudaSuccess) e = cudaMalloc(&b->sc_tune, sizeof(Scalars) * ngrids);
+    if (e == cudaSuccess) e = gd::dev_alloc(&b->sc, sizeof(Scalars) * ngrids);
+    if (e == cudaSuccess) e = gd::dev_alloc(&b->sc_tune, sizeof(Scalars) * ngrids);
     if (e == cudaSuccess) {
         std::vector<Scalars> h(ngrids);
         const double reset = gd::kTReset;
@@ -177,11 +177,11 @@ gd_status gd_batch_create(const gd_config* cfgs, int ngrids, gd_batch** out) {
         const int per_sm = gd::euler_batch_blocks_per_sm(b->order, v);
         const int full = per_sm * sms;
         b->ctas[v] = b->nitems[v] < full ? b->nitems[v] : full;
-        e = cudaMalloc(&b->d_grids[v], sizeof(BatchGrid) * ngrids);
+        e = gd::dev_alloc(&b->d_grids[v], sizeof(BatchGrid) * ngrids);
         if (e == cudaSuccess)
             e = cudaMemcpy(b->d_grids[v], hg.data(), sizeof(BatchGrid) * ngrids,
                            cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMalloc(&b->d_items[v], sizeof(int2) * items.size());
+        if (e == cudaSuccess) e = gd::dev_alloc(&b->d_items[v], sizeof(int2) * items.size());
         if (e == cudaSuccess)
             e = cudaMemcpy(b->d_items[v], items.data(), sizeof(int2) * items.size(),
                            cudaMemcpyHostToDevice);
@@ -198,14 +198,14 @@ gd_status gd_batch_destroy(gd_batch* b) {
     if (!b) return GD_ERR_INVALID_ARG;
     for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
     for (int v = 0; v < gd::kEulerVariants; ++v) {
-        cudaFree(b->d_grids[v]);
-        cudaFree(b->d_items[v]);
+        gd::dev_free(b->d_grids[v]);
+        gd::dev_free(b->d_items[v]);
     }
-    cudaFree(b->pool[0]);
-    cudaFree(b->pool[1]);
-    cudaFree(b->sc);
-    cudaFree(b->sc_tune);
-    cudaFree(b->aos);
+    gd::dev_free(b->pool[0]);
+    gd::dev_free(b->pool[1]);
+    gd::dev_free(b->sc);
+    gd::dev_free(b->sc_tune);
+    gd::dev_free(b->aos);
     delete b;
     return GD_OK;
 }
@@ -218,7 +218,7 @@ gd_status gd_batch_import(gd_batch* b, int grid, const double* s, const double* 
     const long long K = b->K[grid];
     const double *ds = s, *du = u;
     if (is_host) {
-        if (!b->aos) GD_TRY(cudaMalloc(&b->aos, sizeof(double) * 7 * (size_t)b->max_K));
+        if (!b->aos) GD_TRY(gd::dev_alloc(&b->aos, sizeof(double) * 7 * (size_t)b->max_K));
         GD_TRY(cudaMemcpyAsync(b->aos, s, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, st));
         GD_TRY(cudaMemcpyAsync(b->aos + 2 * K, u, sizeof(double) * 2 * K, cudaMemcpyHostToDevice,
                                st));
@@ -238,7 +238,7 @@ gd_status gd_batch_export(gd_batch* b, int grid, double* s, double* u, double* b
     const long long K = b->K[grid];
     double *ds = s, *du = u;
     if (is_host) {
-        if (!b->aos) GD_TRY(cudaMalloc(&b->aos, sizeof(double) * 7 * (size_t)b->max_K));
+        if (!b->aos) GD_TRY(gd::dev_alloc(&b->aos, sizeof(double) * 7 * (size_t)b->max_K));
         ds = b->aos;
         du = b->aos + 2 * K;
     }

@@ -65,8 +65,8 @@ cudaError_t pipe_create(gd_ctx* ctx) {
         HS_TRY(cudaEventCreateWithFlags(&p->ev_up[k], cudaEventDisableTiming));
         HS_TRY(cudaEventCreateWithFlags(&p->ev_out[k], cudaEventDisableTiming));
     }
-    HS_TRY(cudaMalloc(&p->aos_in, sizeof(double) * 7 * (size_t)ctx->K));
-    HS_TRY(cudaMalloc(&p->aos_out, sizeof(double) * 7 * (size_t)ctx->K));
+    HS_TRY(gd::dev_alloc(&p->aos_in, sizeof(double) * 7 * (size_t)ctx->K));
+    HS_TRY(gd::dev_alloc(&p->aos_out, sizeof(double) * 7 * (size_t)ctx->K));
     return cudaSuccess;
 }
 
@@ -322,8 +322,8 @@ void pipe_free(gd_ctx* ctx) {
     if (!p) return;
     for (StepGraph& g : p->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
-    cudaFree(p->aos_in);
-    cudaFree(p->aos_out);
+    gd::dev_free(p->aos_in);
+    gd::dev_free(p->aos_out);
     for (cudaEvent_t e : {p->start, p->down_done, p->comp_done, p->edge_done, p->up_done})
         if (e) cudaEventDestroy(e);
     for (int k = 0; k < kMaxBands; ++k) {

@@ -26,8 +26,8 @@ namespace gd {
 void io_free(gd_ctx* ctx) {
     IoScratch* io = ctx->io;
     if (!io) return;
-    cudaFree(io->dev);
-    cudaFreeHost(io->host);
+    gd::dev_free(io->dev);
+    gd::host_free(io->host);
     delete io;
     ctx->io = nullptr;
 }
@@ -481,10 +481,10 @@ gd_status ensure_dev(gd_ctx* ctx, size_t bytes) {
     }
     gd::IoScratch* io = ctx->io;
     if (io->dev_cap >= bytes) return GD_OK;
-    cudaFree(io->dev);
+    gd::dev_free(io->dev);
     io->dev = nullptr;
     io->dev_cap = 0;
-    IO_TRY(cudaMalloc(&io->dev, bytes));
+    IO_TRY(gd::dev_alloc(&io->dev, bytes));
     io->dev_cap = bytes;
     return GD_OK;
 }
@@ -492,10 +492,10 @@ gd_status ensure_dev(gd_ctx* ctx, size_t bytes) {
 gd_status ensure_host(gd_ctx* ctx, size_t bytes) {
     gd::IoScratch* io = ctx->io;
     if (io->host_cap >= bytes) return GD_OK;
-    cudaFreeHost(io->host);
+    gd::host_free(io->host);
     io->host = nullptr;
     io->host_cap = 0;
-    IO_TRY(cudaMallocHost(&io->host, bytes));
+    IO_TRY(gd::host_alloc(&io->host, bytes));
     io->host_cap = bytes;
     return GD_OK;
 }
@@ -631,14 +631,18 @@ gd_status parse_device_text(gd_ctx* ctx, char* dtext, long long L, char* work, c
     if ((long long)(last_first + last_count) < need) return GD_ERR_INVALID_ARG;  // too short
     token_place_kernel<<<(unsigned)ntiles, NT, 0, st>>>(dtext, tile_first, need, tokpos);
     IO_TRY(cudaGetLastError());
+    // parsed into the other plane set, which every cell's nf fields overwrite; the context
+    // switches to it only when every token parsed, so a failed parse leaves the state as it was
     token_parse_kernel<<<blocks(need), NT, 0, st>>>(dtext, tokpos, need, ctx->nf,
-                                                    ctx->planes(ctx->cur), bad);
+                                                    ctx->planes(1 - ctx->cur), bad);
     IO_TRY(cudaGetLastError());
     ctx->launches += 2;
     long long first_bad = none;
     IO_TRY(cudaMemcpyAsync(&first_bad, bad, sizeof(first_bad), cudaMemcpyDeviceToHost, st));
     IO_TRY(cudaStreamSynchronize(st));
-    return first_bad == none ? GD_OK : GD_ERR_INVALID_ARG;
+    if (first_bad != none) return GD_ERR_INVALID_ARG;
+    ctx->cur = 1 - ctx->cur;
+    return GD_OK;
 }
 
 size_t parse_work_bytes(long long L, long long K) {

@@ -133,6 +133,21 @@ cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
 cudaError_t probe_fp64_peak(double* flops);
 
+// Every device and pinned-host allocation and release the library makes goes through these
+// (gd_api.cu), which count them for gd_alloc_counts.
+cudaError_t dev_alloc_bytes(void** p, size_t bytes);
+cudaError_t host_alloc_bytes(void** p, size_t bytes);
+cudaError_t dev_free(void* p);
+cudaError_t host_free(void* p);
+template <class T>
+cudaError_t dev_alloc(T** p, size_t bytes) {
+    return dev_alloc_bytes(reinterpret_cast<void**>(p), bytes);
+}
+template <class T>
+cudaError_t host_alloc(T** p, size_t bytes) {
+    return host_alloc_bytes(reinterpret_cast<void**>(p), bytes);
+}
+
 // Records e as the process's last CUDA error (gd_last_cuda_error) and returns GD_ERR_CUDA;
 // every entry point reports a failed CUDA call through it.
 gd_status cuda_error(cudaError_t e);

@@ -197,7 +197,7 @@ cudaError_t probe_fp64_peak(double* flops) {
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     double* sink = nullptr;
-    e = cudaMalloc(&sink, 1024 * sizeof(double));
+    e = gd::dev_alloc(&sink, 1024 * sizeof(double));
     if (e != cudaSuccess) return e;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
@@ -213,7 +213,7 @@ cudaError_t probe_fp64_peak(double* flops) {
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    cudaFree(sink);
+    gd::dev_free(sink);
     if (e != cudaSuccess) return e;
     const double fmas = (double)reps * blocks * threads * 8.0 * ITER;
     *flops = 2.0 * fmas / (ms * 1e-3);

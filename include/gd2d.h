@@ -230,8 +230,10 @@ gd_status gd_field_ptr(gd_ctx* ctx, int f, const double** out);
  * differentiated); minmod, wave-speed min/max, HLLC / HLLD region and guard choices and
  * floors are differentiated along the branch the forward values take.  Supported: MHD with
  * HLLD or Euler with HLLC, order 2, Cartesian, periodic on all sides, fast mode, no frozen
- * cells (the Orszag-Tang and Kelvin-Helmholtz configurations); other configurations return
- * GD_ERR_UNSUPPORTED.  All vectors are device pointers in
+ * cells (the Orszag-Tang and Kelvin-Helmholtz configurations), with the dt policy
+ * GD_DT_LAGGED (the recorded dt of a step is the one rotated by the step before it);
+ * other configurations, and a context set to GD_DT_CURRENT, return GD_ERR_UNSUPPORTED from
+ * gd_adj_forward.  All vectors are device pointers in
  * the reference AoS layout (d/ds: K x 2, d/du: K x 2, d/dB: K x 3, Gaussian B; for Euler
  * the d/dB pointers may be null).
  *
@@ -303,7 +305,11 @@ long long gd_batch_launch_count(const gd_batch* b);
  * device current; make that first call before any stream capture.  Every call shares the
  * one array and it keeps the last call's contents (the counters are cleared at the start
  * of each call): calls that overlap on the GPU (other streams, other host threads) race, so
- * serialise them.  Calls no cudaMalloc, cudaFree or other allocating routine. */
+ * serialise them.  Calls no cudaMalloc, cudaFree or other allocating routine
+ * (gd_alloc_counts shows it).  It reports no non-physical state: the floor and non-finite
+ * counts of the step stay in the device array and are not read back (that would
+ * synchronise the stream), so GD_OK says nothing about the values; a caller that needs to
+ * know checks the output itself or steps through a context (gd_step_ref + gd_get_stats). */
 #define GD_STATIC_MAX_CELLS 65536
 #define GD_STATIC_SCRATCH_BYTES (256 + 2 * 7 * 8 * GD_STATIC_MAX_CELLS)
 gd_status gd_step_ref_static(const gd_config* cfg, const double* s, const double* u,
@@ -362,6 +368,13 @@ long long gd_launch_count(const gd_ctx* ctx);
 /* Measures the device's FP64 FMA throughput (FLOP/s, FMA = 2) with a register-resident
  * DFMA loop on every SM; blocking, ~50 ms. */
 gd_status gd_probe_fp64_peak(double* flops_out);
+
+/* Diagnostic (no reference counterpart): how many device or pinned-host allocations
+ * (cudaMalloc, cudaMallocHost) and releases (cudaFree, cudaFreeHost) this library has made
+ * in this process, over all contexts and threads.  Every allocation of the library goes
+ * through the two counted helpers; a caller that must not let the library allocate can
+ * check that a call left both counts unchanged. */
+gd_status gd_alloc_counts(long long* allocs, long long* frees);
 
 /* Test entry point (no reference counterpart): the fast step's own face solver on n
  * independent faces, for per-face checks against the reference's HLLC_Aleksashov /

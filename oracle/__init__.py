@@ -27,7 +27,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libgd_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libgdref.so")
-REF_SRC_DEFAULT = "/root/reference"
+# The reference checkout is located by this environment variable; without it the reference
+# library is not built, and the tests that need it skip.
+REF_SRC_ENV = "GD_REFERENCE_SRC"
+
+
+def ref_src() -> str | None:
+    """The reference sources' directory, if GD_REFERENCE_SRC names one that exists."""
+    p = os.environ.get(REF_SRC_ENV)
+    return p if p and os.path.isdir(p) else None
 
 EULER, MHD = 0, 1
 CARTESIAN, AXISYM = 0, 1
@@ -57,13 +65,20 @@ class OracleConfig(ctypes.Structure):
     ]
 
 
-def build(ref: bool | None = None, ref_src: str = REF_SRC_DEFAULT) -> None:
-    """Compile the oracle; also the reference library when its sources are present."""
+def build(ref: bool | None = None, src: str | None = None) -> None:
+    """Compile the oracle; also the reference library when its sources are given.
+
+    `src` is the reference checkout (default: GD_REFERENCE_SRC).  ref=None builds the
+    reference library when that directory exists, ref=True requires it."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if src is None:
+        src = ref_src()
     if ref is None:
-        ref = os.path.isdir(ref_src)
+        ref = src is not None and os.path.isdir(src)
     if ref:
-        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={ref_src}"],
+        if src is None or not os.path.isdir(src):
+            raise FileNotFoundError(f"reference sources not found: set {REF_SRC_ENV}")
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={src}"],
                        check=True)
 
 

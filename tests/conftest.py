@@ -27,10 +27,10 @@ def oracle_lib():
 def reference():
     import oracle
     if not oracle.Reference.available():
-        if os.path.isdir(oracle.REF_SRC_DEFAULT):
+        if oracle.ref_src() is not None:
             oracle.build(ref=True)
         else:
-            pytest.skip("reference sources not present: libgdref.so cannot be built here")
+            pytest.skip("reference library not built and GD_REFERENCE_SRC not set")
     return oracle.Reference()
 
 

@@ -1,11 +1,12 @@
 """Writes the golden vectors in this directory from the reference's OWN code.
 
 The reference (Gas_Dinamic.cu, kernel.cu) is compiled for the host by oracle/ref_build
-(``make -C oracle ref``) into oracle/_ref/libgdref.so; this script calls its functions and
-stores inputs and outputs as .npz fixtures.  The reference sources are needed only to
-regenerate the fixtures; the tests read the committed .npz files.
+(``make -C oracle ref REF=<checkout>``) into oracle/_ref/libgdref.so; this script calls
+its functions and stores inputs and outputs as .npz fixtures.  The reference sources are
+needed only to regenerate the fixtures (GD_REFERENCE_SRC names the checkout); the tests
+read the committed .npz files.
 
-    python tests/golden/make_golden.py
+    GD_REFERENCE_SRC=<reference checkout> python tests/golden/make_golden.py
 
 Fixtures:
   faces_hllc.npz   Euler HLLC_Aleksashov (kernel.cu:853) on random and branch-targeted states

@@ -115,3 +115,22 @@ def test_null_arguments_rejected(gdlib):
     assert gdlib.gd_advance_to(None, 1.0, 10, 0, None, None) == 1
     assert gdlib.gd_step_ref(None, None, None, None, None, None, None, None, None, 0, 0, None) == 1
     assert gdlib.gd_probe_fp64_peak(None) == 1
+
+
+def test_every_allocation_goes_through_the_counted_helpers():
+    """gd_alloc_counts counts what the library's helpers allocate; that is every allocation
+    only if no source calls the CUDA allocators directly.  The helpers themselves live in
+    gd_api.cu."""
+    csrc = os.path.join(ROOT, "golikov_2d_gb300", "csrc")
+    pat = re.compile(r"(?<![\w:])(cudaMalloc\w*|cudaHostAlloc|cudaFree\w*|cudaMallocAsync)\s*\(")
+    found = []
+    for name in sorted(os.listdir(csrc)):
+        if not name.endswith((".cu", ".cuh", ".h", ".cpp")):
+            continue
+        text = open(os.path.join(csrc, name)).read()
+        text = re.sub(r"//[^\n]*|/\*.*?\*/", "", text, flags=re.S)  # comments
+        for m in pat.finditer(text):
+            found.append((name, m.group(1)))
+    allowed = [("gd_api.cu", "cudaMalloc"), ("gd_api.cu", "cudaMallocHost"),
+               ("gd_api.cu", "cudaFree"), ("gd_api.cu", "cudaFreeHost")]
+    assert sorted(found) == sorted(allowed), found

@@ -209,3 +209,25 @@ def test_unsupported_configurations(cuda):
         sol.adj_forward(3, 1)
     assert e.value.status == 5
     sol.close()
+
+
+@pytest.mark.parametrize("physics", ["mhd", "euler"])
+def test_current_dt_policy_is_rejected(cuda, physics):
+    """Under GD_DT_CURRENT each step's dt comes from a pass over its own input, which the
+    recording and the recomputed segments do not run: gd_adj_forward refuses it, and
+    accepts the same context again once the policy is back to the lagged one."""
+    if physics == "mhd":
+        cfg, s, u, b = problems.orszag_tang(32, 32)
+    else:
+        cfg, s, u, b = problems.kelvin_helmholtz(32, 32)
+    sol = g.Solver(cfg)
+    sol.import_state(s, u, b)
+    sol.set_time(0.0, 0.0)
+    sol.init_dt()
+    sol.set_dt_policy(g.DT_CURRENT)
+    with pytest.raises(g.GdError) as e:
+        sol.adj_forward(3, 1)
+    assert e.value.status == 5
+    sol.set_dt_policy(g.DT_LAGGED)
+    sol.adj_forward(3, 1)
+    sol.close()

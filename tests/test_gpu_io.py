@@ -110,19 +110,28 @@ def test_parse_is_correctly_rounded(cuda, tmp_path):
 
 
 def test_parse_errors(cuda):
-    cfg = problems.orszag_tang(8, 8)[0]
-    sol = g.Solver(cfg)
+    cfg, s, u, b = problems.orszag_tang(8, 8)
+    sol = solver_with(cfg, s, u, b)
     good = sol.format_text()
     with pytest.raises(g.GdError) as e:
         sol.parse_text(good[: len(good) // 2])       # too few numbers
     assert e.value.status == 1
-    bad = good.replace(b" ", b" 1.2.3 ", 1)           # a malformed number
-    with pytest.raises(g.GdError):
-        sol.parse_text(bad)
-    with pytest.raises(g.GdError):
-        sol.parse_text(good.replace(b" ", b" 1e999 ", 1))  # overflow
+    # a malformed number and an overflowing one near the end of the text, after most
+    # tokens parsed: a failed parse leaves the state as it was
+    tail = good.rindex(b" ", 0, len(good) - 2)
+    for junk in (b" 1.2.3 ", b" 1e999 "):
+        with pytest.raises(g.GdError):
+            sol.parse_text(good[:tail] + junk + good[tail + 1:])
+        assert sol.format_text() == good
     with pytest.raises(g.GdError):
         sol.parse_text(b"")
+    # the state after a good parse is the parsed one
+    s2, u2, b2 = s * 1.5, u * 0.5, b * 2.0
+    other = solver_with(cfg, s2, u2, b2)
+    text2 = other.format_text()
+    other.close()
+    sol.parse_text(text2)
+    assert sol.format_text() == text2
     sol.close()
 
 

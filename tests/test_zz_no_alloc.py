@@ -45,8 +45,15 @@ def static_step(cfg, s, u, b, T_do, method=g.METHOD_CONFIG):
 CASES = {
     "sod256_fast": lambda: problems.sod(256, 256),  # exactly GD_STATIC_MAX_CELLS cells
     "kh128x64_fast": lambda: problems.kelvin_helmholtz(128, 64),
+    "kh64_parity": lambda: problems.kelvin_helmholtz(64, 64, mode=g.MODE_PARITY),
+    "ot96_hlld_fast": lambda: problems.orszag_tang(96, 96),
     "ot96_hlld_parity": lambda: problems.orszag_tang(96, 96, mode=g.MODE_PARITY),
     "wind_hlld_fast": lambda: problems.stellar_wind(96, 54, 2.25, 1.25),
+    # the MUSCL-Hancock step (its edge-band and tile launches in fast mode, the per-cell
+    # kernel in parity mode), on a grid whose frozen sphere and edges both lie inside
+    "hancock_wind_fast": lambda: problems.hancock_wind(96, 54, 4.5, 2.5),
+    "hancock_wind_parity": lambda: problems.hancock_wind(96, 54, 4.5, 2.5,
+                                                         mode=g.MODE_PARITY),
 }
 
 
@@ -77,3 +84,42 @@ def test_static_step_rejects_grids_beyond_its_scratch(cuda):
     torch.cuda.synchronize()
     assert st == 1
     assert bool((s2 == 7.0).all()) and float(T.cpu()[0]) == 1e7
+
+
+def test_static_steps_allocate_nothing(cuda):
+    """The property the entry point exists for: once a device is set up, calls make no
+    device allocation and no release.  Checked two ways around repeated calls in both
+    modes, both physics and both Hancock forms: the library's own allocation counter
+    (gd_alloc_counts: every allocation of the library goes through it) and the device's
+    free memory (cudaMemGetInfo), which sees any allocation, the CUDA runtime's included."""
+    import torch
+    L = g.load()
+    calls = []
+    for name in sorted(CASES):
+        cfg, s, u, b = CASES[name]()
+        ds, du, db = to_dev(s), to_dev(u), to_dev(b)
+        out = (torch.zeros_like(ds), torch.zeros_like(du),
+               None if db is None else torch.zeros_like(db))
+        T = torch.tensor([1e7], dtype=torch.float64, device="cuda")
+        Tdo = torch.tensor([1e-5], dtype=torch.float64, device="cuda")
+        calls.append((cfg.cstruct(), (ds, du, db), out, T, Tdo))
+    p = lambda t: None if t is None else t.data_ptr()
+
+    def run_all():
+        for c, (ds, du, db), (s2, u2, b2), T, Tdo in calls:
+            st = L.gd_step_ref_static(ctypes.byref(c), p(ds), p(du), p(db), p(s2), p(u2),
+                                      p(b2), p(T), p(Tdo), g.METHOD_CONFIG, None)
+            assert st == 0, g.STATUS.get(st, st)
+        torch.cuda.synchronize()
+
+    run_all()  # set-up of this device, first launch of every kernel used
+    counts0 = g.alloc_counts()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        run_all()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert g.alloc_counts() == counts0
+    assert free1 == free0
+    for _, _, (s2, u2, b2), T, _ in calls:
+        assert bool(torch.isfinite(s2).all()) and bool(torch.isfinite(u2).all())
+        assert 0.0 < float(T.cpu()[0]) < 1e7
