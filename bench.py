@@ -596,11 +596,77 @@ class AdjointHarness:
             out.update({"bound": bound, "pass": max(fd_rel) <= bound})
         return out
 
+    def fd_switches(self, U0, n, every, ndir, eps_list=(1e-6, 1e-7, 1e-8, 1e-9)):
+        """The central-difference check as the configuration states it: n steps from U0
+        with checkpoints every `every`, `ndir` seeded random unit directions, each at every
+        eps of `eps_list`.  Each pair of runs (U0 + eps v, U0 - eps v) goes through
+        gd_adj_switches, which counts the steps and cells where the two runs take different
+        branches of a non-smooth choice; the quotient is the derivative of the branch the
+        adjoint differentiates only where that count is 0."""
+        torch = self.torch
+        grad, G, rho_t = self.gradient(U0, n, every)
+        rng = np.random.default_rng(11)
+        rows = []
+        for i in range(ndir):
+            d = [self.dev(rng.standard_normal(tuple(x.shape))) for x in U0]
+            nrm = math.sqrt(sum(float((x * x).sum()) for x in d))
+            d = [x / nrm for x in d]
+            ad = sum(float((x * y).sum()) for x, y in zip(grad, d))
+            tn = float((G[0][:, 0] * self.jvp(d)[0][:, 0]).sum())
+            per_eps = []
+            for eps in eps_list:
+                Up = [x + eps * y for x, y in zip(U0, d)]
+                Um = [x - eps * y for x, y in zip(U0, d)]
+                Op, Om = self.zeros(U0), self.zeros(U0)
+                c = self.sol.adj_switches(Up, Um, Op, Om)
+                rp, rm = Op[0][:, 0], Om[0][:, 0]
+                # with the recorded dt sequence held fixed, a run whose own wave speeds
+                # exceed the recorded ones can break its CFL limit and turn non-finite
+                finite = all(bool(torch.isfinite(x).all()) for x in Op + Om)
+                fd = float(((rp - rm) * (0.5 * (rp + rm) - rho_t)).sum()) / (2 * eps)
+                per_eps.append({"eps": eps,
+                                "rel_err": abs(fd - ad) / abs(ad) if finite else None,
+                                "replays_finite": finite,
+                                "switched_cells": c["cells"], "switches": c})
+            rows.append({"direction": i, "adjoint": ad,
+                         "tangent_rel": abs(ad - tn) / abs(ad), "by_eps": per_eps})
+        clean = [(r["direction"], e["eps"], e["rel_err"]) for r in rows for e in r["by_eps"]
+                 if e["switched_cells"] == 0 and e["replays_finite"]]
+        clean_dirs = sorted({c[0] for c in clean})
+        errs = lambda r: [e["rel_err"] for e in r["by_eps"] if e["rel_err"] is not None]
+        best = [min(errs(r)) for r in rows if errs(r)]
+        summary = {
+            "grid": f"{self.cfg.N}x{self.cfg.M}", "steps": n, "ckpt_every": every,
+            "directions": ndir, "eps": list(eps_list),
+            "directions_crossing_a_switch_at_every_eps": ndir - len(clean_dirs),
+            "directions_with_a_switch_free_eps": len(clean_dirs),
+            "max_rel_err_switch_free": max((c[2] for c in clean), default=None),
+            "switch_free_meets_1e-6": all(c[2] <= 1e-6 for c in clean) if clean else None,
+            "switch_free_pairs_by_eps": {f"{e:g}": sum(1 for c in clean if c[1] == e)
+                                         for e in eps_list},
+            "min_switched_cells_by_eps": {
+                f"{e:g}": min(r["by_eps"][j]["switched_cells"] for r in rows)
+                for j, e in enumerate(eps_list)},
+            "nonfinite_replays_by_eps": {
+                f"{e:g}": sum(1 for r in rows if not r["by_eps"][j]["replays_finite"])
+                for j, e in enumerate(eps_list)},
+            "median_rel_err_by_eps": {
+                f"{e:g}": (float(np.median(v)) if v else None) for e, v in
+                ((e, [r["by_eps"][j]["rel_err"] for r in rows
+                      if r["by_eps"][j]["rel_err"] is not None])
+                 for j, e in enumerate(eps_list))},
+            "best_eps_rel_err_max": max(best) if best else None,
+            "best_eps_rel_err_median": float(np.median(best)) if best else None,
+            "tangent_max_rel": max(r["tangent_rel"] for r in rows),
+        }
+        torch.cuda.synchronize()
+        return {"summary": summary, "per_direction": rows}
+
     def close(self):
         self.sol.close()
 
 
-def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=20,
+def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8,
                     fd_N=32, fd_pre=40, fd_steps=30):
     """Orszag-Tang MHD N x N, HLLD + minmod, `nsteps` steps with checkpoints every `every`;
     loss = 1/2 |rho_n - rho_target|^2, the target being the final density of its own run
@@ -615,12 +681,12 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
       directions.  The map is piecewise smooth: minmod switches (|l| against |r|, signs),
       the Orszag-Tang initial state itself (rho and p uniform: minmod(0, 0)) and, from step
       59 on the 512 grid, the clamp p <= 0 -> 1e-6.  A difference quotient whose +-eps
-      straddles a switch is not the derivative; in a smooth field the |l| / |r| comparison
-      sits within ~1e-5 of switching in many cells, so on the 512 grid a unit direction
-      crosses switches at every eps that rounding allows.  The bounded check (1e-6) runs on
-      the same problem at `fd_N` (state after `fd_pre` steps, `fd_steps` steps), where the
-      quotient resolves; windows of the 512 grid from the state after `pre` steps are
-      reported beside it."""
+      straddles a switch is not the derivative.  The check as configured (N x N from the
+      initial state, `nsteps` steps, `ndir` directions) runs every direction at four eps
+      through gd_adj_switches, which counts the cells and steps where the +eps and -eps runs
+      take different branches (minmod picks, fallbacks, HLLD speeds, region, guards,
+      floors); the bound applies where that count is 0.  A bounded check (1e-6) also runs
+      on the same problem at `fd_N` (state after `fd_pre` steps, `fd_steps` steps)."""
     stream = torch.cuda.current_stream()
 
     def timed(fn):
@@ -671,11 +737,11 @@ def measure_adjoint(g, torch, N=512, nsteps=100, every=10, ndir=32, ntan=8, pre=
                                               f"Orszag-Tang state after {fd_pre} steps",
                                               bound=1e-6)
     Hs.close()
-    H.start(U_ic, pre)
+    # the configuration's own check: from the initial state, nsteps, checkpoints every
+    # `every`, ndir directions, with the branch switches of every difference quotient
+    H.start(U_ic)
     U0 = H.state()
-    res["central_differences_512"] = [
-        H.fd_window(U0, n, every, ndir // 4, f"Orszag-Tang state after {pre} steps")
-        for n in (fd_steps, nsteps)]
+    res["central_differences_config"] = H.fd_switches(U0, nsteps, every, ndir)
     H.close()
     return res
 

@@ -50,7 +50,7 @@ EXPORTS = (
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
-    "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
+    "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay", "gd_adj_switches",
     "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text", "gd_write_binary",
     "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot",
 )
@@ -147,6 +147,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    L.gd_adj_switches.argtypes = [vp] + [vp] * 12 + [ctypes.POINTER(ll), vp]
     sz = ctypes.c_size_t
     tecp = ctypes.POINTER(gd_tecplot_opts)
     L.gd_format_text.argtypes = [vp, vp, sz, ctypes.POINTER(sz), vp]
@@ -178,7 +179,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
                  "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
-                 "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text",
+                 "gd_adj_switches", "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text",
                  "gd_write_binary", "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot"):
         getattr(L, name).restype = i
     _lib = L
@@ -360,6 +361,19 @@ class Solver:
 
     def adj_replay(self, s, u, b, os_, ou, ob, stream=None) -> None:
         self._vec_call(self.lib.gd_adj_replay, "gd_adj_replay", (s, u, b), (os_, ou, ob), stream)
+
+    SWITCH_KINDS = ("minmod", "fallback", "speeds", "region", "guards", "floors",
+                    "cell_steps", "cells")
+
+    def adj_switches(self, Up, Um, Op, Om, stream=None) -> dict:
+        """Replays the recorded map from Up and Um side by side into Op and Om (each a tuple
+        (s, u, b) of device tensors) and returns the branch-switch counts between the two
+        runs (gd_adj_switches), keyed by SWITCH_KINDS."""
+        counts = (ctypes.c_longlong * 8)()
+        p = [t.data_ptr() for t in (*Up, *Um, *Op, *Om)]
+        _check(self.lib.gd_adj_switches(self.handle, *p, counts, _stream_handle(stream)),
+               "gd_adj_switches")
+        return dict(zip(self.SWITCH_KINDS, (int(c) for c in counts)))
 
     def field_ptr(self, f: int) -> int:
         p = ctypes.c_void_p()

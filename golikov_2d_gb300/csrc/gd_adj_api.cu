@@ -319,4 +319,56 @@ gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const dou
     return GD_OK;
 }
 
+gd_status gd_adj_switches(gd_ctx* ctx, const double* sp, const double* up, const double* bp,
+                          const double* sm, const double* um, const double* bm, double* osp,
+                          double* oup, double* obp, double* osm, double* oum, double* obm,
+                          long long* counts, gd_stream stream) {
+    if (!ctx || !ctx->adj || !counts) return GD_ERR_INVALID_ARG;
+    if (ctx->nf != 7) return GD_ERR_UNSUPPORTED;  // the switch codes are those of HLLD
+    for (const void* p : {(const void*)sp, (const void*)up, (const void*)bp, (const void*)sm,
+                          (const void*)um, (const void*)bm, (const void*)osp, (const void*)oup,
+                          (const void*)obp, (const void*)osm, (const void*)oum, (const void*)obm})
+        if (!p) return GD_ERR_INVALID_ARG;
+    gd::AdjStore* a = ctx->adj;
+    const long long K = ctx->K;
+    const int nf = ctx->nf;
+    const int nk = gd::switch_kinds();
+    cudaStream_t st = (cudaStream_t)stream;
+    // work space: both runs' two states in the two segment buffers (each holds at least two
+    // states), their update terms in the two aux buffers, marks and counters in scratch
+    double* wp[2] = {a->seg, a->seg + (size_t)nf * K};
+    double* wm[2] = {a->seg2, a->seg2 + (size_t)nf * K};
+    a->seg_holds = -1;
+    a->seg2_holds = -1;
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(a->scratch);
+    unsigned char* step_mark = reinterpret_cast<unsigned char*>(a->scratch + 8);
+    unsigned char* ever_mark = step_mark + K;
+    GD_TRY(cudaMemsetAsync(a->scratch, 0, 64 + 2 * (size_t)K, st));
+    GD_TRY(gd::launch_aos_to_soa(sp, up, bp, planes_at(wp[0], nf, K), K, nf, st));
+    GD_TRY(gd::launch_aos_to_soa(sm, um, bm, planes_at(wm[0], nf, K), K, nf, st));
+    ctx->launches += 2;
+    int c = 0;
+    for (int k = 0; k < a->nsteps; ++k) {
+        const CPlanes ip = cplanes_at(wp[c], nf, K), im = cplanes_at(wm[c], nf, K);
+        GD_TRY(gd::launch_switch_faces(ctx->P, ip, im, ctr, step_mark, st));
+        GD_TRY(step_aux(ctx, ctx->P, ip, planes_at(wp[c ^ 1], nf, K), a->dts + k,
+                        (unsigned long long*)a->tbits, nullptr, nullptr, a->aux, st));
+        GD_TRY(step_aux(ctx, ctx->P, im, planes_at(wm[c ^ 1], nf, K), a->dts + k,
+                        (unsigned long long*)a->tbits, nullptr, nullptr, a->aux2, st));
+        GD_TRY(gd::launch_switch_cells(ctx->P, ip, a->aux, im, a->aux2, ctr, step_mark,
+                                       ever_mark, st));
+        ctx->launches += 4;
+        c ^= 1;
+    }
+    GD_TRY(gd::launch_switch_total(K, ever_mark, ctr, st));
+    GD_TRY(gd::launch_soa_to_aos(cplanes_at(wp[c], nf, K), osp, oup, obp, K, nf, st));
+    GD_TRY(gd::launch_soa_to_aos(cplanes_at(wm[c], nf, K), osm, oum, obm, K, nf, st));
+    ctx->launches += 3;
+    unsigned long long h[16] = {};
+    GD_TRY(cudaMemcpyAsync(h, ctr, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost, st));
+    GD_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < nk; ++i) counts[i] = (long long)h[i];
+    return GD_OK;
+}
+
 }  // extern "C"

@@ -886,7 +886,221 @@ int grid_cells(long long K) {
     return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
 }
 
+// ---------------------------------------------------------------------------------------
+// Branch switches between two runs (gd_adj_switches).  A central difference of runs from
+// U0 + eps v and U0 - eps v is the derivative of the branch both take only where every
+// non-smooth choice comes out the same in both.  Per face, the choices its flux depends on,
+// computed with the forward's own operations (as adj_face_kernel repeats them): the minmod
+// pick of its low cell's slope (every cell's slope is counted at exactly one face per
+// direction), the rho / p fallbacks of its two face states, and the HLLD choices: which
+// side gives min(u), max(u), max(cf) and max(|S|) (speeds), the upwind side and the region
+// of the fan (region), and the guards disc <= 0, |tt| >= 1e-5 on both sides, |bn| > 1e-6
+// and sign(bn) (guards).  Per cell, the update's floors rho <= 0 and p <= 0.  Counters
+// (kSw*): (step, face) pairs per face category, (step, cell) pairs for floors and for
+// cells touched by any switch, and, at the end, the cells switched at any step.
+// ---------------------------------------------------------------------------------------
+struct FaceCode {
+    unsigned int minmod, fallback, speeds, region, guards;
+};
+
+__device__ __forceinline__ FaceCode face_code(const Params& P, const CPlanes& U, bool isx,
+                                              const long long* kc) {
+    FaceCode code{0u, 0u, 0u, 0u, 0u};
+    double c[4][NF];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) c[t][f] = ld_b(U, f, kc[t]);
+    double qa[NF], qb[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        int sa, sb_;
+        const double da = slope_sel(c[0][f], c[1][f], c[2][f], sa);
+        const double db = slope_sel(c[1][f], c[2][f], c[3][f], sb_);
+        const double va = fma(0.5, da, c[1][f]), vb = fma(-0.5, db, c[2][f]);
+        const bool fu = f < 2 && le_zero(va), fd = f < 2 && le_zero(vb);
+        qa[f] = fu ? c[1][f] : va;
+        qb[f] = fd ? c[2][f] : vb;
+        code.minmod |= (unsigned int)(sa + 1) << (2 * f);
+        if (f < 2) code.fallback |= (fu ? 1u : 0u) << (2 * f) | (fd ? 2u : 0u) << (2 * f);
+    }
+    const double la[7] = {qa[0], qa[1], isx ? qa[2] : qa[3], isx ? qa[3] : qa[2],
+                          isx ? qa[4] : qa[5], isx ? qa[5] : qa[4], qa[6]};
+    const double lb[7] = {qb[0], qb[1], isx ? qb[2] : qb[3], isx ? qb[3] : qb[2],
+                          isx ? qb[4] : qb[5], isx ? qb[5] : qb[4], qb[6]};
+    SideV A, B;
+    side_fwd(A, la, P);
+    side_fwd(B, lb, P);
+    // the forward part of hlld_vjp up to the region, operation for operation
+    const bool minA = !dlt(B.un, A.un);
+    const bool maxB = dlt(A.un, B.un);
+    const double uminN = minA ? A.un : B.un;
+    const double umaxN = maxB ? B.un : A.un;
+    const bool cfB = abs_bits(A.cf) < abs_bits(B.cf);
+    const double cmax = cfB ? B.cf : A.cf;
+    const double SL = uminN - cmax, SR = umaxN + cmax;
+    const double suL = SL - A.un, suR = SR - B.un;
+    const double mL = A.r * suL, mR = B.r * suR;
+    const double iden = rcp_fast(mR - mL);
+    const double SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
+    const bool UUR = abs_bits(SL) < abs_bits(SR);
+    const double iS = rcp_fast(SR - SL);
+    const double bn = fma(SR, B.bn, -SL * A.bn) * iS;
+    const double iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
+    const double rLL = mL * iL, rRR = mR * iR;
+    const double bbn = bn * bn;
+    const double ttL = fma(mL, SL - SM, -bbn);
+    const bool gL = abs_bits(ttL) >= 0x3EE4F8B588E368F1ULL;
+    const double ttR = fma(mR, SR - SM, -bbn);
+    const bool gR = abs_bits(ttR) >= 0x3EE4F8B588E368F1ULL;
+    double isLL, isRR, sLL, sRR;
+    rsqrt_and_sqrt(rLL, isLL, sLL);
+    rsqrt_and_sqrt(rRR, isRR, sRR);
+    const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
+    const double abn = dabs(bn);
+    const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
+    const double SRR = bnz ? fma(abn, isRR, SM) : SM;
+    const bool takeL = ge_zero(SL) || ge_zero(SM);
+    int level;
+    if (takeL) level = ge_zero(SL) ? 0 : (ge_zero(SLL) ? 1 : 2);
+    else level = gt_zero(SRR) ? 2 : (gt_zero(SR) ? 1 : 0);
+    code.speeds = (minA ? 1u : 0u) | (maxB ? 2u : 0u) | (cfB ? 4u : 0u) | (UUR ? 8u : 0u);
+    code.region = (takeL ? 1u : 0u) | ((unsigned int)level << 1);
+    code.guards = (A.disc0 ? 1u : 0u) | (B.disc0 ? 2u : 0u) | (gL ? 4u : 0u) | (gR ? 8u : 0u) |
+                  (bnz ? 16u : 0u) | (bnz && lt_zero(bn) ? 32u : 0u);
+    return code;
+}
+
+// warp-aggregated counter increment: one atomic per warp and kind
+__device__ __forceinline__ void count_if(unsigned long long* ctr, bool hit) {
+    const unsigned int m = __ballot_sync(0xffffffffu, hit);
+    if (m != 0u && (threadIdx.x & 31) == (unsigned)(__ffs((int)m) - 1))
+        atomicAdd(ctr, (unsigned long long)__popc(m));
+}
+
+__global__ void __launch_bounds__(FBX * FBY) switch_face_kernel(Params P, CPlanes Ua, CPlanes Ub,
+                                                                unsigned long long* ctr,
+                                                                unsigned char* step_mark) {
+    const int N = P.N, M = P.M;
+    const bool isx = blockIdx.z == 0;
+    const int ix = blockIdx.x * FBX + threadIdx.x;
+    const int iy = blockIdx.y * FBY + threadIdx.y;
+    const bool in = ix < N && iy < M;
+    FaceCode a{0u, 0u, 0u, 0u, 0u}, b{0u, 0u, 0u, 0u, 0u};
+    long long kc[4] = {0, 0, 0, 0};
+    if (in) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            kc[t] = isx ? (long long)iy * N + wrap(ix - 2 + t, N)
+                        : (long long)wrap(iy - 2 + t, M) * N + ix;
+        a = face_code(P, Ua, isx, kc);
+        b = face_code(P, Ub, isx, kc);
+    }
+    const bool sm = a.minmod != b.minmod, sf = a.fallback != b.fallback;
+    const bool ss = a.speeds != b.speeds, sr = a.region != b.region, sg = a.guards != b.guards;
+    // counted per warp: threadIdx is 32 x 4, so each warp is one threadIdx.y row
+    count_if(ctr + 0, sm);
+    count_if(ctr + 1, sf);
+    count_if(ctr + 2, ss);
+    count_if(ctr + 3, sr);
+    count_if(ctr + 4, sg);
+    if (sm || sf || ss || sr || sg) {
+        // the slope of the low cell, both face states and the flux between them
+        step_mark[kc[1]] = 1;
+        step_mark[kc[2]] = 1;
+    }
+}
+
+// Floors of the update of U (with the forward's flux differences and Powell term aux), as
+// adj_update_kernel recomputes them: bit 0 rho <= 0, bit 1 p <= 0.
+__device__ __forceinline__ unsigned int floor_code(const Params& P, const CPlanes& U,
+                                                   const double* aux, long long K, long long k) {
+    const double r = U.f[0][k], p = U.f[1][k], u = U.f[2][k], v = U.f[3][k];
+    const double bx = __dmul_rn(U.f[4][k], kInvSpi4), by = __dmul_rn(U.f[5][k], kInvSpi4);
+    const double bz = __dmul_rn(U.f[6][k], kInvSpi4);
+    double d[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) d[f] = aux[(size_t)f * K + k];
+    const double divb = aux[(size_t)7 * K + k];
+    const double ub = fma(u, bx, v * by);
+    const double bb = fma(bz, bz, fma(by, by, bx * bx));
+    const double E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(u, u, v * v), bb));
+    double r2 = r - d[0];
+    const bool rfl = le_zero(r2);
+    if (rfl) r2 = r;
+    const double mx2 = fma(r, u, -fma(bx, divb, d[2]));
+    const double my2 = fma(r, v, -fma(by, divb, d[3]));
+    const double bx2 = bx - fma(u, divb, d[4]);
+    const double by2 = by - fma(v, divb, d[5]);
+    const double bz2 = bz - d[6];
+    const double E2 = E - fma(ub, divb, d[1]);
+    const double inv = rcp_fast(r2);
+    const double u2 = mx2 * inv, v2 = my2 * inv;
+    const double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2),
+                                      fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+    return (rfl ? 1u : 0u) | (le_zero(p2) ? 2u : 0u);
+}
+
+__global__ void __launch_bounds__(NT) switch_cell_kernel(Params P, CPlanes Ua, const double* auxa,
+                                                         CPlanes Ub, const double* auxb,
+                                                         unsigned long long* ctr,
+                                                         unsigned char* step_mark,
+                                                         unsigned char* ever_mark) {
+    const long long K = (long long)P.N * P.M;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long K_up = (K + 31) / 32 * 32;  // whole warps through the loop (ballots)
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K_up; k += stride) {
+        bool fl = false, any = false;
+        if (k < K) {
+            fl = floor_code(P, Ua, auxa, K, k) != floor_code(P, Ub, auxb, K, k);
+            any = fl || step_mark[k] != 0;
+            if (any) {
+                ever_mark[k] = 1;
+                step_mark[k] = 0;
+            }
+        }
+        count_if(ctr + 5, fl);
+        count_if(ctr + 6, any);
+    }
+}
+
+__global__ void __launch_bounds__(NT) switch_total_kernel(long long K,
+                                                          const unsigned char* ever_mark,
+                                                          unsigned long long* ctr) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long K_up = (K + 31) / 32 * 32;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K_up; k += stride)
+        count_if(ctr + 7, k < K && ever_mark[k] != 0);
+}
+
 }  // namespace
+
+int switch_kinds() { return 8; }
+
+cudaError_t launch_switch_faces(const Params& P, const CPlanes& Ua, const CPlanes& Ub,
+                                unsigned long long* ctr, unsigned char* step_mark,
+                                cudaStream_t st) {
+    const unsigned gxb = (unsigned)((P.N + FBX - 1) / FBX), gyb = (unsigned)((P.M + FBY - 1) / FBY);
+    if (gyb > 65535u) return cudaErrorInvalidConfiguration;
+    switch_face_kernel<<<dim3(gxb, gyb, 2), dim3(FBX, FBY), 0, st>>>(P, Ua, Ub, ctr, step_mark);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_switch_cells(const Params& P, const CPlanes& Ua, const double* auxa,
+                                const CPlanes& Ub, const double* auxb, unsigned long long* ctr,
+                                unsigned char* step_mark, unsigned char* ever_mark,
+                                cudaStream_t st) {
+    const long long K = (long long)P.N * P.M;
+    switch_cell_kernel<<<grid_cells(K), NT, 0, st>>>(P, Ua, auxa, Ub, auxb, ctr, step_mark,
+                                                     ever_mark);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_switch_total(long long K, const unsigned char* ever_mark,
+                                unsigned long long* ctr, cudaStream_t st) {
+    switch_total_kernel<<<grid_cells(K), NT, 0, st>>>(K, ever_mark, ctr);
+    return cudaGetLastError();
+}
 
 int adjoint_scratch_planes() { return kScratchPlanes; }
 

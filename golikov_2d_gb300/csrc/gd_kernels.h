@@ -86,6 +86,21 @@ cudaError_t launch_adjoint_step_euler(const Params& P, const CPlanes& U, const d
                                       const CPlanes& lam_out, const Planes& lam_in,
                                       double* scratch, const double* T_do, cudaStream_t st);
 cudaError_t prepare_adjoint();
+// Branch switches between two runs of the MHD step (gd_adj_switches): per step, the face
+// choices of the two input states (counters 0-4: minmod, rho/p fallback, wave-speed picks,
+// HLLD region, guards; (step, face) pairs; faces mark their two cells in step_mark), then
+// the update floors of both steps (counter 5, (step, cell) pairs) and the marked cells
+// (counter 6; moved into ever_mark); at the end the cells marked at any step (counter 7).
+int switch_kinds();
+cudaError_t launch_switch_faces(const Params& P, const CPlanes& Ua, const CPlanes& Ub,
+                                unsigned long long* ctr, unsigned char* step_mark,
+                                cudaStream_t st);
+cudaError_t launch_switch_cells(const Params& P, const CPlanes& Ua, const double* auxa,
+                                const CPlanes& Ub, const double* auxb, unsigned long long* ctr,
+                                unsigned char* step_mark, unsigned char* ever_mark,
+                                cudaStream_t st);
+cudaError_t launch_switch_total(long long K, const unsigned char* ever_mark,
+                                unsigned long long* ctr, cudaStream_t st);
 cudaError_t launch_adjoint_step(const Params& P, const CPlanes& U, const double* aux,
                                 const CPlanes& lam_out, const Planes& lam_in, double* scratch,
                                 const double* T_do, cudaStream_t st);

@@ -250,6 +250,24 @@ gd_status gd_tangent(gd_ctx* ctx, const double* vs, const double* vu, const doub
                      double* os, double* ou, double* ob, gd_stream stream);
 gd_status gd_adj_replay(gd_ctx* ctx, const double* s, const double* u, const double* b,
                         double* os, double* ou, double* ob, gd_stream stream);
+/* Diagnostic of the central-difference check (MHD; Euler contexts: GD_ERR_UNSUPPORTED):
+ * replays the recorded map from two initial states (U0 + eps v and U0 - eps v) side by
+ * side, writes both final states (as gd_adj_replay would) and counts where the two runs
+ * take different branches of a non-smooth choice, step by step.  counts[0..7]:
+ *   0 minmod pick of a cell's slope           (step, face) pairs, each slope at one face
+ *   1 rho / p face-state fallback             (step, face) pairs
+ *   2 HLLD wave-speed picks (min u, max u, max cf, max |S|)   (step, face) pairs
+ *   3 HLLD upwind side and fan region                          (step, face) pairs
+ *   4 HLLD guards (disc <= 0, |tt| >= 1e-5 either side, |bn| > 1e-6, sign bn)  pairs
+ *   5 update floors rho <= 0, p <= 0          (step, cell) pairs
+ *   6 cells touched by any of these           (step, cell) pairs
+ *   7 cells touched at any step               cells
+ * A difference quotient is the derivative of the branch the adjoint differentiates only
+ * where all counts are 0.  Blocking (returns with the counts on the host). */
+gd_status gd_adj_switches(gd_ctx* ctx, const double* sp, const double* up, const double* bp,
+                          const double* sm, const double* um, const double* bm, double* osp,
+                          double* oup, double* obp, double* osm, double* oum, double* obm,
+                          long long* counts, gd_stream stream);
 
 /* ---- batched: many independent grids --------------------------------------------------
  * No counterpart in the reference (it advances one grid, kernel.cu:4102).  A batch holds
