@@ -43,32 +43,37 @@ __global__ void __launch_bounds__(NT) eadj_update_kernel(Params P, CPlanes U, co
         double r2 = r - d[0];
         const bool rfl = le_zero(r2);
         if (rfl) r2 = 0.0001;
-        const double E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
         const double inv = rcp_fast(r2);
         const double mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
         const double u2 = mx2 * inv, v2 = my2 * inv;
-        const double q2 = fma(u2, u2, v2 * v2);
-        const double p2 = fma(-0.5 * r2, q2, E - d[1]) * P.gm1;
+        const double w = fma(u, u, v * v);
+        const double K1 = r * w;
+        const double K2 = fma(mx2, u2, my2 * v2);
+        const double p2 = fma(P.hgm1, K1 - K2, fma(-P.gm1, d[1], p));
         const bool pfl = le_zero(p2);
         // reverse; a floored value is a constant
         double r2b = lam_out.f[0][k], u2b = lam_out.f[2][k], v2b = lam_out.f[3][k];
         const double p2b = lam_out.f[1][k];
         double db[NF] = {0, 0, 0, 0};
-        double Eb = 0.0;
+        double rb = 0.0, pb = 0.0, ub = 0.0, vb = 0.0, mx2b = 0.0, my2b = 0.0;
         if (!pfl) {
-            // p2 = (E - d1 - 0.5 r2 (u2^2 + v2^2)) gm1
-            const double Xb = p2b * P.gm1;
-            Eb = Xb;
-            db[1] = -Xb;
-            r2b -= 0.5 * Xb * q2;
-            u2b -= Xb * r2 * u2;
-            v2b -= Xb * r2 * v2;
+            // p2 = p - gm1 d1 + hgm1 (K1 - K2), K1 = r (u^2 + v^2), K2 = mx2 u2 + my2 v2
+            pb = p2b;
+            db[1] = -p2b * P.gm1;
+            const double Kb = p2b * P.hgm1;
+            rb = Kb * w;
+            ub = 2.0 * Kb * r * u;
+            vb = 2.0 * Kb * r * v;
+            mx2b = -Kb * u2;
+            my2b = -Kb * v2;
+            u2b -= Kb * mx2;
+            v2b -= Kb * my2;
         }
         // u2 = mx2 / r2, v2 = my2 / r2
-        const double mx2b = u2b * inv, my2b = v2b * inv;
+        mx2b += u2b * inv;
+        my2b += v2b * inv;
         const double invb = u2b * mx2 + v2b * my2;
         r2b -= invb * inv * inv;
-        double rb = 0.0, pb = 0.0, ub = 0.0, vb = 0.0;
         if (!rfl) {
             rb += r2b;
             db[0] = -r2b;
@@ -79,11 +84,6 @@ __global__ void __launch_bounds__(NT) eadj_update_kernel(Params P, CPlanes U, co
         vb += my2b * r;
         db[2] = -mx2b;
         db[3] = -my2b;
-        // E = p / (gamma - 1) + 0.5 r (u^2 + v^2)
-        pb += Eb * P.inv_gm1;
-        rb += 0.5 * Eb * fma(u, u, v * v);
-        ub += Eb * r * u;
-        vb += Eb * r * v;
         double* s = scratch;
         s[0 * K + k] = rb;
         s[1 * K + k] = pb;
@@ -123,74 +123,64 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     const double un = takeL ? unL : unR, ut = takeL ? utL : utR;
     const double S = takeL ? SL : SR, su = takeL ? suL : suR, mm = takeL ? mL : mR;
     const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
-    const double Fm0 = r * un;
-    const double q = fma(un, un, ut * ut);
-    const double E = fma(p, P.inv_gm1, 0.5 * r * q);
-    double inv = 0.0, rz = 0.0, pst = 0.0, ezn = 0.0, ez = 0.0, drz = 0.0;
-    if (star) {
-        inv = rcp_fast(S - SM);
-        rz = r * (su * inv);
-        pst = fma(mm, SM - un, p);
-        ezn = fma(-p, un, fma(E, su, pst * SM));
-        ez = ezn * inv;
-        drz = rz - r;
-    }
-    // ---- reverse.  F.m = Fm0 [+ S drz]; F.mn = Fm0 un + p [+ S (rz SM - Fm0)];
-    // F.mt = Fm0 ut [+ S ut drz]; F.e = (E + p) un [+ S (ez - E)]
+    const double w = fma(un, un, ut * ut);
+    const double E = fma(p, P.inv_gm1, 0.5 * r * w);
+    // ---- reverse.  Star: F.m = mm q, F.mn = F.m SM + pst, F.mt = F.m ut,
+    // F.e = X q with q = SM / (S - SM), pst = mm (SM - un) + p, X = E su - p un + pst S.
+    // Otherwise F.m = r un, F.mn = F.m un + p, F.mt = F.m ut, F.e = (E + p) un.
     const double Fmb = Fb[0], Fmnb = Fb[1], Fmtb = Fb[2], Feb = Fb[3];
     double rb = 0.0, pb = 0.0, unb = 0.0, utb = 0.0, Sb = 0.0, sub = 0.0, mmb = 0.0;
-    double SMb = 0.0, Eb = 0.0, Fm0b = Fmb;
+    double SMb = 0.0, Eb = 0.0;
     if (star) {
-        Sb += Feb * (ez - E) + Fmtb * ut * drz + Fmb * drz + Fmnb * fma(rz, SM, -Fm0);
-        const double ezb = Feb * S;
-        Eb -= Feb * S;
-        utb += Fmtb * S * drz;
-        double drzb = Fmtb * S * ut + Fmb * S;
-        Fm0b -= Fmnb * S;
-        double rzb = Fmnb * S * SM;
-        SMb += Fmnb * S * rz;
-        // drz = rz - r
-        rzb += drzb;
-        rb -= drzb;
-        // ez = ezn inv, ezn = E su + pst SM - p un
-        const double eznb = ezb * inv;
-        double invb = ezb * ezn;
-        Eb += eznb * su;
-        sub += eznb * E;
-        const double pstb = eznb * SM;
-        SMb += eznb * pst;
-        pb -= eznb * un;
-        unb -= eznb * p;
+        const double inv = rcp_fast(S - SM);
+        const double q = SM * inv;
+        const double pst = fma(mm, SM - un, p);
+        const double Fm = mm * q;
+        const double X = fma(E, su, fma(-p, un, pst * S));
+        double qb = Feb * X;
+        const double Xb = Feb * q;
+        const double Fmbt = fma(Fmnb, SM, fma(Fmtb, ut, Fmb));  // all of F.m's adjoint
+        utb += Fmtb * Fm;
+        SMb += Fmnb * Fm;
+        double pstb = Fmnb;
+        // X = E su - p un + pst S
+        Eb += Xb * su;
+        sub += Xb * E;
+        pb -= Xb * un;
+        unb -= Xb * p;
+        pstb += Xb * S;
+        Sb += Xb * pst;
+        // F.m = mm q
+        mmb += Fmbt * q;
+        qb += Fmbt * mm;
         // pst = mm (SM - un) + p
         mmb += pstb * (SM - un);
         SMb += pstb * mm;
         unb -= pstb * mm;
         pb += pstb;
-        // rz = r su inv
-        rb += rzb * su * inv;
-        sub += rzb * r * inv;
-        invb += rzb * r * su;
-        // inv = 1 / (S - SM)
-        const double t = -invb * inv * inv;
+        // q = SM inv, inv = 1 / (S - SM)
+        SMb += qb * inv;
+        const double t = -(qb * SM) * inv * inv;
         Sb += t;
         SMb -= t;
+    } else {
+        const double Fm0 = r * un;
+        Eb += Feb * un;
+        pb += Feb * un;
+        unb += Feb * (E + p);
+        const double Fm0b = fma(Fmnb, un, fma(Fmtb, ut, Fmb));
+        utb += Fmtb * Fm0;
+        unb += Fmnb * Fm0;
+        pb += Fmnb;
+        // Fm0 = r un
+        rb += Fm0b * un;
+        unb += Fm0b * r;
     }
-    // F.e's base (E + p) un, F.mt's base Fm0 ut, F.mn's base Fm0 un + p
-    Eb += Feb * un;
-    pb += Feb * un;
-    unb += Feb * (E + p);
-    Fm0b += Fmtb * ut + Fmnb * un;
-    utb += Fmtb * Fm0;
-    unb += Fmnb * Fm0;
-    pb += Fmnb;
     // E = p / (gamma - 1) + 0.5 r (un^2 + ut^2)
     pb += Eb * P.inv_gm1;
-    rb += 0.5 * Eb * q;
+    rb += 0.5 * Eb * w;
     unb += Eb * r * un;
     utb += Eb * r * ut;
-    // Fm0 = r un
-    rb += Fm0b * un;
-    unb += Fm0b * r;
     // the K side's adjoints to its side
     double rLb = 0, pLb = 0, unLb = 0, utLb = 0, rRb = 0, pRb = 0, unRb = 0, utRb = 0;
     double SLb = 0, SRb = 0, suLb = 0, suRb = 0, mLb = 0, mRb = 0;

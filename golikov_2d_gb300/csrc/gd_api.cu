@@ -105,6 +105,7 @@ Params make_params(const gd_config& c) {
     P.inv_dx = 1.0 / c.dx;
     P.inv_dy = 1.0 / c.dy;
     P.inv_gm1 = 1.0 / (c.gamma - 1.0);
+    P.hgm1 = 0.5 * (c.gamma - 1.0);
     P.ambient_p = 1.0 / c.gamma;
     // rad passed to the flux: dy on x-faces in the Euler kernels (kernel.cu:1811, 3562),
     // dx on x-faces in the MHD kernels (kernel.cu:2560)
@@ -548,6 +549,7 @@ gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long l
     P.gamma = gamma;
     P.gm1 = gamma - 1.0;
     P.inv_gm1 = 1.0 / (gamma - 1.0);
+    P.hgm1 = 0.5 * (gamma - 1.0);
     const cudaStream_t st = (cudaStream_t)stream;
     GD_CUDA(physics == GD_EULER ? gd::launch_euler_face_probe(P, n, axis, L, R, flux, speed, st)
                                 : gd::launch_mhd_face_probe(P, n, axis, L, R, flux, speed, st));

@@ -18,7 +18,10 @@
 // Two kernels share the tile body: euler_fast_kernel (one grid, one CTA per tile) and
 // euler_batch_kernel (a persistent launch that walks the tiles of many independent grids,
 // each grid with its own parameters, state, dt reduction and funk_time rotation).  Tile
-// shapes 32x16, 32x8, 16x16 and 64x8 are compiled; the autotuner picks one.
+// shapes 16x16, 32x8, 32x16 and 64x8 are compiled; the autotuner picks one for a batch, and
+// the single-grid step uses 16x16 (49 KB of shared memory and 64 registers a thread: four
+// CTAs, 32 warps, per SM; at 32x16, 93 KB, two CTAs left the FP64 pipe waiting on its own
+// results once the flux took fewer operations: 7.01 against 6.49 ms per step at 4096^2).
 //
 // Reference semantics kept: primitive reconstruction of (rho, p, vx, vy) with the rho/p
 // face fallback to the cell value (kernel.cu:3436-3544), Davis wave speeds and the HLLC
@@ -75,22 +78,24 @@ __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T
     const T mm = takeL ? mL : mR;
     const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
 
-    FluxE<T> F;
-    F.m = r * un;
-    F.mn = fma(F.m, un, p);
-    F.mt = F.m * ut;
     const T E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
-    F.e = (E + p) * un;
+    FluxE<T> F;
     if (star) {
-        const T inv = rcp_fast(S - SM);
-        const T rz = r * (su * inv);
-        const T pst = fma(mm, SM - un, p);
-        const T ez = fma(-p, un, fma(E, su, pst * SM)) * inv;
-        const T drz = rz - r;
-        F.mn = fma(S, fma(rz, SM, -F.m), F.mn);
-        F.m = fma(S, drz, F.m);
-        F.mt = fma(S, ut * drz, F.mt);
-        F.e = fma(S, ez - E, F.e);
+        // F_K + S_K (U*_K - U_K) is the physical flux of the star state, F(U*_K) with the
+        // star pressure: the jump conditions across S_K are what define rho*, p* and E*
+        // (kernel.cu:1119-1158).  With q = S_M / (S_K - S_M):
+        //   rho* S_M = mm q,  mom: rho* S_M^2 + p*,  (E* + p*) S_M = q (E su - p u + p* S_K)
+        const T q = SM * rcp_fast(S - SM);
+        const T pst = fma(mm, SM - un, p);  // p* = p_K + rho_K (S_K - u_K) (S_M - u_K)
+        F.m = mm * q;
+        F.mn = fma(F.m, SM, pst);
+        F.mt = F.m * ut;
+        F.e = fma(E, su, fma(-p, un, pst * S)) * q;
+    } else {
+        F.m = r * un;
+        F.mn = fma(F.m, un, p);
+        F.mt = F.m * ut;
+        F.e = (E + p) * un;
     }
     return F;
 }
@@ -359,11 +364,15 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         }
         T r2 = r - d[0];
         if (le_zero(r2)) { r2 = cst<T>(0.0001); ++nfl_r; }
-        const T E = fma(p, P.inv_gm1, 0.5 * r * fma(u, u, v * v));
         const T inv = rcp_fast(r2);
-        const T u2 = fma(r, u, -d[2]) * inv;
-        const T v2 = fma(r, v, -d[3]) * inv;
-        T p2 = fma(-0.5 * r2, fma(u2, u2, v2 * v2), E - d[1]) * P.gm1;
+        const T mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
+        const T u2 = mx2 * inv;
+        const T v2 = my2 * inv;
+        // p' = (gamma - 1) (E - d_E - K'/2) with E = p / (gamma - 1) + K / 2, K = rho |v|^2,
+        // K' = rho' |v'|^2 = m' . v' (kernel.cu:1861-1870)
+        const T K1 = r * fma(u, u, v * v);
+        const T K2 = fma(mx2, u2, my2 * v2);
+        T p2 = fma(P.hgm1, K1 - K2, fma(-P.gm1, d[1], p));
         if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
         if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2)) ++nbad;
         store_cell(out, k, 0, r2);
@@ -490,19 +499,19 @@ cudaError_t launch_batch(const BatchGrid* grids, const int2* items, int nitems, 
     return cudaGetLastError();
 }
 
-// tile shapes of the variants: 0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8
+// tile shapes of the variants: 0: 16x16 (the single-grid step's), 1: 32x8, 2: 32x16, 3: 64x8
 #define GD_EULER_DISPATCH(ORDER, VAR, CALL, ARGS) \
     switch (VAR) {                                \
         case 1: return CALL<ORDER, 32, 8> ARGS;   \
-        case 2: return CALL<ORDER, 16, 16> ARGS;  \
+        case 2: return CALL<ORDER, 32, 16> ARGS;  \
         case 3: return CALL<ORDER, 64, 8> ARGS;   \
-        default: return CALL<ORDER, 32, 16> ARGS; \
+        default: return CALL<ORDER, 16, 16> ARGS; \
     }
 
 }  // namespace
 
 void euler_tile_shape(int variant, int* tx, int* ty) {
-    static const int shapes[kEulerVariants][2] = {{32, 16}, {32, 8}, {16, 16}, {64, 8}};
+    static const int shapes[kEulerVariants][2] = {{16, 16}, {32, 8}, {32, 16}, {64, 8}};
     const int v = (variant >= 0 && variant < kEulerVariants) ? variant : 0;
     *tx = shapes[v][0];
     *ty = shapes[v][1];
@@ -511,9 +520,9 @@ void euler_tile_shape(int variant, int* tx, int* ty) {
 size_t euler_smem_bytes(int order, int variant) {
     switch (variant) {
         case 1: return order == 1 ? Shape<1, 32, 8>::bytes : Shape<2, 32, 8>::bytes;
-        case 2: return order == 1 ? Shape<1, 16, 16>::bytes : Shape<2, 16, 16>::bytes;
+        case 2: return order == 1 ? Shape<1, 32, 16>::bytes : Shape<2, 32, 16>::bytes;
         case 3: return order == 1 ? Shape<1, 64, 8>::bytes : Shape<2, 64, 8>::bytes;
-        default: return order == 1 ? Shape<1, 32, 16>::bytes : Shape<2, 32, 16>::bytes;
+        default: return order == 1 ? Shape<1, 16, 16>::bytes : Shape<2, 16, 16>::bytes;
     }
 }
 
@@ -532,16 +541,16 @@ int euler_batch_blocks_per_sm(int order, int variant) {
     if (order == 1) {
         switch (variant) {
             case 1: return blocks_per_sm<1, 32, 8>();
-            case 2: return blocks_per_sm<1, 16, 16>();
+            case 2: return blocks_per_sm<1, 32, 16>();
             case 3: return blocks_per_sm<1, 64, 8>();
-            default: return blocks_per_sm<1, 32, 16>();
+            default: return blocks_per_sm<1, 16, 16>();
         }
     }
     switch (variant) {
         case 1: return blocks_per_sm<2, 32, 8>();
-        case 2: return blocks_per_sm<2, 16, 16>();
+        case 2: return blocks_per_sm<2, 32, 16>();
         case 3: return blocks_per_sm<2, 64, 8>();
-        default: return blocks_per_sm<2, 32, 16>();
+        default: return blocks_per_sm<2, 16, 16>();
     }
 }
 
@@ -600,8 +609,8 @@ cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Plan
                                   Scalars* ctr, double* aux, cudaStream_t st) {
     // variant 0, the launch gd_advance makes: the recorded step is the plain step
     if (P.order == 1)
-        return launch_single<1, 32, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
-    return launch_single<2, 32, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
+        return launch_single<1, 16, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
+    return launch_single<2, 16, 16>(P, in, out, T_do, T_bits, rot, ctr, 0, st, aux);
 }
 
 cudaError_t launch_euler_batch(int variant, int order, const BatchGrid* grids, const int2* items,

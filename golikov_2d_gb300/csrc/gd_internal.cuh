@@ -38,7 +38,7 @@ struct Params {
     int tile_row0, tile_rows;
     unsigned int tile_nblocks;
     // derived
-    double gm1, inv_gm1;
+    double gm1, inv_gm1, hgm1;  // gamma - 1, 1 / (gamma - 1), (gamma - 1) / 2
     double inv_dx, inv_dy;  // 1/dx, 1/dy: the fast kernels scale fluxes by T_do * inv_dx
     double ambient_p;   // 1/gamma
     double krad_x;      // krit * rad used for faces with an x normal

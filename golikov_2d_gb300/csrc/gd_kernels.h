@@ -19,7 +19,7 @@ cudaError_t prepare_mhd_fast();
 cudaError_t launch_euler_tangent(const Params& P, const CPlanes& in, const CPlanes& din,
                                  const Planes& out, const Planes& dout, const double* T_do,
                                  cudaStream_t st);
-// The Euler step (variant 0) writing its flux differences d[0..3] per cell to `aux`.
+// The Euler step (variant 0, as gd_advance launches it) writing its flux differences d[0..3] per cell to `aux`.
 cudaError_t launch_euler_fast_aux(const Params& P, const CPlanes& in, const Planes& out,
                                   const double* T_do, unsigned long long* T_bits, Scalars* rot,
                                   Scalars* ctr, double* aux, cudaStream_t st);
@@ -43,7 +43,8 @@ int mhd_tile_height();
 // which honour the same band parameters; their blocks are 32 cells wide.
 constexpr int kParityBlockRows = 4;
 
-// Tile-shape variants of the fast Euler kernels (0: 32x16, 1: 32x8, 2: 16x16, 3: 64x8).
+// Tile-shape variants of the fast Euler kernels (0: 16x16, the single-grid step's; 1: 32x8;
+// 2: 32x16; 3: 64x8).
 constexpr int kEulerVariants = 4;
 void euler_tile_shape(int variant, int* tx, int* ty);
 size_t euler_smem_bytes(int order, int variant);

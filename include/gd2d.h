@@ -278,7 +278,7 @@ gd_status gd_adj_switches(gd_ctx* ctx, const double* sp, const double* up, const
  *   GD_BATCH_LOOPED_SYNC as GD_BATCH_LOOPED, the host waiting for each launch to finish
  *                        before the next, as the reference's main loop synchronises after
  *                        each of its launches (kernel.cu:4113-4137); no graph (use_graph 0)
- * gd_batch_autotune times every compiled tile shape (32x16, 32x8, 16x16, 64x8; the halo
+ * gd_batch_autotune times every compiled tile shape (16x16, 32x8, 32x16, 64x8; the halo
  * width is the stencil's, 2 cells for order 2) on the batch's own grids without changing
  * their state or time, and keeps the fastest for GD_BATCH_PERSISTENT. */
 enum { GD_BATCH_PERSISTENT = 0, GD_BATCH_LOOPED = 1, GD_BATCH_LOOPED_SYNC = 2 };
@@ -289,7 +289,8 @@ typedef struct gd_batch_info {
     int tile_x, tile_y;        /* tile shape in use for the persistent schedule */
     int ctas;                  /* CTAs of the persistent launch */
     long long tiles;           /* work items per persistent step */
-    double tuned_ms[4];        /* autotuner: ms per step of each tile shape (0 = not timed) */
+    double tuned_ms[4];        /* autotuner: ms per step of the tile shapes 16x16, 32x8,
+                                  32x16, 64x8 (0 = not timed) */
 } gd_batch_info;
 
 gd_status gd_batch_create(const gd_config* cfgs, int ngrids, gd_batch** out);

@@ -1,5 +1,5 @@
 """Both discrete adjoints (MHD HLLD, Euler HLLC) and their tangents on ragged and tiny periodic
-grids: sides that are not multiples of the tiles (the forward's 32 x 16 and 32 x 8 tiles, the
+grids: sides that are not multiples of the tiles (the forward's 16 x 16 and 32 x 8 tiles, the
 reverse passes' 32 x 4 blocks), down to the smallest grid the context accepts (3 x 3), where
 the stencil's periodic wrap reaches across the whole grid.  On each: the replay reproduces the
 recorded run bit for bit, and the dot-product identity <lam, J v> = <J^T lam, v> between the

@@ -98,7 +98,7 @@ def test_graph_equals_plain(cuda):
 
 
 def test_non_multiple_tile_sizes(cuda, oracle_lib):
-    """Grids that are not multiples of the 32 x 16 tile, both orders."""
+    """Grids that are not multiples of the Euler step's 16 x 16 tile, both orders."""
     for N, M in ((37, 19), (65, 33), (3, 3)):
         for order in (1, 2):
             cfg, s, u, b = problems.four_quadrant(max(N, M), np.random.default_rng(N))
