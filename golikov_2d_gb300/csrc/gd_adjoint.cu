@@ -209,7 +209,7 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
     const bool maxB = dlt(A.un, B.un);               // umaxN = B.un (else A.un)
     const double uminN = minA ? A.un : B.un;
     const double umaxN = maxB ? B.un : A.un;
-    const bool cfB = abs_bits(A.cf) < abs_bits(B.cf);
+    const bool cfB = mag_lt(A.cf, B.cf);
     const double cmax = cfB ? B.cf : A.cf;
     const double SL = uminN - cmax, SR = umaxN + cmax;
     const double suL = SL - A.un, suR = SR - B.un;
@@ -219,8 +219,8 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
     const double SM = SMn * iden;
     const double PTTn = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT));
     const double PTT = PTTn * iden;
-    const bool UUR = abs_bits(SL) < abs_bits(SR);
-    const double UU = UUR ? dabs(SR) : dabs(SL);
+    const bool UUR = mag_lt(SL, SR);
+    const double UU = dabs(UUR ? SR : SL);
     const double iS = rcp_fast(SR - SL);
     const double bnn = fma(SR, B.bn, -SL * A.bn);
     const double bn = bnn * iS;
@@ -229,7 +229,7 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
     const double bbn = bn * bn;
     // star states
     const double ttL = fma(mL, SL - SM, -bbn);
-    const bool gL = abs_bits(ttL) >= 0x3EE4F8B588E368F1ULL;
+    const bool gL = mag_ge(ttL, kMag1em5);
     double itL = 0, cL = 0, dL = 0, vLL, wLL, btL, bzL;
     if (gL) {
         itL = rcp_fast(ttL);
@@ -243,7 +243,7 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
         vLL = A.ut; wLL = 0.0; btL = 0.0; bzL = 0.0;
     }
     const double ttR = fma(mR, SR - SM, -bbn);
-    const bool gR = abs_bits(ttR) >= 0x3EE4F8B588E368F1ULL;
+    const bool gR = mag_ge(ttR, kMag1em5);
     double itR = 0, cR = 0, dR = 0, vRR, wRR, btR, bzR;
     if (gR) {
         itR = rcp_fast(ttR);
@@ -260,7 +260,7 @@ __device__ __forceinline__ void hlld_vjp(const double* qa, const double* qb, con
     double isLL, isRR, sLL, sRR;
     rsqrt_and_sqrt(rLL, isLL, sLL);
     rsqrt_and_sqrt(rRR, isRR, sRR);
-    const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
+    const bool bnz = mag_ge(bn, kMag1em6 + 1);
     const double abn = dabs(bn);
     const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
     const double SRR = bnz ? fma(abn, isRR, SM) : SM;
@@ -736,7 +736,7 @@ __device__ __forceinline__ double ld_b(const CPlanes& U, int f, long long k) {
 __device__ __forceinline__ double slope_sel(double cm, double c, double cp, int& sel) {
     const double l = c - cm, r = cp - c;
     const double s = minmod(l, r);
-    sel = (bits(s) << 1) == 0 ? 0 : ((abs_bits(l) <= abs_bits(r)) ? -1 : 1);
+    sel = mag(s) == 0 ? 0 : (mag_lt(r, l) ? 1 : -1);
     return s;
 }
 
@@ -936,27 +936,27 @@ __device__ __forceinline__ FaceCode face_code(const Params& P, const CPlanes& U,
     const bool maxB = dlt(A.un, B.un);
     const double uminN = minA ? A.un : B.un;
     const double umaxN = maxB ? B.un : A.un;
-    const bool cfB = abs_bits(A.cf) < abs_bits(B.cf);
+    const bool cfB = mag_lt(A.cf, B.cf);
     const double cmax = cfB ? B.cf : A.cf;
     const double SL = uminN - cmax, SR = umaxN + cmax;
     const double suL = SL - A.un, suR = SR - B.un;
     const double mL = A.r * suL, mR = B.r * suR;
     const double iden = rcp_fast(mR - mL);
     const double SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
-    const bool UUR = abs_bits(SL) < abs_bits(SR);
+    const bool UUR = mag_lt(SL, SR);
     const double iS = rcp_fast(SR - SL);
     const double bn = fma(SR, B.bn, -SL * A.bn) * iS;
     const double iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
     const double rLL = mL * iL, rRR = mR * iR;
     const double bbn = bn * bn;
     const double ttL = fma(mL, SL - SM, -bbn);
-    const bool gL = abs_bits(ttL) >= 0x3EE4F8B588E368F1ULL;
+    const bool gL = mag_ge(ttL, kMag1em5);
     const double ttR = fma(mR, SR - SM, -bbn);
-    const bool gR = abs_bits(ttR) >= 0x3EE4F8B588E368F1ULL;
+    const bool gR = mag_ge(ttR, kMag1em5);
     double isLL, isRR, sLL, sRR;
     rsqrt_and_sqrt(rLL, isLL, sLL);
     rsqrt_and_sqrt(rRR, isRR, sRR);
-    const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;
+    const bool bnz = mag_ge(bn, kMag1em6 + 1);
     const double abn = dabs(bn);
     const double SLL = bnz ? fma(-abn, isLL, SM) : SM;
     const double SRR = bnz ? fma(abn, isRR, SM) : SM;

@@ -249,7 +249,7 @@ __device__ __forceinline__ int wrap(int i, int n) {
 __device__ __forceinline__ double slope_sel(double cm, double c, double cp, int& sel) {
     const double l = c - cm, r = cp - c;
     const double s = minmod(l, r);
-    sel = (bits(s) << 1) == 0 ? 0 : ((abs_bits(l) <= abs_bits(r)) ? -1 : 1);
+    sel = mag(s) == 0 ? 0 : (mag_lt(r, l) ? 1 : -1);
     return s;
 }
 

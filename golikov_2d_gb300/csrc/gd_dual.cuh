@@ -77,6 +77,9 @@ __device__ __forceinline__ Dual sqrt_over(Dual a, Dual r) {
     return {v, 0.5 * v * (a.d / a.v - r.d / r.v)};
 }
 __device__ __forceinline__ unsigned long long abs_bits(Dual x) { return abs_bits(x.v); }
+__device__ __forceinline__ unsigned long long mag(Dual x) { return mag(x.v); }
+__device__ __forceinline__ bool mag_lt(Dual a, Dual b) { return mag_lt(a.v, b.v); }
+__device__ __forceinline__ bool mag_ge(Dual x, unsigned long long m) { return mag_ge(x.v, m); }
 __device__ __forceinline__ bool le_zero(Dual x) { return le_zero(x.v); }
 __device__ __forceinline__ bool gt_zero(Dual x) { return gt_zero(x.v); }
 __device__ __forceinline__ bool lt_zero(Dual x) { return lt_zero(x.v); }
@@ -87,12 +90,12 @@ __device__ __forceinline__ Dual dabs(Dual x) { return lt_zero(x.v) ? -x : x; }
 __device__ __forceinline__ Dual dmin(Dual a, Dual b) { return dlt(b.v, a.v) ? b : a; }
 __device__ __forceinline__ Dual dmax(Dual a, Dual b) { return dlt(a.v, b.v) ? b : a; }
 __device__ __forceinline__ Dual max_nonneg(Dual a, Dual b) {
-    return abs_bits(a.v) < abs_bits(b.v) ? b : a;
+    return mag_lt(a, b) ? b : a;
 }
 __device__ __forceinline__ Dual minmod(Dual a, Dual b) {
     const long long ba = bits(a.v), bb = bits(b.v);
     const bool zero = ((ba << 1) == 0) | ((bb << 1) == 0) | ((ba ^ bb) < 0);
-    const Dual m = (abs_bits(a.v) <= abs_bits(b.v)) ? a : b;
+    const Dual m = mag(a.v) <= mag(b.v) ? a : b;
     return zero ? Dual{0.0, 0.0} : m;
 }
 __device__ __forceinline__ double value_of(Dual x) { return x.v; }

@@ -48,8 +48,8 @@ struct FluxE {
 };
 
 // HLLC flux in a local frame: un = normal velocity, ut = in-plane tangential velocity.
-// Returns the flux (mass, normal momentum, tangential momentum, energy) and, in UU,
-// max(|SL|, |SR|).  T is double, or Dual for the tangent (value and derivative, the branch
+// Returns the flux (mass, normal momentum, tangential momentum, energy) and, in UU, SL or
+// SR, the one of larger magnitude (signed; the dt reduction takes |UU|).  T is double, or Dual for the tangent (value and derivative, the branch
 // choices taken on the value).
 template <class T>
 __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
@@ -65,7 +65,7 @@ __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T
     const T suL = SL - unL, suR = SR - unR;
     const T mL = rL * suL, mR = rR * suR;
     const T SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
-    UU = max_nonneg(dabs(SL), dabs(SR));
+    UU = max_nonneg(SL, SR);  // signed: the block reduction takes the magnitude
 
     // Side whose state (or star state) gives the flux at x/t = 0 (kernel.cu:1119-1158).
     const bool takeL = gt_zero(SL) || ge_zero(SM);
@@ -114,7 +114,7 @@ __device__ __forceinline__ FluxE<T> hll_local(T rL, T pL, T unL, T utL, T rR, T 
     const T cm = max_nonneg(cL, cR);
     const T DL = dmin(unL, unR) - cm;
     const T DR = dmax(unL, unR) + cm;
-    UU = max_nonneg(dabs(DL), dabs(DR));
+    UU = max_nonneg(DL, DR);  // signed: the block reduction takes the magnitude
     const bool left = gt_zero(DL), right = !left && lt_zero(DR);
     FluxE<T> F;
     if (left || right) {  // one side's physical flux
@@ -650,7 +650,7 @@ __global__ void euler_face_probe_kernel(Params P, long long n, int axis,
     o[1] = F.e;
     o[2] = isx ? F.mn : F.mt;
     o[3] = isx ? F.mt : F.mn;
-    speed[i] = UU;
+    speed[i] = dabs(UU);
 }
 }  // namespace
 

@@ -486,7 +486,7 @@ __global__ void mhd_face_probe_kernel(Params P, long long n, int axis,
     o[5] = (isx ? F.bt : F.bn) * kSpi4;
     o[6] = F.bz * kSpi4;
     o[7] = F.e;
-    speed[i] = UU;
+    speed[i] = dabs(UU);
 }
 }  // namespace
 

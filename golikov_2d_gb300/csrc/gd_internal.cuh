@@ -102,28 +102,77 @@ __device__ __forceinline__ double clamp_to_end(const Scalars* sc, double T) {
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
-__device__ __forceinline__ unsigned long long abs_bits(double x) {
-    return (unsigned long long)bits(x) & 0x7fffffffffffffffULL;
+
+// The magnitude of x as an order key: the bit pattern shifted left by one, which drops the
+// sign.  For non-NaN a, b: mag(a) < mag(b) <=> |a| < |b|, and mag(x) >> 53 is the biased
+// exponent.  Magnitude comparisons must stay integer operations, and the compiler is apt to
+// turn them into FP64 ones: a mask of the sign bit becomes fabs, issued on the FP64 pipe
+// where no FP64 instruction absorbs it as an operand modifier, and a test of the key against
+// zero becomes an FP64 comparison (measured on sm_103a: two FP64 operations per minmod
+// either way, 18 per Euler cell).  The comparisons the step kernels make per face or per
+// cell (mag_lt, mag_ge, minmod) are therefore written in inline PTX, which the compiler keeps
+// as integer operations.
+__device__ __forceinline__ unsigned long long mag(double x) {
+    return (unsigned long long)bits(x) << 1;
 }
-__device__ __forceinline__ double dabs(double x) { return from_bits((long long)abs_bits(x)); }
+// |a| < |b| for non-NaN a, b
+__device__ __forceinline__ bool mag_lt(double a, double b) {
+    unsigned int r;
+    asm("{\n\t.reg .b64 ma, mb;\n\t.reg .pred p;\n\t"
+        "shl.b64 ma, %1, 1;\n\tshl.b64 mb, %2, 1;\n\t"
+        "setp.lt.u64 p, ma, mb;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "l"(bits(a)), "l"(bits(b)));
+    return r != 0;
+}
+// mag(x) >= m (m a magnitude key)
+__device__ __forceinline__ bool mag_ge(double x, unsigned long long m) {
+    unsigned int r;
+    asm("{\n\t.reg .b64 mx;\n\t.reg .pred p;\n\t"
+        "shl.b64 mx, %1, 1;\n\tsetp.ge.u64 p, mx, %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "l"(bits(x)), "l"(m));
+    return r != 0;
+}
+// mag() of 1e-5 and 1e-6, the HLLD guards' thresholds (Gas_Dinamic.cu:1306-1369)
+constexpr unsigned long long kMag1em5 = 0x3EE4F8B588E368F1ULL << 1;
+constexpr unsigned long long kMag1em6 = 0x3EB0C6F7A0B5ED8DULL << 1;
+// The bit pattern of |x|, masked in inline PTX so that it stays an integer operation.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    unsigned long long r;
+    asm("and.b64 %0, %1, 0x7FFFFFFFFFFFFFFF;" : "=l"(r) : "l"(bits(x)));
+    return r;
+}
+// |x| for use as an FP64 operand (free there as an operand modifier)
+__device__ __forceinline__ double dabs(double x) { return fabs(x); }
 // x <= 0 (for non-NaN x): sign bit set, or +0.
 __device__ __forceinline__ bool le_zero(double x) { return bits(x) <= 0; }
 // x > 0 (for non-NaN x)
 __device__ __forceinline__ bool gt_zero(double x) { return bits(x) > 0; }
 
-// Largest of two non-negative values by bit pattern.
+// Of two values, the one of larger magnitude (for non-negative values, the larger), by bit
+// pattern.
 __device__ __forceinline__ double max_nonneg(double a, double b) {
-    return abs_bits(a) < abs_bits(b) ? b : a;
+    return mag_lt(a, b) ? b : a;
 }
 
 // minmod(a, b): 0 unless a and b are non-zero with the same sign, else the one of smaller
 // magnitude.  Equal, bit for bit, to the reference's (sign(a)+sign(b))/2 * min(|a|,|b|)
-// (kernel.cu:51-62) for non-NaN inputs.
+// (kernel.cu:51-62) for non-NaN inputs.  The sign, zero and magnitude tests and both
+// selects are integer operations in inline PTX (see mag).
 __device__ __forceinline__ double minmod(double a, double b) {
-    const long long ba = bits(a), bb = bits(b);
-    const bool zero = ((ba << 1) == 0) | ((bb << 1) == 0) | ((ba ^ bb) < 0);
-    const double m = (abs_bits(a) <= abs_bits(b)) ? a : b;
-    return zero ? 0.0 : m;
+    long long r;
+    asm("{\n\t.reg .b64 ma, mb, s;\n\t.reg .pred pz, pl;\n\t"
+        "shl.b64 ma, %1, 1;\n\t"
+        "shl.b64 mb, %2, 1;\n\t"
+        "xor.b64 s, %1, %2;\n\t"
+        "setp.lt.s64 pz, s, 0;\n\t"          // signs differ
+        "setp.eq.or.u64 pz, ma, 0, pz;\n\t"  // or a is +-0
+        "setp.eq.or.u64 pz, mb, 0, pz;\n\t"  // or b is +-0
+        "setp.le.u64 pl, ma, mb;\n\t"
+        "selp.b64 %0, %1, %2, pl;\n\t"
+        "selp.b64 %0, 0, %0, pz;\n\t"
+        "}"
+        : "=l"(r) : "l"(bits(a)), "l"(bits(b)));
+    return from_bits(r);
 }
 
 // Order-preserving integer key of a double (non-NaN): a < b  <=>  key(a) < key(b), with
@@ -154,7 +203,7 @@ __device__ __forceinline__ bool ge_zero(double x) { return !lt_zero(x); }
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ bool in_f32_range(double x) {
     // biased exponent within [1023-120, 1023+120]
-    const unsigned int e = (unsigned int)((abs_bits(x) >> 52));
+    const unsigned int e = (unsigned int)(mag(x) >> 53);
     return (e - 903u) <= 240u;
 }
 
@@ -228,7 +277,7 @@ __device__ __forceinline__ double sqrt_over(double a, double r) { return a * rsq
 
 // isfinite(x) on the integer pipe: the exponent field is not all ones
 __device__ __forceinline__ bool finite_bits(double x) {
-    return (abs_bits(x) >> 52) != 0x7ffULL;
+    return (mag(x) >> 53) != 0x7ffULL;
 }
 
 // ---------------------------------------------------------------------------------------

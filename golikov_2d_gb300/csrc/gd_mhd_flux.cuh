@@ -94,7 +94,8 @@ __device__ __forceinline__ Dual sgn_select(Dual v, int idbn) {
     return idbn == 0 ? Dual{0.0, 0.0} : (idbn < 0 ? -v : v);
 }
 
-// HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = max(|SL|, |SR|).  The energy and the
+// HLLD (method 3) or HLLC-MHD (method 2) flux.  UU = SL or SR, the one of larger magnitude
+// (signed; the dt reduction takes |UU|).  The energy and the
 // physical flux are formed for the sides that use them: both for HLLC-MHD (its HLL state of
 // the fan), the upwind side K alone for HLLD, whose star energy is likewise K's alone.
 template <class T>
@@ -109,7 +110,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
     const T iden = rcp_fast(mR - mL);
     const T SM = ((fma(mR, B.un, -mL * A.un) - B.pT) + A.pT) * iden;
     const T PTT = fma(mL * mR, B.un - A.un, fma(mR, A.pT, -mL * B.pT)) * iden;
-    UU = max_nonneg(dabs(SL), dabs(SR));
+    UU = max_nonneg(SL, SR);  // signed: the block reduction takes the magnitude
     const T iS = rcp_fast(SR - SL);
     const T bn = fma(SR, B.bn, -SL * A.bn) * iS;
     const T iL = rcp_fast(SL - SM), iR = rcp_fast(SR - SM);
@@ -161,7 +162,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
         T vLL, wLL, btL, bzL, vRR, wRR, btR, bzR;
         {
             const T tt = fma(mL, SL - SM, -bbn);
-            if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {  // |tt| >= 1e-5
+            if (mag_ge(tt, kMag1em5)) {  // |tt| >= 1e-5
                 const T it = rcp_fast(tt);
                 const T c = bn * (SM - A.un) * it;
                 const T d = fma(mL, suL, -bbn) * it;
@@ -175,7 +176,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
         }
         {
             const T tt = fma(mR, SR - SM, -bbn);
-            if (abs_bits(tt) >= 0x3EE4F8B588E368F1ULL) {
+            if (mag_ge(tt, kMag1em5)) {
                 const T it = rcp_fast(tt);
                 const T c = bn * (SM - B.un) * it;
                 const T d = fma(mR, suR, -bbn) * it;
@@ -191,7 +192,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
         T isLL, isRR, sLL, sRR;
         rsqrt_and_sqrt(rLL, isLL, sLL);
         rsqrt_and_sqrt(rRR, isRR, sRR);
-        const bool bnz = abs_bits(bn) > 0x3EB0C6F7A0B5ED8DULL;  // |bn| > 1e-6
+        const bool bnz = mag_ge(bn, kMag1em6 + 1);  // |bn| > 1e-6
         const T abn = dabs(bn);
         const T SLL = bnz ? fma(-abn, isLL, SM) : SM;
         const T SRR = bnz ? fma(abn, isRR, SM) : SM;
@@ -243,7 +244,7 @@ __device__ __forceinline__ FluxM<T> hlld_local(const Side<T>& A, const Side<T>& 
         }
     }
     // normal-field flux replaced by the diffusive term (Gas_Dinamic.cu:1488-1490)
-    F.bn = -UU * (B.bn - A.bn);
+    F.bn = -dabs(UU) * (B.bn - A.bn);
     return F;
 }
 
