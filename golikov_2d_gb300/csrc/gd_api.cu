@@ -246,7 +246,6 @@ gd_status gd_destroy(gd_ctx* ctx) {
     gd::dev_free(ctx->state[0]);
     gd::dev_free(ctx->state[1]);
     gd::dev_free(ctx->sc);
-    gd::dev_free(ctx->ref_planes);
     gd::dev_free(ctx->aos);
     gd::adj_free(ctx);
     gd::io_free(ctx);
@@ -284,15 +283,16 @@ gd_status gd_step_ref(gd_ctx* ctx, const double* s, const double* u, const doubl
         P.method = method;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    if (!ctx->ref_planes)
-        GD_CUDA(gd::dev_alloc(&ctx->ref_planes, sizeof(double) * 2 * (size_t)ctx->nf * ctx->K));
-    const Planes pin = ctx->ref_plane_set(0), pout = ctx->ref_plane_set(1);
-    GD_CUDA(gd::launch_aos_to_soa(s, u, b, pin, ctx->K, ctx->nf, st));
-    ctx->launches += 1;
-    GD_CUDA(launch_step(ctx, P, gd_ctx::cplanes(pin), pout, T_do, (unsigned long long*)T, nullptr,
-                        ctx->sc, 0, st));
-    GD_CUDA(gd::launch_soa_to_aos(gd_ctx::cplanes(pout), s2, u2, b2, ctx->K, ctx->nf, st));
-    ctx->launches += 1;
+    // the step reads and writes the reference layout itself: one launch, no staging
+    CPlanes in{};
+    in.s = s;
+    in.u = u;
+    in.b = ctx->nf == 7 ? b : nullptr;
+    Planes out{};
+    out.s = s2;
+    out.u = u2;
+    out.b = ctx->nf == 7 ? b2 : nullptr;
+    GD_CUDA(launch_step(ctx, P, in, out, T_do, (unsigned long long*)T, nullptr, ctx->sc, 0, st));
     return GD_OK;
 }
 

@@ -12,7 +12,8 @@ namespace gd {
 // Record of a differentiated forward run (gd_adj_forward): dt sequence, checkpoints and
 // work buffers of the reverse and tangent sweeps.
 // gd_step_host: the two copy streams, the events of the band pipeline and the AoS staging
-// of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K).
+// of the input and of the output (7 K doubles each: s 2K, u 2K, b 3K), which the step reads
+// and writes directly.
 // The banded step is captured once per (host buffers, current plane set) into a CUDA graph
 // and replayed: a graph launch puts all of a step's copies and launches on the GPU at once,
 // where enqueuing them one API call at a time (a dozen per band) paces a short step.
@@ -81,7 +82,6 @@ struct gd_ctx {
     double* state[2] = {nullptr, nullptr};  // nf planes of K doubles each
     int cur = 0;
     Scalars* sc = nullptr;                  // device scalars of the resident state
-    double* ref_planes = nullptr;           // 2 * nf * K: SoA in/out for gd_step_ref
     double* aos = nullptr;                  // 7 * K: AoS staging for host import/export
     long long launches = 0;
     int step_launches = 1;                  // kernel launches of one step (fast Hancock: 2)
@@ -103,12 +103,6 @@ struct gd_ctx {
         CPlanes c{};
         for (int f = 0; f < gd::kMaxFields; ++f) c.f[f] = p.f[f];
         return c;
-    }
-    Planes ref_plane_set(int which) const {
-        Planes p{};
-        for (int f = 0; f < gd::kMaxFields; ++f)
-            p.f[f] = f < nf ? ref_planes + ((size_t)which * nf + f) * K : nullptr;
-        return p;
     }
 };
 

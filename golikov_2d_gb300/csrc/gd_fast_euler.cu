@@ -176,7 +176,7 @@ __device__ __forceinline__ void load_cell(const Params& P, const DualIn& in, int
     for (int f = 0; f < NF; ++f) v[f] = Dual{a[f], b[f]};
 }
 __device__ __forceinline__ void store_cell(const Planes& out, long long k, int f, double x) {
-    out.f[f][k] = x;
+    store_f(out, f, k, x);
 }
 __device__ __forceinline__ void store_cell(const DualOut& out, long long k, int f, Dual x) {
     out.v.f[f][k] = x.v;

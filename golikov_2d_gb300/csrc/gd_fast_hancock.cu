@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
         if (gx >= 0 && gx < N && gy >= 0 && gy < M) {
             const long long k = (long long)gy * N + gx;
 #pragma unroll
-            for (int f = 0; f < NF; ++f) v[f] = in.f[f][k];
+            for (int f = 0; f < NF; ++f) v[f] = load_f(in, f, k);
             v[4] *= kInvSpi4;
             v[5] *= kInvSpi4;
             v[6] *= kInvSpi4;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
     if (my_flag == 1 && !dt_only) {
         const long long k = (long long)gy * N + gx;
 #pragma unroll
-        for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+        for (int f = 0; f < NF; ++f) store_f(out, f, k, load_f(in, f, k));
     } else if (my_flag == 2 && !dt_only) {
         const double hT = 0.5 * T_do;
         const double kx = hT * P.inv_dx, ky = hT * P.inv_dy;
@@ -324,13 +324,13 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
             !finite_bits(bx2) || !finite_bits(by2) || !finite_bits(bz2))
             ++nbad;
         const long long k = (long long)gy * N + gx;
-        out.f[0][k] = r2;
-        out.f[1][k] = p2;
-        out.f[2][k] = u2;
-        out.f[3][k] = v2;
-        out.f[4][k] = bx2 * kSpi4;
-        out.f[5][k] = by2 * kSpi4;
-        out.f[6][k] = bz2 * kSpi4;
+        store_f(out, 0, k, r2);
+        store_f(out, 1, k, p2);
+        store_f(out, 2, k, u2);
+        store_f(out, 3, k, v2);
+        store_f(out, 4, k, bx2 * kSpi4);
+        store_f(out, 5, k, by2 * kSpi4);
+        store_f(out, 6, k, bz2 * kSpi4);
     }
     if (ctr != nullptr && (nfl_r | nfl_p | nbad)) {
         if (nfl_r) atomicAdd(&ctr->rho_floor, (unsigned long long)nfl_r);
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
         const double y = hancock_y(P, m);
         if (hancock_frozen(P, n, y)) {
             if (!dt_only)
-                for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+                for (int f = 0; f < NF; ++f) store_f(out, f, k, load_f(in, f, k));
         } else {
             active = true;
             double res[NF];
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(BNT) hancock_band_kernel(Params P, CPlanes in,
                         break;
                     }
                 }
-                for (int f = 0; f < NF; ++f) out.f[f][k] = res[f];
+                for (int f = 0; f < NF; ++f) store_f(out, f, k, res[f]);
             }
         }
     }

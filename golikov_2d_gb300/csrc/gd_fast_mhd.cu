@@ -75,7 +75,7 @@ __device__ __forceinline__ void load_state(const Params& P, const DualCPlanes& i
 }
 
 __device__ __forceinline__ void store_state(const Planes& out, long long k, int f, double x) {
-    out.f[f][k] = x;
+    store_f(out, f, k, x);
 }
 __device__ __forceinline__ void store_state(const DualPlanes& out, long long k, int f, Dual x) {
     out.v.f[f][k] = x.v;
@@ -83,7 +83,7 @@ __device__ __forceinline__ void store_state(const DualPlanes& out, long long k, 
 }
 __device__ __forceinline__ void copy_cell(const CPlanes& in, const Planes& out, long long k) {
 #pragma unroll
-    for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+    for (int f = 0; f < NF; ++f) store_f(out, f, k, load_f(in, f, k));
 }
 __device__ __forceinline__ void copy_cell(const DualCPlanes& in, const DualPlanes& out,
                                           long long k) {

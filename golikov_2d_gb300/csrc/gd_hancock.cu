@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(HNT) hancock_parity_kernel(Params P, CPlanes i
         const double y = hancock_y(P, m);
         if (hancock_frozen(P, n, y)) {
             if (!dt_only)
-                for (int f = 0; f < 7; ++f) out.f[f][k] = in.f[f][k];
+                for (int f = 0; f < 7; ++f) store_f(out, f, k, load_f(in, f, k));
         } else {
             active = true;
             double res[7];
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(HNT) hancock_parity_kernel(Params P, CPlanes i
                         break;
                     }
                 }
-                for (int f = 0; f < 7; ++f) out.f[f][k] = res[f];
+                for (int f = 0; f < 7; ++f) store_f(out, f, k, res[f]);
             }
         }
     }

@@ -32,7 +32,7 @@ __device__ __forceinline__ HC hload(const CPlanes& in, int N, int n, int m) {
     HC c;
     const long long k = (long long)m * N + n;
 #pragma unroll
-    for (int f = 0; f < 7; ++f) c.q[f] = in.f[f][k];
+    for (int f = 0; f < 7; ++f) c.q[f] = load_f(in, f, k);
     return c;
 }
 

@@ -5,10 +5,12 @@
 // The reference moves its state between host and device with blocking cudaMemcpy calls
 // around its loop (kernel.cu:4005-4010, 4093-4095, 4163-4165).  gd_import + gd_advance(1) +
 // gd_export does the same in three sequential phases.  Here the grid is cut into bands of
-// whole tile rows.  Band k's rows go up and are converted to planes on one copy stream; on
-// the caller's stream band k is stepped as soon as its neighbours' rows (the stencil's halo)
-// are there; its output is converted back and goes down on a second copy stream while later
-// bands are stepped.  The two copy directions and the SMs work at once, so a step costs
+// whole tile rows.  Band k's rows go up, in the reference's AoS layout, to a device staging
+// buffer on one copy stream; on the caller's stream band k is stepped as soon as its
+// neighbours' rows (the stencil's halo) are there, the step reading the staging buffer
+// itself and writing its output both to the context's planes (the resident state) and to
+// an AoS staging buffer, from which it goes down on a second copy stream while later bands
+// are stepped: no conversion pass.  The two copy directions and the SMs work at once, so a step costs
 // about the step itself plus one band of each copy.  The whole banded step is captured into
 // a CUDA graph per (host buffers, plane set) and replayed, so its few hundred copies and
 // launches reach the GPU in one submission.  The step is the same kernel with the
@@ -94,32 +96,6 @@ cudaError_t copy_rows(double* dst_s, double* dst_u, double* dst_b, const double*
     return cudaSuccess;
 }
 
-Planes shift(Planes p, int nf, long long c0) {
-    for (int f = 0; f < nf; ++f) p.f[f] += c0;
-    return p;
-}
-CPlanes cshift(Planes p, int nf, long long c0) {
-    CPlanes c{};
-    for (int f = 0; f < nf; ++f) c.f[f] = p.f[f] + c0;
-    return c;
-}
-
-cudaError_t to_planes(gd_ctx* ctx, Rows r, cudaStream_t st) {
-    const double* a = ctx->pipe->aos_in;
-    const long long K = ctx->K;
-    ctx->launches += 1;
-    return gd::launch_aos_to_soa(a + 2 * r.c0, a + 2 * K + 2 * r.c0, a + 4 * K + 3 * r.c0,
-                                 shift(ctx->planes(ctx->cur), ctx->nf, r.c0), r.n, ctx->nf, st);
-}
-
-cudaError_t from_planes(gd_ctx* ctx, Rows r, cudaStream_t st) {
-    double* a = ctx->pipe->aos_out;
-    const long long K = ctx->K;
-    ctx->launches += 1;
-    return gd::launch_soa_to_aos(cshift(ctx->planes(1 - ctx->cur), ctx->nf, r.c0),
-                                 a + 2 * r.c0, a + 2 * K + 2 * r.c0, a + 4 * K + 3 * r.c0, r.n,
-                                 ctx->nf, st);
-}
 
 // The banded step.  Returns a CUDA error or cudaSuccess; the caller synchronises.
 cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const double* b,
@@ -174,30 +150,26 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     HS_TRY(cudaEventRecord(p->start, st));
     HS_TRY(cudaStreamWaitEvent(p->up, p->start, 0));
     HS_TRY(cudaStreamWaitEvent(p->down, p->start, 0));
-    // up stream: host rows to the AoS staging, then to the planes of the current state; the
-    // seam rows first, then the bands in order
+    // up stream: host rows to the AoS staging; the seam rows first, then the bands in order
     const Rows wrap_rows{(long long)(M - H) * N, (long long)H * N};
-    if (wrap) {
+    if (wrap)
         HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, wrap_rows, nf,
                          cudaMemcpyHostToDevice, p->up));
-        HS_TRY(to_planes(ctx, wrap_rows, p->up));
-    }
     int n_up = 0;  // bands whose upload is enqueued
     auto enqueue_up = [&](int upto) -> cudaError_t {
         for (; n_up <= upto && n_up < B; ++n_up) {
             const Rows r = band_rows_up(n_up);
             HS_TRY(copy_rows(ai, ai + 2 * K, ai + 4 * K, s, u, b, r, nf,
                              cudaMemcpyHostToDevice, p->up));
-            HS_TRY(to_planes(ctx, r, p->up));
             HS_TRY(cudaEventRecord(p->ev_up[n_up], p->up));
         }
         return cudaSuccess;
     };
-    // down stream: band k's result to AoS and to the host while later bands are stepped
+    // down stream: band k's result from the AoS staging to the host while later bands are
+    // stepped
     auto enqueue_down = [&](int k) -> cudaError_t {
         HS_TRY(cudaStreamWaitEvent(p->down, p->ev_out[k], 0));
         if (hk) HS_TRY(cudaStreamWaitEvent(p->down, p->edge_done, 0));
-        HS_TRY(from_planes(ctx, band_rows(k), p->down));
         return copy_rows(s2, u2, b2, ao, ao + 2 * K, ao + 4 * K, band_rows(k), nf,
                          cudaMemcpyDeviceToHost, p->down);
     };
@@ -205,8 +177,8 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
     // next upload, the step and the download, so the first step is queued after two bands'
     // uploads rather than after all of them (each band is a dozen API calls).
     HS_TRY(enqueue_up(1));
-    // the step on band k once bands k and k + 1 are planes (band k - 1, and the seam rows,
-    // came before), bands taken in turn by the caller's stream and kCompStreams - 1 more:
+    // the step on band k once bands k and k + 1 are up (band k - 1, and the seam rows, came
+    // before), bands taken in turn by the caller's stream and kCompStreams - 1 more:
     // the bands write disjoint rows and share one rotation ticket, so later bands' blocks
     // may start while the last wave of this one drains
     Params P = ctx->P;
@@ -219,8 +191,16 @@ cudaError_t banded_step(gd_ctx* ctx, const double* s, const double* u, const dou
             nblocks += gd::hancock_fast_blocks(P, row_bound(k), row_bound(k + 1), 2);
     }
     P.tile_nblocks = nblocks;
-    const CPlanes in = gd_ctx::cplanes(ctx->planes(ctx->cur));
-    const Planes out = ctx->planes(1 - ctx->cur);
+    // in: the AoS staging of the upload; out: the next resident plane set and the AoS
+    // staging of the download
+    CPlanes in{};
+    in.s = ai;
+    in.u = ai + 2 * K;
+    in.b = nf == 7 ? ai + 4 * K : nullptr;
+    Planes out = ctx->planes(1 - ctx->cur);
+    out.s = ao;
+    out.u = ao + 2 * K;
+    out.b = nf == 7 ? ao + 4 * K : nullptr;
     for (int k = 0; k < B; ++k) {
         HS_TRY(enqueue_up(k + 2));
         const int si = k % gd::kCompStreams;

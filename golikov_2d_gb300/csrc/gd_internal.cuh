@@ -45,13 +45,32 @@ struct Params {
     double krad_y;      // krit * rad used for faces with a y normal
 };
 
-// SoA planes: f[k] + m*N + n.
+// A state: SoA planes, f[k] + m*N + n; or, where s is set, the reference's AoS layout
+// (kernel.cu:3814-3825: s = {rho, p}, u = {vx, vy}, b = {Bx, By, Bz} per cell), which the
+// drop-in step (gd_step_ref) and the host-to-host step (gd_step_host) read and write without
+// a conversion pass.  An output with both set is written in both layouts.  Step kernels
+// access a field of a cell through load_f / store_f; the layout test is the same for every
+// thread of a launch.
 struct Planes {
     double* f[kMaxFields];
+    double *s, *u, *b;
 };
 struct CPlanes {
     const double* f[kMaxFields];
+    const double *s, *u, *b;
 };
+__device__ __forceinline__ double load_f(const CPlanes& p, int f, long long k) {
+    if (p.s == nullptr) return p.f[f][k];
+    return f < 2 ? p.s[2 * k + f] : (f < 4 ? p.u[2 * k + (f - 2)] : p.b[3 * k + (f - 4)]);
+}
+__device__ __forceinline__ void store_f(const Planes& p, int f, long long k, double x) {
+    if (p.f[0] != nullptr) p.f[f][k] = x;
+    if (p.s != nullptr) {
+        if (f < 2) p.s[2 * k + f] = x;
+        else if (f < 4) p.u[2 * k + (f - 2)] = x;
+        else p.b[3 * k + (f - 4)] = x;
+    }
+}
 
 struct Scalars;
 
@@ -338,7 +357,7 @@ __device__ __forceinline__ void fetch_cell(const Params& P, const CPlanes& in, i
     }
     const long long k = (long long)sy * P.N + sx;
 #pragma unroll
-    for (int f = 0; f < NF; ++f) v[f] = in.f[f][k];
+    for (int f = 0; f < NF; ++f) v[f] = load_f(in, f, k);
     if (bc >= 0) ghost_transform<NF>(v, bc, P.ambient_p);
 }
 

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(PNT) parity_kernel(Params P, CPlanes in, Plane
         if (P.frozen_radius > 0.0) frozen = sqrt(x * x + y * y) < P.frozen_radius;
         if (frozen) {
             if (!dt_only)
-                for (int f = 0; f < NF; ++f) out.f[f][k] = in.f[f][k];
+                for (int f = 0; f < NF; ++f) store_f(out, f, k, load_f(in, f, k));
         } else {
             active = true;
             const double dx = P.dx, dy = P.dy;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(PNT) parity_kernel(Params P, CPlanes in, Plane
                 for (int f = 0; f < NF; ++f) {
                     if (!isfinite(res[f])) { ++nbad; break; }
                 }
-                for (int f = 0; f < NF; ++f) out.f[f][k] = res[f];
+                for (int f = 0; f < NF; ++f) store_f(out, f, k, res[f]);
             }
         }
     }
