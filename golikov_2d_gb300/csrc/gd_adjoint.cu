@@ -164,13 +164,12 @@ __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params
     double disc = fma(S.a, S.a, -4.0 * S.gp * S.bn2);
     S.disc0 = le_zero(disc);
     S.disc = S.disc0 ? 0.0 : disc;
-    // sqrt_fast(disc) = disc * rsqrt_fast(disc), kept apart so the reverse reuses 1/sqrt
-    S.rq = rsqrt_fast(S.disc);
-    const double sq = (bits(S.disc) << 1) == 0 ? 0.0 : S.disc * S.rq;
+    // sqrt_fast(disc) of the forward, keeping 1/sqrt(disc) for the reverse
+    double sq;
+    sqrt_and_rs(S.disc, sq, S.rq);
     const double X = 0.5 * (S.a + sq);
     // cf = sqrt_over(X, r) of the forward, keeping its 1/sqrt(X r) for the reverse
-    S.rs = rsqrt_times(X, S.r);
-    S.cf = X * S.rs;
+    sqrt_over_rs(X, S.r, S.cf, S.rs);
 }
 
 // per-side adjoint accumulators of the face state and of two derived quantities

@@ -106,8 +106,9 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     const double rR = b[0], pR = b[1], unR = b[2], utR = b[3];
     // ---- forward
     const double gpL = g * pL, gpR = g * pR;
-    const double rsL = rsqrt_times(gpL, rL), rsR = rsqrt_times(gpR, rR);
-    const double cL = gpL * rsL, cR = gpR * rsR;  // sqrt_over(g p, rho)
+    double cL, cR, rsL, rsR;  // sqrt_over(g p, rho) of the forward and 1/sqrt(g p rho)
+    sqrt_over_rs(gpL, rL, cL, rsL);
+    sqrt_over_rs(gpR, rR, cR, rsR);
     const double aL = unL - cL, aR = unR - cR;
     const double bL = unL + cL, bR = unR + cR;
     const bool slR = dlt(aR, aL);  // SL = dmin(aL, aR)

@@ -57,9 +57,11 @@ __device__ __forceinline__ Dual rsqrt_fast(Dual x) {
     return {r, -0.5 * x.d * r * r * r};
 }
 __device__ __forceinline__ Dual sqrt_fast(Dual x) {
+    // the value as the double step computes it, so the tangent takes the step's branches
+    double s, r;
+    sqrt_and_rs(x.v, s, r);
     if (x.v == 0.0) return {0.0, 0.0};
-    const double r = rsqrt_fast(x.v);
-    return {x.v * r, 0.5 * x.d * r};
+    return {s, 0.5 * x.d * r};
 }
 
 // value-only predicates and selections (derivative follows the selected branch)

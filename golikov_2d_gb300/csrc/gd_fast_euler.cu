@@ -231,23 +231,42 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
     __syncthreads();
 
     // ---- S: slopes --------------------------------------------------------------------------
+    // A thread takes a run of G cells along the direction, so neighbouring slopes share their
+    // difference: G + 1 FP64 subtractions per G cells instead of 2 G.
     if (ORDER == 2) {
-        for (int i = tid; i < TY * (TX + 2); i += NT) {
-            const int ly = i / (TX + 2), c = i - ly * (TX + 2);  // cell x = c - 1
-            const T* row = prim + (ly + H) * SX + (c - 1 + H);
+        constexpr int GX = (TX + 2) % 3 == 0 ? 3 : 2, GY = (TY + 2) % 3 == 0 ? 3 : 2;
+        constexpr int NGX = (TX + 2) / GX, NGY = (TY + 2) / GY;
+        static_assert((TX + 2) % GX == 0 && (TY + 2) % GY == 0, "slope runs tile the rows");
+        for (int i = tid; i < TY * NGX; i += NT) {
+            const int ly = i / NGX, c0 = (i - ly * NGX) * GX;  // cells x = c0 - 1 ...
+            const T* row = prim + (ly + H) * SX + (c0 - 1 + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 const T* q = row + f * SY * SX;
-                slx[(f * TY + ly) * (TX + 2) + c] = minmod(q[0] - q[-1], q[1] - q[0]);
+                T* o = slx + (f * TY + ly) * (TX + 2) + c0;
+                T dl = q[0] - q[-1];
+#pragma unroll
+                for (int j = 0; j < GX; ++j) {
+                    const T dr = q[j + 1] - q[j];
+                    o[j] = minmod(dl, dr);
+                    dl = dr;
+                }
             }
         }
-        for (int i = tid; i < (TY + 2) * TX; i += NT) {
-            const int r = i / TX, lx = i - r * TX;  // cell y = r - 1
-            const T* col = prim + (r - 1 + H) * SX + (lx + H);
+        for (int i = tid; i < NGY * TX; i += NT) {
+            const int g = i / TX, lx = i - g * TX, r0 = g * GY;  // cells y = r0 - 1 ...
+            const T* col = prim + (r0 - 1 + H) * SX + (lx + H);
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
                 const T* q = col + f * SY * SX;
-                sly[(f * (TY + 2) + r) * TX + lx] = minmod(q[0] - q[-SX], q[SX] - q[0]);
+                T* o = sly + (f * (TY + 2) + r0) * TX + lx;
+                T dl = q[0] - q[-SX];
+#pragma unroll
+                for (int j = 0; j < GY; ++j) {
+                    const T dr = q[(j + 1) * SX] - q[j * SX];
+                    o[j * TX] = minmod(dl, dr);
+                    dl = dr;
+                }
             }
         }
         __syncthreads();

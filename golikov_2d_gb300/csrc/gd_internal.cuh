@@ -204,8 +204,10 @@ __device__ __forceinline__ long long okey(double x) {
 __device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }
 __device__ __forceinline__ double dmin(double a, double b) { return dlt(b, a) ? b : a; }
 __device__ __forceinline__ double dmax(double a, double b) { return dlt(a, b) ? b : a; }
-// x < 0 strictly (-0 is not negative), x >= 0
-__device__ __forceinline__ bool lt_zero(double x) { return bits(x) < 0 && (bits(x) << 1) != 0; }
+// x < 0 strictly (-0 is not negative), x >= 0: the bit pattern, as unsigned, above -0's
+__device__ __forceinline__ bool lt_zero(double x) {
+    return (unsigned long long)bits(x) > 0x8000000000000000ULL;
+}
 __device__ __forceinline__ bool ge_zero(double x) { return !lt_zero(x); }
 
 // ---------------------------------------------------------------------------------------
@@ -264,9 +266,29 @@ __device__ __forceinline__ double rsqrt_fast(double x) {
     return rsqrt_newton(x);
 }
 
+// sqrt(x) and 1/sqrt(x) from one seed y ~ 1/sqrt(x): with w = x y and e = 1 - w y,
+// sqrt(x) = w (1 + e/2 + 3 e^2 / 8) and 1/sqrt(x) = y (1 + e/2 + 3 e^2 / 8) to O(e^3): five
+// FP64 operations for the root alone, where x * rsqrt(x) takes six.  Outside the fast range
+// (rsqrt_ok), the correctly rounded pair, with sqrt(+-0) = 0 exactly.
+__device__ __forceinline__ void sqrt_and_rs(double x, double& sx, double& ix) {
+    if (!rsqrt_ok(x)) {
+        sx = sqrt(x);
+        ix = 1.0 / sx;
+        return;
+    }
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double w = x * y;
+    const double e = fma(-w, y, 1.0);
+    const double et = e * fma(0.375, e, 0.5);
+    sx = fma(w, et, w);
+    ix = fma(y, et, y);
+}
 __device__ __forceinline__ double sqrt_fast(double x) {
-    // sqrt(x) = x * rsqrt(x), exact zero preserved (the +-0 test on the integer pipe)
-    return (bits(x) << 1) == 0 ? 0.0 : x * rsqrt_fast(x);
+    double sx, ix;
+    sqrt_and_rs(x, sx, ix);
+    return sx;
 }
 
 // 1/sqrt(x) and sqrt(x) = x / sqrt(x) together; where the fast path does not apply, the
@@ -289,10 +311,46 @@ __device__ __forceinline__ double rsqrt_times(double a, double r) {
     return rsqrt_newton(x);
 }
 
-// sqrt(a / r) (a sound or fast magnetosonic speed, a >= 0) as a * rsqrt(a r): a = 0 gives 0,
-// as the reference's sqrt(a / r) (the plain product would be 0 * inf); r = 0 gives inf and
-// r < 0 NaN, as there
-__device__ __forceinline__ double sqrt_over(double a, double r) { return a * rsqrt_times(a, r); }
+// The seed of 1/sqrt(a r) without the FP64 product: the leading 23 bits of each factor
+// re-biased into FP32 (integer pipe), one FP32 product, the FP32 rsqrt; valid for a and r
+// positive with exponents within +-60 of 1 (each factor's truncation 2^-23, the product's
+// rounding 2^-24, the rsqrt's error ~2^-23: a relative seed error below 2^-21).
+__device__ __forceinline__ bool in_half_range_pos(double x) {
+    const unsigned int e = (unsigned int)(mag(x) >> 53);
+    return gt_zero(x) && (e - 963u) <= 120u;
+}
+__device__ __forceinline__ float seed23_f32(double x) {
+    const int hi = __double2hiint(x);
+    const unsigned int lo = (unsigned int)__double2loint(x);
+    return __int_as_float((hi & (int)0x80000000) |
+                          (((hi & 0x7fffffff) - (896 << 20)) << 3) | (int)(lo >> 29));
+}
+
+// sqrt(a / r) (a sound or fast magnetosonic speed, a >= 0) and 1/sqrt(a r).  With y the seed
+// of 1/sqrt(a r), w = a y and e = 1 - w r y: sqrt(a / r) = w (1 + e/2 + 3 e^2 / 8) to O(e^3),
+// six FP64 operations where a * rsqrt(a r) takes seven.  Outside the seeded range: a = 0
+// gives 0, as the reference's sqrt(a / r) (the plain product would be 0 * inf); r = 0 gives
+// inf and r < 0 NaN, as there.
+__device__ __forceinline__ void sqrt_over_rs(double a, double r, double& c, double& rs) {
+    if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
+        rs = rsqrt_times(a, r);
+        c = a * rs;
+        return;
+    }
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
+    const double y = widen_f32(f);
+    const double w = a * y;
+    const double e = fma(-w, r * y, 1.0);
+    const double et = e * fma(0.375, e, 0.5);
+    c = fma(w, et, w);
+    rs = fma(y, et, y);
+}
+__device__ __forceinline__ double sqrt_over(double a, double r) {
+    double c, rs;
+    sqrt_over_rs(a, r, c, rs);
+    return c;
+}
 
 // isfinite(x) on the integer pipe: the exponent field is not all ones
 __device__ __forceinline__ bool finite_bits(double x) {

@@ -4,7 +4,10 @@ Bounds, stated here and asserted:
   * one step from the same state: relative L1 difference of every conserved field
     (rho, rho v, E[, B]) <= 1e-12 (PER_STEP_TOL);
   * N steps of the full lagged-dt protocol: <= NSTEP_TOL (rounding differences between
-    face-once / reference-order arithmetic grow through the nonlinear dynamics);
+    face-once / reference-order arithmetic grow through the nonlinear dynamics); for the
+    Orszag-Tang run <= OT_NSTEP_TOL: there the reference's own arithmetic, started from a
+    state moved by one ulp per value, ends 5e-10 to 4e-9 away after 100 steps at 128^2
+    (tests/test_oracle_conditioning.py), so no rounding model can be held tighter;
   * dt: relative difference <= 1e-12.
 Plus properties that hold for the fast path on its own: y-invariance of Sod, exact
 conservation of the face-once update on periodic grids (to rounding), graph == plain."""
@@ -19,6 +22,7 @@ pytestmark = pytest.mark.gpu
 
 PER_STEP_TOL = 1e-12
 NSTEP_TOL = 1e-9
+OT_NSTEP_TOL = 1e-8
 
 def hll(case):
     cfg, s, u, b = case
@@ -139,7 +143,7 @@ def test_fast_orszag_tang_nsteps(cuda, oracle_lib):
     so, uo, bo, T_do, TT = oracle_run(oracle_lib, cfg, s, u, b, 100)
     sg, ug, bg, st = gpu_run(cfg, s, u, b, 100)
     err = max_rel_l1(cfg, (sg, ug, bg), (so, uo, bo))
-    assert err <= NSTEP_TOL, err
+    assert err <= OT_NSTEP_TOL, err
     assert abs(st.t - TT) <= 1e-10 * TT
     assert st.nonfinite == 0
 
