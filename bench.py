@@ -293,7 +293,10 @@ def measure_batched(g, torch, steps, ngrids=512):
            "total_cells": cells, "steps": steps,
            "tile": f"{info.tile_x}x{info.tile_y}", "ctas": info.ctas, "tiles": info.tiles,
            "autotune_ms_per_step": {f"{tx}x{ty}": round(info.tuned_ms[v], 4) for v, (tx, ty) in
-                                    enumerate(((32, 16), (32, 8), (16, 16), (64, 8)))}}
+                                    enumerate(((16, 16), (32, 8), (32, 16), (64, 8)))},
+           # cells of the tiles that lie outside their grids: tiles are the persistent
+           # launch's work items, and a partly filled tile keeps its warps' FP64 issue
+           "tile_fill": cells / (info.tiles * info.tile_x * info.tile_y)}
     for name, sched, graph in (("persistent_graph", g.BATCH_PERSISTENT, True),
                                ("looped_plain", g.BATCH_LOOPED, False),
                                ("looped_sync", g.BATCH_LOOPED_SYNC, False)):
@@ -878,8 +881,9 @@ def measure_hancock(g, torch, steps=20, parity_steps=3, warmup=3, N=3226, M=1792
     return out
 
 
-def cpu_baseline(workload, cfg, s, u, b, nsteps=2, threads=None):
-    """The oracle on all host cores, `nsteps` full steps of the workload."""
+def cpu_baseline(workload, cfg, s, u, b, nsteps=24, threads=None):
+    """The oracle on all host cores, `nsteps` full steps of the workload (about 10 s of CPU
+    work for Kelvin-Helmholtz 4096^2 on 16 cores)."""
     import oracle
     oracle.build(ref=False)
     o = oracle.Oracle()
