@@ -178,6 +178,16 @@ __device__ __forceinline__ void load_cell(const Params& P, const DualIn& in, int
 __device__ __forceinline__ void store_cell(const Planes& out, long long k, int f, double x) {
     store_f(out, f, k, x);
 }
+__device__ __forceinline__ void store_cell2(const Planes& out, long long k, int f0, double a,
+                                            double b) {
+    store_pair(out, f0, k, a, b);
+}
+__device__ __forceinline__ void store_cell(const DualOut& out, long long k, int f, Dual x);
+__device__ __forceinline__ void store_cell2(const DualOut& out, long long k, int f0, Dual a,
+                                            Dual b) {
+    store_cell(out, k, f0, a);
+    store_cell(out, k, f0 + 1, b);
+}
 __device__ __forceinline__ void store_cell(const DualOut& out, long long k, int f, Dual x) {
     out.v.f[f][k] = x.v;
     out.d.f[f][k] = x.d;
@@ -358,8 +368,8 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         const long long k = (long long)gy * N + gx;
         if (P.frozen && !cell_active(P, gx, gy)) {  // the faces' own test
             if (!dt_only) {
-                store_cell(out, k, 0, r); store_cell(out, k, 1, p);
-                store_cell(out, k, 2, u); store_cell(out, k, 3, v);
+                store_cell2(out, k, 0, r, p);
+                store_cell2(out, k, 2, u, v);
             }
             continue;
         }
@@ -394,10 +404,8 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         T p2 = fma(P.hgm1, K1 - K2, fma(-P.gm1, d[1], p));
         if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
         if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2)) ++nbad;
-        store_cell(out, k, 0, r2);
-        store_cell(out, k, 1, p2);
-        store_cell(out, k, 2, u2);
-        store_cell(out, k, 3, v2);
+        store_cell2(out, k, 0, r2, p2);
+        store_cell2(out, k, 2, u2, v2);
     }
     res.umax_x = umax_x;
     res.umax_y = umax_y;

@@ -77,6 +77,16 @@ __device__ __forceinline__ void load_state(const Params& P, const DualCPlanes& i
 __device__ __forceinline__ void store_state(const Planes& out, long long k, int f, double x) {
     store_f(out, f, k, x);
 }
+__device__ __forceinline__ void store_state2(const Planes& out, long long k, int f0, double a,
+                                             double b) {
+    store_pair(out, f0, k, a, b);
+}
+__device__ __forceinline__ void store_state(const DualPlanes& out, long long k, int f, Dual x);
+__device__ __forceinline__ void store_state2(const DualPlanes& out, long long k, int f0, Dual a,
+                                             Dual b) {
+    store_state(out, k, f0, a);
+    store_state(out, k, f0 + 1, b);
+}
 __device__ __forceinline__ void store_state(const DualPlanes& out, long long k, int f, Dual x) {
     out.v.f[f][k] = x.v;
     out.d.f[f][k] = x.d;
@@ -347,10 +357,8 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2) ||
             !finite_bits(bx2) || !finite_bits(by2) || !finite_bits(bz2))
             ++nbad;
-        store_state(out, k, 0, r2);
-        store_state(out, k, 1, p2);
-        store_state(out, k, 2, u2);
-        store_state(out, k, 3, v2);
+        store_state2(out, k, 0, r2, p2);
+        store_state2(out, k, 2, u2, v2);
         store_state(out, k, 4, bx2 * kSpi4);
         store_state(out, k, 5, by2 * kSpi4);
         store_state(out, k, 6, bz2 * kSpi4);

@@ -71,6 +71,50 @@ __device__ __forceinline__ void store_f(const Planes& p, int f, long long k, dou
         else p.b[3 * k + (f - 4)] = x;
     }
 }
+// The AoS pairs {rho, p} and {vx, vy} move as single 16-byte accesses where the array is
+// 16-byte aligned (a double2 array always is; the test is the same for every thread).
+__device__ __forceinline__ bool aligned16(const void* p) {
+    return ((unsigned long long)p & 15ULL) == 0;
+}
+// fields f0 and f0 + 1 (f0 = 0: rho, p; f0 = 2: vx, vy) of cell k
+__device__ __forceinline__ void store_pair(const Planes& p, int f0, long long k, double a,
+                                           double b) {
+    if (p.f[0] != nullptr) {
+        p.f[f0][k] = a;
+        p.f[f0 + 1][k] = b;
+    }
+    if (p.s != nullptr) {
+        double* d = f0 == 0 ? p.s : p.u;
+        if (aligned16(d)) {
+            reinterpret_cast<double2*>(d)[k] = make_double2(a, b);
+        } else {
+            d[2 * k] = a;
+            d[2 * k + 1] = b;
+        }
+    }
+}
+// the NF fields of cell k
+template <int NF>
+__device__ __forceinline__ void load_cell_fields(const CPlanes& in, long long k, double* v) {
+    if (in.s == nullptr) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[f] = in.f[f][k];
+        return;
+    }
+    if (aligned16(in.s) && aligned16(in.u)) {
+        const double2 a = reinterpret_cast<const double2*>(in.s)[k];
+        const double2 c = reinterpret_cast<const double2*>(in.u)[k];
+        v[0] = a.x; v[1] = a.y; v[2] = c.x; v[3] = c.y;
+    } else {
+        v[0] = in.s[2 * k]; v[1] = in.s[2 * k + 1];
+        v[2] = in.u[2 * k]; v[3] = in.u[2 * k + 1];
+    }
+    if (NF > 4) {
+        v[4] = in.b[3 * k];
+        v[5] = in.b[3 * k + 1];
+        v[6] = in.b[3 * k + 2];
+    }
+}
 
 struct Scalars;
 
@@ -414,8 +458,7 @@ __device__ __forceinline__ void fetch_cell(const Params& P, const CPlanes& in, i
         sy = ghost_source(gy, P.M, bc);
     }
     const long long k = (long long)sy * P.N + sx;
-#pragma unroll
-    for (int f = 0; f < NF; ++f) v[f] = load_f(in, f, k);
+    load_cell_fields<NF>(in, k, v);
     if (bc >= 0) ghost_transform<NF>(v, bc, P.ambient_p);
 }
 
