@@ -466,6 +466,27 @@ def adjoint_step_case(g, torch, N=512):
     return 0 if ok else 1
 
 
+def batch_step_case(g, torch, ngrids=512):
+    """The batched workload for kernel profiles: the 512 grids imported, a dt pass, then four
+    persistent steps (16 x 16 tiles, no autotuning), so the fifth euler_batch_kernel launch
+    is a plain step."""
+    from golikov_2d_gb300 import problems
+    grids = problems.batch_four_quadrant(ngrids)
+    b = g.Batch([c for c, *_ in grids])
+    for k, (c, s, u, _) in enumerate(grids):
+        b.import_grid(k, s, u)
+    b.set_time(0.0, 0.0)
+    b.init_dt()
+    b.advance(4, schedule=g.BATCH_PERSISTENT, use_graph=False)
+    torch.cuda.synchronize()
+    info = b.info()
+    bad = sum(b.stats(k, allow_nonfinite=True).nonfinite for k in range(ngrids))
+    b.close()
+    print(json.dumps({"case": "batch-step", "tiles": info.tiles, "nonfinite_cells": bad}),
+          flush=True)
+    return 0 if bad == 0 else 1
+
+
 def adjoint_step_euler_case(g, torch, N=512):
     """The Euler counterpart for kernel profiles: Kelvin-Helmholtz N x N, 20 plain steps, a
     10-step recording, one backward sweep and one tangent sweep."""
@@ -1201,9 +1222,11 @@ def main():
     ap.add_argument("--io", type=int, default=1)
     ap.add_argument("--hancock", type=int, default=1)
     ap.add_argument("--case", default="bench",
-                    choices=["bench", "adjoint-step", "adjoint-step-euler", "io", "hancock"],
+                    choices=["bench", "adjoint-step", "adjoint-step-euler", "io", "hancock",
+                             "batch-step"],
                     help="adjoint-step (-euler): a short differentiation run of the MHD (Euler) "
-                         "step for kernel profiles; "
+                         "step for kernel profiles; batch-step: the batched workload's "
+                         "persistent steps for kernel profiles; "
                          "io: the state-file measurement alone; hancock: the MUSCL-Hancock "
                          "measurement alone")
     args = ap.parse_args()
@@ -1215,6 +1238,12 @@ def main():
         import torch
         import golikov_2d_gb300 as g
         return adjoint_step_case(g, torch)
+    if args.case == "batch-step":
+        import torch
+        import golikov_2d_gb300 as g
+        from golikov_2d_gb300 import _build
+        _build.build()
+        return batch_step_case(g, torch)
     if args.case == "adjoint-step-euler":
         import torch
         import golikov_2d_gb300 as g
