@@ -47,6 +47,7 @@ EXPORTS = (
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
     "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
     "gd_probe_fp64_peak", "gd_probe_faces", "gd_step_ref_static", "gd_alloc_counts",
+    "gd_check_int_mul",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
@@ -144,6 +145,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_probe_faces.argtypes = [i, i, d, i, ll, vp, vp, vp, vp, vp]
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
     L.gd_alloc_counts.argtypes = [ctypes.POINTER(ll), ctypes.POINTER(ll)]
+    L.gd_check_int_mul.argtypes = [ll, ctypes.c_ulonglong, ctypes.POINTER(ll)]
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
@@ -174,7 +176,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_import", "gd_export", "gd_set_time", "gd_init_dt", "gd_advance",
                  "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_probe_faces",
-                 "gd_step_ref_static", "gd_alloc_counts",
+                 "gd_step_ref_static", "gd_alloc_counts", "gd_check_int_mul",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
@@ -522,6 +524,16 @@ def probe_fp64_peak() -> float:
     v = ctypes.c_double()
     _check(L.gd_probe_fp64_peak(ctypes.byref(v)), "gd_probe_fp64_peak")
     return v.value
+
+
+def check_int_mul(pairs: int = 1 << 24, seed: int = 1) -> dict:
+    """Device check of the step kernels' integer-pipe binary64 multiplication against the
+    FP64 unit's multiply (gd_check_int_mul): mismatched results (NaN results excepted), NaN
+    payload differences, pairs outside the integer fast path, pairs checked."""
+    L = load()
+    c = (ctypes.c_longlong * 4)()
+    _check(L.gd_check_int_mul(int(pairs), int(seed), c), "gd_check_int_mul")
+    return {"mismatches": c[0], "nan_payload": c[1], "slow_path": c[2], "checked": c[3]}
 
 
 def alloc_counts() -> tuple[int, int]:

@@ -106,6 +106,7 @@ Params make_params(const gd_config& c) {
     P.inv_dy = 1.0 / c.dy;
     P.inv_gm1 = 1.0 / (c.gamma - 1.0);
     P.hgm1 = 0.5 * (c.gamma - 1.0);
+    P.g_gm1 = c.gamma / (c.gamma - 1.0);
     P.ambient_p = 1.0 / c.gamma;
     // rad passed to the flux: dy on x-faces in the Euler kernels (kernel.cu:1811, 3562),
     // dx on x-faces in the MHD kernels (kernel.cu:2560)
@@ -532,6 +533,12 @@ gd_status gd_probe_fp64_peak(double* flops_out) {
     return GD_OK;
 }
 
+gd_status gd_check_int_mul(long long pairs, unsigned long long seed, long long* counts_out) {
+    if (!counts_out || pairs <= 0 || pairs > (1LL << 34)) return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::check_imul(pairs, seed, counts_out));
+    return GD_OK;
+}
+
 gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long long n,
                          const double* L, const double* R, double* flux, double* speed,
                          gd_stream stream) {
@@ -550,6 +557,7 @@ gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long l
     P.gm1 = gamma - 1.0;
     P.inv_gm1 = 1.0 / (gamma - 1.0);
     P.hgm1 = 0.5 * (gamma - 1.0);
+    P.g_gm1 = gamma / (gamma - 1.0);
     const cudaStream_t st = (cudaStream_t)stream;
     GD_CUDA(physics == GD_EULER ? gd::launch_euler_face_probe(P, n, axis, L, R, flux, speed, st)
                                 : gd::launch_mhd_face_probe(P, n, axis, L, R, flux, speed, st));

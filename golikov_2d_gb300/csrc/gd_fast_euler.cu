@@ -49,26 +49,29 @@ struct FluxE {
 
 // HLLC flux in a local frame: un = normal velocity, ut = in-plane tangential velocity.
 // Returns the flux (mass, normal momentum, tangential momentum, energy) and, in UU, SL or
-// SR, the one of larger magnitude (signed; the dt reduction takes |UU|).  T is double, or Dual for the tangent (value and derivative, the branch
-// choices taken on the value).
+// SR, the one of larger magnitude (signed; the dt reduction takes |UU|).  T is double, or
+// Dual for the tangent (value and derivative, the branch choices taken on the value).
+// Products go through mulx (on the integer pipes for double), sums and fused
+// multiply-adds through the FP64 unit.
 template <class T>
 __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
                                                T utR, const Params& P, T& UU) {
     const double g = P.gamma;
-    const T gpL = g * pL, gpR = g * pR;
-    const T cL = sqrt_over(gpL, rL);  // sqrt(g p / rho)
-    const T cR = sqrt_over(gpR, rR);
+    const T cL = sqrt_over_im(mulx(g, pL), rL);  // sqrt(g p / rho)
+    const T cR = sqrt_over_im(mulx(g, pR), rR);
     const T aL = unL - cL, aR = unR - cR;
     const T bL = unL + cL, bR = unR + cR;
     const T SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
     const T SR = dmax(bL, bR);
     const T suL = SL - unL, suR = SR - unR;
-    const T mL = rL * suL, mR = rR * suR;
-    const T SM = (fma(mR, unR, -mL * unL) + (pL - pR)) * rcp_fast(mR - mL);
+    const T mL = mulx(rL, suL), mR = mulx(rR, suR);
+    // S_M = Nm / D (kernel.cu:1001-1003): its sign is the sign of Nm times that of D
+    const T Nm = fma(mR, unR, fma(-mL, unL, pL - pR));
+    const T D = mR - mL;
     UU = max_nonneg(SL, SR);  // signed: the block reduction takes the magnitude
 
     // Side whose state (or star state) gives the flux at x/t = 0 (kernel.cu:1119-1158).
-    const bool takeL = gt_zero(SL) || ge_zero(SM);
+    const bool takeL = gt_zero(SL) || !quotient_neg(Nm, D);
     const T r = takeL ? rL : rR;
     const T p = takeL ? pL : pR;
     const T un = takeL ? unL : unR;
@@ -78,24 +81,34 @@ __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T
     const T mm = takeL ? mL : mR;
     const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
 
-    const T E = fma(p, P.inv_gm1, 0.5 * r * fma(un, un, ut * ut));
+    const T V2 = fma(un, un, mulx(ut, ut));
     FluxE<T> F;
     if (star) {
         // F_K + S_K (U*_K - U_K) is the physical flux of the star state, F(U*_K) with the
         // star pressure: the jump conditions across S_K are what define rho*, p* and E*
-        // (kernel.cu:1119-1158).  With q = S_M / (S_K - S_M):
-        //   rho* S_M = mm q,  mom: rho* S_M^2 + p*,  (E* + p*) S_M = q (E su - p u + p* S_K)
-        const T q = SM * rcp_fast(S - SM);
-        const T pst = fma(mm, SM - un, p);  // p* = p_K + rho_K (S_K - u_K) (S_M - u_K)
-        F.m = mm * q;
+        // (kernel.cu:1119-1158).  With q = S_M / (S_K - S_M), p* = p + rho su (S_M - un),
+        // su = S_K - un and G = gamma / (gamma - 1):
+        //   mass rho* S_M = rho su q,  momentum rho* S_M^2 + p*,  tangential rho* S_M ut,
+        //   energy (E* + p*) S_M = q su (p G + rho (|v|^2 / 2 + S_K (S_M - un))).
+        // S_M and q from one reciprocal: with X = S_K D - Nm = D (S_K - S_M),
+        //   S_M = Nm X / (D X),  q = Nm D / (D X).
+        const T X = fma(S, D, -Nm);
+        const T R = rcp_fast(mulx(D, X));
+        const T NR = mulx(Nm, R);
+        const T SM = mulx(NR, X);
+        const T q = mulx(NR, D);
+        const T SMu = SM - un;
+        const T pst = fma(mm, SMu, p);
+        const T qs = mulx(q, su);
+        F.m = mulx(r, qs);
         F.mn = fma(F.m, SM, pst);
-        F.mt = F.m * ut;
-        F.e = fma(E, su, fma(-p, un, pst * S)) * q;
+        F.mt = mulx(F.m, ut);
+        F.e = mulx(qs, fma(p, P.g_gm1, mulx(r, fma(0.5, V2, mulx(S, SMu)))));
     } else {
-        F.m = r * un;
+        F.m = mulx(r, un);
         F.mn = fma(F.m, un, p);
-        F.mt = F.m * ut;
-        F.e = (E + p) * un;
+        F.mt = mulx(F.m, ut);
+        F.e = mulx(un, fma(p, P.g_gm1, mulx(mulx(0.5, r), V2)));  // (E + p) un
     }
     return F;
 }
@@ -382,7 +395,7 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         for (int f = 0; f < NF; ++f) {
             const T* a = fxc + f * TY * (TX + 1);
             const T* b = fyc + f * (TY + 1) * TX;
-            d[f] = fma(kx, a[1] - a[0], ky * (b[TX] - b[0]));
+            d[f] = fma(kx, a[1] - a[0], mulx(ky, b[TX] - b[0]));
         }
         if constexpr (std::is_same<T, double>::value) {
             if (aux != nullptr) {  // the recording of the adjoint: the flux differences used
@@ -395,12 +408,12 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         if (le_zero(r2)) { r2 = cst<T>(0.0001); ++nfl_r; }
         const T inv = rcp_fast(r2);
         const T mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
-        const T u2 = mx2 * inv;
-        const T v2 = my2 * inv;
+        const T u2 = mulx(mx2, inv);
+        const T v2 = mulx(my2, inv);
         // p' = (gamma - 1) (E - d_E - K'/2) with E = p / (gamma - 1) + K / 2, K = rho |v|^2,
         // K' = rho' |v'|^2 = m' . v' (kernel.cu:1861-1870)
-        const T K1 = r * fma(u, u, v * v);
-        const T K2 = fma(mx2, u2, my2 * v2);
+        const T K1 = r * fma(u, u, mulx(v, v));
+        const T K2 = fma(mx2, u2, mulx(my2, v2));
         T p2 = fma(P.hgm1, K1 - K2, fma(-P.gm1, d[1], p));
         if (le_zero(p2)) { p2 = cst<T>(0.000001); ++nfl_p; }
         if (!finite_bits(r2) || !finite_bits(p2) || !finite_bits(u2) || !finite_bits(v2)) ++nbad;

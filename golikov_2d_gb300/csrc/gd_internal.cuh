@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gd2d.h"
+#include "gd_swfp.cuh"
 
 namespace gd {
 
@@ -39,6 +40,7 @@ struct Params {
     unsigned int tile_nblocks;
     // derived
     double gm1, inv_gm1, hgm1;  // gamma - 1, 1 / (gamma - 1), (gamma - 1) / 2
+    double g_gm1;               // gamma / (gamma - 1)
     double inv_dx, inv_dy;  // 1/dx, 1/dy: the fast kernels scale fluxes by T_do * inv_dx
     double ambient_p;   // 1/gamma
     double krad_x;      // krit * rad used for faces with an x normal
@@ -253,6 +255,20 @@ __device__ __forceinline__ bool lt_zero(double x) {
     return (unsigned long long)bits(x) > 0x8000000000000000ULL;
 }
 __device__ __forceinline__ bool ge_zero(double x) { return !lt_zero(x); }
+// n / d < 0 strictly, from the bit patterns (inline PTX, see mag): the signs differ and n is
+// not +-0
+__device__ __forceinline__ bool quotient_neg(double n, double d) {
+    unsigned int r;
+    asm("{\n\t.reg .b64 x, m;\n\t.reg .pred p;\n\t"
+        "xor.b64 x, %1, %2;\n\t"
+        "shl.b64 m, %1, 1;\n\t"
+        "setp.lt.s64 p, x, 0;\n\t"
+        "setp.ne.and.u64 p, m, 0, p;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t"
+        "}"
+        : "=r"(r) : "l"(bits(n)), "l"(bits(d)));
+    return r != 0;
+}
 
 // ---------------------------------------------------------------------------------------
 // FP64 reciprocal and reciprocal square root for the fast path.
@@ -394,6 +410,33 @@ __device__ __forceinline__ double sqrt_over(double a, double r) {
     double c, rs;
     sqrt_over_rs(a, r, c, rs);
     return c;
+}
+
+// a * b formed on the integer pipes (swfp::mul_rn: the bits of the FP64 multiply, NaN
+// payloads aside), leaving the FP64 unit to the kernel's other operations
+__device__ __forceinline__ double imul(double a, double b) { return swfp::mul_rn(a, b); }
+__device__ __forceinline__ double mulx(double a, double b) { return imul(a, b); }
+
+// sqrt_fast with its products on the integer pipes
+__device__ __forceinline__ double sqrt_fast_im(double x) {
+    if (!rsqrt_ok(x)) return sqrt(x);
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double w = imul(x, y);
+    const double e = fma(-w, y, 1.0);
+    return fma(w, imul(e, fma(0.375, e, 0.5)), w);
+}
+// sqrt_over with its three products on the integer pipes
+__device__ __forceinline__ double sqrt_over_im(double a, double r) {
+    if (!(in_half_range_pos(a) && in_half_range_pos(r))) return a * rsqrt_times(a, r);
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
+    const double y = widen_f32(f);
+    const double w = imul(a, y);
+    const double e = fma(-w, imul(r, y), 1.0);
+    const double et = imul(e, fma(0.375, e, 0.5));
+    return fma(w, et, w);
 }
 
 // isfinite(x) on the integer pipe: the exponent field is not all ones

@@ -1,5 +1,5 @@
-// gd_util.cu -- layout conversion, the funk_time rotation, scalar setup and the FP64
-// throughput probe.
+// gd_util.cu -- layout conversion, the funk_time rotation, scalar setup, the FP64
+// throughput probe and the check of the integer-pipe multiplication.
 #include "gd_internal.cuh"
 #include "gd_kernels.h"
 
@@ -187,6 +187,85 @@ cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st) {
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st) {
     reset_T_kernel<<<1, 1, 0, st>>>(sc);
     return cudaGetLastError();
+}
+
+namespace {
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {  // splitmix64
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+// imul against the FP64 unit's multiply on n seeded operand pairs per thread, in four
+// classes: any bit pattern; exponents near 1; a subnormal operand; products near the
+// overflow and underflow limits.  counts: mismatches, NaN-payload differences, pairs outside
+// the integer fast path, pairs checked.
+__global__ void check_imul_kernel(unsigned long long* counts, unsigned long long seed, int n) {
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    unsigned long long bad = 0, nanpay = 0, slow = 0;
+    for (int i = 0; i < n; ++i) {
+        const unsigned long long r1 = mix64(seed + 3 * (t * n + i)), r2 = mix64(r1 + 1),
+                                 r3 = mix64(r2 + 2);
+        unsigned long long A = r1, B = r2;
+        const unsigned long long keep = 0x800fffffffffffffULL;
+        switch ((int)(r3 & 3)) {
+            case 1:
+                A = (A & keep) | ((1003 + (r3 >> 8) % 40) << 52);
+                B = (B & keep) | ((1003 + (r3 >> 20) % 40) << 52);
+                break;
+            case 2:
+                A = (A & keep) >> (r3 >> 58);
+                break;
+            case 3: {
+                const unsigned long long ea = 1 + (r3 >> 8) % 2046;
+                const unsigned long long eb = ((r3 >> 40) & 1) ? 3067 - ea + (r3 >> 48) % 9 - 4
+                                                               : 1024 - ea + (r3 >> 48) % 61 - 30;
+                A = (A & keep) | (ea << 52);
+                B = (B & keep) | ((eb & 0x7ff) << 52);
+                break;
+            }
+            default:
+                break;
+        }
+        const double a = from_bits((long long)A), b = from_bits((long long)B);
+        bool ok;
+        (void)swfp::dmul_fast(a, b, ok);
+        slow += !ok;
+        const double s = imul(a, b);
+        double h;
+        asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(h) : "d"(a), "d"(b));
+        if (bits(s) != bits(h)) {
+            if (isnan(s) && isnan(h)) ++nanpay;
+            else ++bad;
+        }
+    }
+    atomicAdd(counts + 0, bad);
+    atomicAdd(counts + 1, nanpay);
+    atomicAdd(counts + 2, slow);
+    atomicAdd(counts + 3, (unsigned long long)n);
+}
+}  // namespace
+
+cudaError_t check_imul(long long pairs, unsigned long long seed, long long* out) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 4, threads = 256;
+    const long long per = (pairs + (long long)blocks * threads - 1) / ((long long)blocks * threads);
+    unsigned long long* counts = nullptr;
+    e = gd::dev_alloc(&counts, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(counts, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        check_imul_kernel<<<blocks, threads>>>(counts, seed, (int)(per < 1 ? 1 : per));
+        e = cudaGetLastError();
+    }
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, counts, sizeof h, cudaMemcpyDeviceToHost);
+    gd::dev_free(counts);
+    for (int i = 0; i < 4; ++i) out[i] = (long long)h[i];
+    return e;
 }
 
 cudaError_t probe_fp64_peak(double* flops) {

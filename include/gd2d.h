@@ -388,6 +388,14 @@ long long gd_launch_count(const gd_ctx* ctx);
  * DFMA loop on every SM; blocking, ~50 ms. */
 gd_status gd_probe_fp64_peak(double* flops_out);
 
+/* Diagnostic (no reference counterpart): checks, on the device, the step kernels' IEEE-754
+ * binary64 multiplication on the integer pipes against the FP64 unit's multiply on about
+ * `pairs` seeded operand pairs (any bit patterns, exponents near 1, subnormal operands,
+ * products near the overflow and underflow limits).  counts_out[0]: results whose bits
+ * differ (NaN results excepted), [1]: NaN results whose payloads differ, [2]: pairs outside
+ * the integer fast path, [3]: pairs checked.  Blocking. */
+gd_status gd_check_int_mul(long long pairs, unsigned long long seed, long long* counts_out);
+
 /* Diagnostic (no reference counterpart): how many device or pinned-host allocations
  * (cudaMalloc, cudaMallocHost) and releases (cudaFree, cudaFreeHost) this library has made
  * in this process, over all contexts and threads.  Every allocation of the library goes
