@@ -45,10 +45,10 @@ __global__ void __launch_bounds__(NT) eadj_update_kernel(Params P, CPlanes U, co
         if (rfl) r2 = 0.0001;
         const double inv = rcp_fast(r2);
         const double mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
-        const double u2 = mx2 * inv, v2 = my2 * inv;
-        const double w = fma(u, u, v * v);
+        const double u2 = imul(mx2, inv), v2 = imul(my2, inv);
+        const double w = fma(u, u, imul(v, v));
         const double K1 = r * w;
-        const double K2 = fma(mx2, u2, my2 * v2);
+        const double K2 = fma(mx2, u2, imul(my2, v2));
         const double p2 = fma(P.hgm1, K1 - K2, fma(-P.gm1, d[1], p));
         const bool pfl = le_zero(p2);
         // reverse; a floored value is a constant
@@ -97,91 +97,101 @@ __global__ void __launch_bounds__(NT) eadj_update_kernel(Params P, CPlanes U, co
 // ---------------------------------------------------------------------------------------
 // Reverse sweep of one HLLC face flux in the local frame.  Inputs: the face states a (low)
 // and b (high) as (r, p, un, ut) and the flux adjoint (m, mn, mt, e).  Writes the adjoints of
-// a and b to ab, bb.  The forward part repeats hllc_local of gd_fast_euler.cu.
+// a and b to ab, bb.  The forward part repeats hllc_local of gd_fast_euler.cu operation for
+// operation (products on the integer pipes where it has them there: the same bits).
+//   Nm = mR unR - mL unL + pL - pR, D = mR - mL, m = rho (S - un); K the side that gives
+//   the flux.  Star: X = S D - Nm, R = 1 / (D X), S_M = Nm R X (= Nm / D), q = Nm R D
+//   (= Nm / X), F.m = r qs with qs = q su, F.mn = F.m S_M + p*, p* = mm (S_M - un) + p,
+//   F.mt = F.m ut, F.e = qs (p G + r (|v|^2 / 2 + S (S_M - un))).  Otherwise F.m = r un,
+//   F.mn = F.m un + p, F.mt = F.m ut, F.e = un (p G + r |v|^2 / 2).  G = gamma / (gamma - 1).
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const double* Fb,
                                          const Params& P, double* ab, double* bb) {
-    const double g = P.gamma;
+    const double g = P.gamma, G = P.g_gm1;
     const double rL = a[0], pL = a[1], unL = a[2], utL = a[3];
     const double rR = b[0], pR = b[1], unR = b[2], utR = b[3];
     // ---- forward
-    const double gpL = g * pL, gpR = g * pR;
+    const double gpL = imul(g, pL), gpR = imul(g, pR);
     double cL, cR, rsL, rsR;  // sqrt_over(g p, rho) of the forward and 1/sqrt(g p rho)
-    sqrt_over_rs(gpL, rL, cL, rsL);
-    sqrt_over_rs(gpR, rR, cR, rsR);
+    sqrt_over_rs_im(gpL, rL, cL, rsL);
+    sqrt_over_rs_im(gpR, rR, cR, rsR);
     const double aL = unL - cL, aR = unR - cR;
     const double bL = unL + cL, bR = unR + cR;
     const bool slR = dlt(aR, aL);  // SL = dmin(aL, aR)
     const bool srR = dlt(bL, bR);  // SR = dmax(bL, bR)
     const double SL = slR ? aR : aL, SR = srR ? bR : bL;
     const double suL = SL - unL, suR = SR - unR;
-    const double mL = rL * suL, mR = rR * suR;
-    const double SMn = fma(mR, unR, -mL * unL) + (pL - pR);
-    const double iden = rcp_fast(mR - mL);
-    const double SM = SMn * iden;
-    const bool takeL = gt_zero(SL) || ge_zero(SM);
+    const double mL = imul(rL, suL), mR = imul(rR, suR);
+    const double Nm = fma(mR, unR, fma(-mL, unL, pL - pR));
+    const double D = mR - mL;
+    const bool takeL = gt_zero(SL) || !quotient_neg(Nm, D);
     const double r = takeL ? rL : rR, p = takeL ? pL : pR;
     const double un = takeL ? unL : unR, ut = takeL ? utL : utR;
     const double S = takeL ? SL : SR, su = takeL ? suL : suR, mm = takeL ? mL : mR;
     const bool star = takeL ? !gt_zero(SL) : ge_zero(SR);
-    const double w = fma(un, un, ut * ut);
-    const double E = fma(p, P.inv_gm1, 0.5 * r * w);
-    // ---- reverse.  Star: F.m = mm q, F.mn = F.m SM + pst, F.mt = F.m ut,
-    // F.e = X q with q = SM / (S - SM), pst = mm (SM - un) + p, X = E su - p un + pst S.
-    // Otherwise F.m = r un, F.mn = F.m un + p, F.mt = F.m ut, F.e = (E + p) un.
+    const double V2 = fma(un, un, imul(ut, ut));
+    // ---- reverse
     const double Fmb = Fb[0], Fmnb = Fb[1], Fmtb = Fb[2], Feb = Fb[3];
-    double rb = 0.0, pb = 0.0, unb = 0.0, utb = 0.0, Sb = 0.0, sub = 0.0, mmb = 0.0;
-    double SMb = 0.0, Eb = 0.0;
+    double rb, pb, unb, utb, V2b, Sb = 0.0, sub = 0.0, mmb = 0.0, Nmb = 0.0, Db = 0.0;
     if (star) {
-        const double inv = rcp_fast(S - SM);
-        const double q = SM * inv;
-        const double pst = fma(mm, SM - un, p);
-        const double Fm = mm * q;
-        const double X = fma(E, su, fma(-p, un, pst * S));
-        double qb = Feb * X;
-        const double Xb = Feb * q;
-        const double Fmbt = fma(Fmnb, SM, fma(Fmtb, ut, Fmb));  // all of F.m's adjoint
-        utb += Fmtb * Fm;
-        SMb += Fmnb * Fm;
-        double pstb = Fmnb;
-        // X = E su - p un + pst S
-        Eb += Xb * su;
-        sub += Xb * E;
-        pb -= Xb * un;
-        unb -= Xb * p;
-        pstb += Xb * S;
-        Sb += Xb * pst;
-        // F.m = mm q
-        mmb += Fmbt * q;
-        qb += Fmbt * mm;
-        // pst = mm (SM - un) + p
-        mmb += pstb * (SM - un);
-        SMb += pstb * mm;
-        unb -= pstb * mm;
-        pb += pstb;
-        // q = SM inv, inv = 1 / (S - SM)
-        SMb += qb * inv;
-        const double t = -(qb * SM) * inv * inv;
-        Sb += t;
-        SMb -= t;
-    } else {
-        const double Fm0 = r * un;
-        Eb += Feb * un;
-        pb += Feb * un;
-        unb += Feb * (E + p);
-        const double Fm0b = fma(Fmnb, un, fma(Fmtb, ut, Fmb));
-        utb += Fmtb * Fm0;
-        unb += Fmnb * Fm0;
+        const double X = fma(S, D, -Nm);
+        const double R = rcp_fast(imul(D, X));
+        const double NR = imul(Nm, R);
+        const double SM = imul(NR, X);
+        const double q = imul(NR, D);
+        const double SMu = SM - un;
+        const double qs = imul(q, su);
+        const double Fm = imul(r, qs);
+        const double t2 = fma(0.5, V2, imul(S, SMu));
+        const double inner = fma(p, G, imul(r, t2));
+        // F.e = qs inner, inner = p G + r t2, t2 = V2 / 2 + S SMu
+        double qsb = imul(Feb, inner);
+        const double innerb = imul(Feb, qs);
+        pb = imul(innerb, G);
+        rb = imul(innerb, t2);
+        const double t2b = imul(innerb, r);
+        V2b = imul(0.5, t2b);
+        Sb = imul(t2b, SMu);
+        double SMub = imul(t2b, S);
+        // F.m = r qs, with all of F.m's adjoint (F.mn = F.m SM + p*, F.mt = F.m ut)
+        const double Fmbt = fma(Fmnb, SM, fma(Fmtb, ut, Fmb));
+        rb = fma(Fmbt, qs, rb);
+        qsb = fma(Fmbt, r, qsb);
+        utb = imul(Fmtb, Fm);
+        double SMb = imul(Fmnb, Fm);
+        // qs = q su
+        const double qb = imul(qsb, su);
+        sub = imul(qsb, q);
+        // p* = mm SMu + p (its adjoint is Fmnb)
+        mmb = imul(Fmnb, SMu);
+        SMub = fma(Fmnb, mm, SMub);
         pb += Fmnb;
-        // Fm0 = r un
-        rb += Fm0b * un;
-        unb += Fm0b * r;
+        // SMu = SM - un
+        SMb += SMub;
+        unb = -SMub;
+        // q = Nm / X, SM = Nm / D, X = S D - Nm, with 1 / X = D R and 1 / D = X R
+        const double DR = imul(D, R), XR = imul(X, R);
+        const double Xb = -imul(imul(qb, q), DR);
+        Nmb = fma(qb, DR, imul(SMb, XR)) - Xb;
+        Db = fma(Xb, S, -imul(imul(SMb, SM), XR));
+        Sb = fma(Xb, D, Sb);
+    } else {
+        // F.e = un H, H = p G + hr V2 with hr = r / 2
+        const double hr = imul(0.5, r);
+        const double H = fma(p, G, imul(hr, V2));
+        const double Fm = imul(r, un);
+        const double Hb = imul(Feb, un);
+        const double Fm0b = fma(Fmnb, un, fma(Fmtb, ut, Fmb));  // all of F.m's adjoint
+        unb = fma(Feb, H, fma(Fm0b, r, imul(Fmnb, Fm)));
+        pb = fma(Hb, G, Fmnb);
+        rb = fma(imul(0.5, Hb), V2, imul(Fm0b, un));
+        V2b = imul(Hb, hr);
+        utb = imul(Fmtb, Fm);
     }
-    // E = p / (gamma - 1) + 0.5 r (un^2 + ut^2)
-    pb += Eb * P.inv_gm1;
-    rb += 0.5 * Eb * w;
-    unb += Eb * r * un;
-    utb += Eb * r * ut;
+    // V2 = un^2 + ut^2
+    const double V2b2 = V2b + V2b;
+    unb = fma(V2b2, un, unb);
+    utb = fma(V2b2, ut, utb);
     // the K side's adjoints to its side
     double rLb = 0, pLb = 0, unLb = 0, utLb = 0, rRb = 0, pRb = 0, unRb = 0, utRb = 0;
     double SLb = 0, SRb = 0, suLb = 0, suRb = 0, mLb = 0, mRb = 0;
@@ -190,24 +200,18 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     } else {
         rRb = rb; pRb = pb; unRb = unb; utRb = utb; SRb = Sb; suRb = sub; mRb = mmb;
     }
-    // SM = SMn iden, SMn = mR unR - mL unL + pL - pR, iden = 1 / (mR - mL)
-    const double SMnb = SMb * iden, idenb = SMb * SMn;
-    mRb += SMnb * unR;
-    unRb += SMnb * mR;
-    mLb -= SMnb * unL;
-    unLb -= SMnb * mL;
-    pLb += SMnb;
-    pRb -= SMnb;
-    {
-        const double t = -idenb * iden * iden;
-        mRb += t;
-        mLb -= t;
-    }
+    // Nm = mR unR - mL unL + pL - pR, D = mR - mL
+    mRb = fma(Nmb, unR, mRb + Db);
+    unRb = fma(Nmb, mR, unRb);
+    mLb = fma(-Nmb, unL, mLb - Db);
+    unLb = fma(-Nmb, mL, unLb);
+    pLb += Nmb;
+    pRb -= Nmb;
     // mL = rL suL, mR = rR suR; suL = SL - unL, suR = SR - unR
-    rLb += mLb * suL;
-    suLb += mLb * rL;
-    rRb += mRb * suR;
-    suRb += mRb * rR;
+    rLb = fma(mLb, suL, rLb);
+    suLb = fma(mLb, rL, suLb);
+    rRb = fma(mRb, suR, rRb);
+    suRb = fma(mRb, rR, suRb);
     SLb += suLb;
     unLb -= suLb;
     SRb += suRb;
@@ -218,12 +222,12 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     if (srR) { unRb += SRb; cRb += SRb; } else { unLb += SRb; cLb += SRb; }
     // c = sqrt(g p / r): d/d(g p) = 0.5 / sqrt(g p r), d/dr = -0.5 c / r (0 where p = 0)
     if ((bits(gpL) << 1) != 0) {
-        pLb += cLb * 0.5 * rsL * g;
-        rLb -= 0.5 * cLb * cL * rcp_fast(rL);
+        pLb = fma(imul(imul(0.5, cLb), rsL), g, pLb);
+        rLb -= imul(imul(imul(0.5, cLb), cL), rcp_fast(rL));
     }
     if ((bits(gpR) << 1) != 0) {
-        pRb += cRb * 0.5 * rsR * g;
-        rRb -= 0.5 * cRb * cR * rcp_fast(rR);
+        pRb = fma(imul(imul(0.5, cRb), rsR), g, pRb);
+        rRb -= imul(imul(imul(0.5, cRb), cR), rcp_fast(rR));
     }
     ab[0] = rLb; ab[1] = pLb; ab[2] = unLb; ab[3] = utLb;
     bb[0] = rRb; bb[1] = pRb; bb[2] = unRb; bb[3] = utRb;
@@ -254,9 +258,10 @@ __device__ __forceinline__ double slope_sel(double cm, double c, double cp, int&
     return s;
 }
 
-__global__ void __launch_bounds__(FBX * FBY) eadj_face_kernel(Params P, CPlanes U,
-                                                              double* scratch,
-                                                              const double* __restrict__ T_do_ptr) {
+// at most 128 registers a thread (four blocks per SM): uncapped, the integer products of the
+// sweep took 146 and three blocks, slower
+__global__ void __launch_bounds__(FBX * FBY, 4)
+    eadj_face_kernel(Params P, CPlanes U, double* scratch, const double* __restrict__ T_do_ptr) {
     const int N = P.N, M = P.M;
     const long long K = (long long)N * M;
     const bool isx = blockIdx.z == 0;

@@ -89,10 +89,15 @@ __device__ __forceinline__ bool ge_zero(Dual x) { return ge_zero(x.v); }
 __device__ __forceinline__ bool isfinite(Dual x) { return ::isfinite(x.v); }
 __device__ __forceinline__ bool finite_bits(Dual x) { return finite_bits(x.v); }
 __device__ __forceinline__ bool quotient_neg(Dual n, Dual d) { return quotient_neg(n.v, d.v); }
+template <bool OUTLINE = false>
 __device__ __forceinline__ Dual mulx(Dual a, Dual b) { return a * b; }
+template <bool OUTLINE = false>
 __device__ __forceinline__ Dual mulx(double a, Dual b) { return a * b; }
+template <bool OUTLINE = false>
 __device__ __forceinline__ Dual mulx(Dual a, double b) { return a * b; }
+template <bool OUTLINE = false>
 __device__ __forceinline__ Dual sqrt_over_im(Dual a, Dual r) { return sqrt_over(a, r); }
+template <bool OUTLINE = false>
 __device__ __forceinline__ Dual sqrt_fast_im(Dual x) { return sqrt_fast(x); }
 __device__ __forceinline__ Dual dabs(Dual x) { return lt_zero(x.v) ? -x : x; }
 __device__ __forceinline__ Dual dmin(Dual a, Dual b) { return dlt(b.v, a.v) ? b : a; }

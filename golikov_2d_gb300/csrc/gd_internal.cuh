@@ -406,6 +406,22 @@ __device__ __forceinline__ void sqrt_over_rs(double a, double r, double& c, doub
     c = fma(w, et, w);
     rs = fma(y, et, y);
 }
+// sqrt_over_rs with its products on the integer pipes: the same c as sqrt_over_im
+__device__ __forceinline__ void sqrt_over_rs_im(double a, double r, double& c, double& rs) {
+    if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
+        rs = rsqrt_times(a, r);
+        c = a * rs;
+        return;
+    }
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
+    const double y = widen_f32(f);
+    const double w = swfp::mul_rn(a, y);
+    const double e = fma(-w, swfp::mul_rn(r, y), 1.0);
+    const double et = swfp::mul_rn(e, fma(0.375, e, 0.5));
+    c = fma(w, et, w);
+    rs = fma(y, et, y);
+}
 __device__ __forceinline__ double sqrt_over(double a, double r) {
     double c, rs;
     sqrt_over_rs(a, r, c, rs);
@@ -414,28 +430,35 @@ __device__ __forceinline__ double sqrt_over(double a, double r) {
 
 // a * b formed on the integer pipes (swfp::mul_rn: the bits of the FP64 multiply, NaN
 // payloads aside), leaving the FP64 unit to the kernel's other operations
-__device__ __forceinline__ double imul(double a, double b) { return swfp::mul_rn(a, b); }
-__device__ __forceinline__ double mulx(double a, double b) { return imul(a, b); }
+// (OUTLINE: the general case out of line, see swfp::mul_rn)
+template <bool OUTLINE = false>
+__device__ __forceinline__ double imul(double a, double b) {
+    return swfp::mul_rn<OUTLINE>(a, b);
+}
+template <bool OUTLINE = false>
+__device__ __forceinline__ double mulx(double a, double b) { return imul<OUTLINE>(a, b); }
 
 // sqrt_fast with its products on the integer pipes
+template <bool OUTLINE = false>
 __device__ __forceinline__ double sqrt_fast_im(double x) {
     if (!rsqrt_ok(x)) return sqrt(x);
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
     const double y = widen_f32(r);
-    const double w = imul(x, y);
+    const double w = imul<OUTLINE>(x, y);
     const double e = fma(-w, y, 1.0);
-    return fma(w, imul(e, fma(0.375, e, 0.5)), w);
+    return fma(w, imul<OUTLINE>(e, fma(0.375, e, 0.5)), w);
 }
 // sqrt_over with its three products on the integer pipes
+template <bool OUTLINE = false>
 __device__ __forceinline__ double sqrt_over_im(double a, double r) {
     if (!(in_half_range_pos(a) && in_half_range_pos(r))) return a * rsqrt_times(a, r);
     float f;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
     const double y = widen_f32(f);
-    const double w = imul(a, y);
-    const double e = fma(-w, imul(r, y), 1.0);
-    const double et = imul(e, fma(0.375, e, 0.5));
+    const double w = imul<OUTLINE>(a, y);
+    const double e = fma(-w, imul<OUTLINE>(r, y), 1.0);
+    const double et = imul<OUTLINE>(e, fma(0.375, e, 0.5));
     return fma(w, et, w);
 }
 

@@ -28,9 +28,10 @@ struct FluxM {
     T m, mn, mt, e, bn, bt, bz;  // mass, normal / tangential momentum, energy, field
 };
 
-// The per-side products (side, side_flux) form on the integer pipes (mulx); the HLLD core
-// keeps its products on the FP64 unit: the MHD and Hancock tiles run two CTAs per SM, too few
-// warps to cover the integer product's latency on that chain (measured slower).
+// The per-side products (side, side_flux) form on the integer pipes (mulx, general case out
+// of line); the HLLD core keeps its products on the FP64 unit: the MHD and Hancock tiles run
+// two CTAs per SM, too few warps to cover the integer product's latency on that chain
+// (measured slower).
 
 // One side of the face in the local frame (un normal, ut in-plane tangential, uz = 0): what
 // the wave speeds and the star states need from both sides.
@@ -43,15 +44,15 @@ template <class T>
 __device__ __forceinline__ void side(Side<T>& S, T r, T p, T un, T ut, T bn, T bt, T bz,
                                      const Params& P) {
     S.r = r; S.p = p; S.un = un; S.ut = ut; S.bn = bn; S.bt = bt; S.bz = bz;
-    const T bn2 = mulx(bn, bn);
+    const T bn2 = mulx<true>(bn, bn);
     S.bb = fma(bz, bz, fma(bt, bt, bn2));
     S.pT = fma(0.5, S.bb, p);
-    const T gp = mulx(P.gamma, p);
+    const T gp = mulx<true>(P.gamma, p);
     const T a = gp + S.bb;
-    T disc = fma(a, a, mulx(mulx(-4.0, gp), bn2));
+    T disc = fma(a, a, mulx<true>(mulx<true>(-4.0, gp), bn2));
     disc = le_zero(disc) ? cst<T>(0.0) : disc;
-    const T X = mulx(0.5, a + sqrt_fast_im(disc));  // rho cf^2
-    S.cf = sqrt_over_im(X, r);                       // sqrt(X / r)
+    const T X = mulx<true>(0.5, a + sqrt_fast_im<true>(disc));  // rho cf^2
+    S.cf = sqrt_over_im<true>(X, r);                             // sqrt(X / r)
 }
 
 // a side's total energy and physical flux (mass, normal / tangential momentum, energy,
@@ -63,13 +64,15 @@ struct SideF {
 
 template <class T>
 __device__ __forceinline__ void side_flux(SideF<T>& F, const Side<T>& S, const Params& P) {
-    F.E = fma(S.p, P.inv_gm1, mulx(0.5, fma(S.r, fma(S.un, S.un, mulx(S.ut, S.ut)), S.bb)));
-    F.F0 = mulx(S.r, S.un);
+    F.E = fma(S.p, P.inv_gm1,
+              mulx<true>(0.5, fma(S.r, fma(S.un, S.un, mulx<true>(S.ut, S.ut)), S.bb)));
+    F.F0 = mulx<true>(S.r, S.un);
     F.F1 = fma(F.F0, S.un, fma(-S.bn, S.bn, S.pT));
-    F.F2 = fma(F.F0, S.ut, -mulx(S.bn, S.bt));
-    F.F4 = fma(F.E + S.pT, S.un, -mulx(S.bn, fma(S.ut, S.bt, mulx(S.un, S.bn))));
-    F.F6 = fma(S.un, S.bt, -mulx(S.ut, S.bn));
-    F.F7 = mulx(S.un, S.bz);
+    F.F2 = fma(F.F0, S.ut, -mulx<true>(S.bn, S.bt));
+    F.F4 = fma(F.E + S.pT, S.un,
+               -mulx<true>(S.bn, fma(S.ut, S.bt, mulx<true>(S.un, S.bn))));
+    F.F6 = fma(S.un, S.bt, -mulx<true>(S.ut, S.bn));
+    F.F7 = mulx<true>(S.un, S.bz);
 }
 
 // field-by-field select of one side (selects, no arithmetic)

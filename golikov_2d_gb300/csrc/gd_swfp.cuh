@@ -159,10 +159,25 @@ GD_HD uint64_t dmul_slow(uint64_t A, uint64_t B) {
     return S | bits;
 }
 
+#if defined(__CUDA_ARCH__)
+static __device__ __noinline__ uint64_t dmul_slow_call(uint64_t A, uint64_t B) {
+    return dmul_slow(A, B);
+}
+#endif
+
+// a * b rounded to nearest even, any operands.  OUTLINE: on the device the rare general case
+// is a call instead of an inlined copy, which keeps a kernel with many products smaller (the
+// call's register conventions can cost more than that saves in a kernel tight on registers).
+template <bool OUTLINE = false>
 GD_HD double mul_rn(double a, double b) {
     bool ok;
     double r = dmul_fast(a, b, ok);
+#if defined(__CUDA_ARCH__)
+    if (!ok) r = from_bits(OUTLINE ? dmul_slow_call(to_bits(a), to_bits(b))
+                                   : dmul_slow(to_bits(a), to_bits(b)));
+#else
     if (!ok) r = from_bits(dmul_slow(to_bits(a), to_bits(b)));
+#endif
     return r;
 }
 
