@@ -156,20 +156,20 @@ struct SideV {
 
 __device__ __forceinline__ void side_fwd(SideV& S, const double* q, const Params& P) {
     S.r = q[0]; S.p = q[1]; S.un = q[2]; S.ut = q[3]; S.bn = q[4]; S.bt = q[5]; S.bz = q[6];
-    S.bn2 = S.bn * S.bn;
+    S.bn2 = imul<true>(S.bn, S.bn);
     S.bb = fma(S.bz, S.bz, fma(S.bt, S.bt, S.bn2));
     S.pT = fma(0.5, S.bb, S.p);
-    S.gp = P.gamma * S.p;
+    S.gp = imul<true>(P.gamma, S.p);
     S.a = S.gp + S.bb;
-    double disc = fma(S.a, S.a, -4.0 * S.gp * S.bn2);
+    double disc = fma(S.a, S.a, imul<true>(imul<true>(-4.0, S.gp), S.bn2));
     S.disc0 = le_zero(disc);
     S.disc = S.disc0 ? 0.0 : disc;
     // sqrt_fast(disc) of the forward, keeping 1/sqrt(disc) for the reverse
     double sq;
-    sqrt_and_rs(S.disc, sq, S.rq);
-    const double X = 0.5 * (S.a + sq);
+    sqrt_and_rs_im<true>(S.disc, sq, S.rq);
+    const double X = imul<true>(0.5, S.a + sq);
     // cf = sqrt_over(X, r) of the forward, keeping its 1/sqrt(X r) for the reverse
-    sqrt_over_rs(X, S.r, S.cf, S.rs);
+    sqrt_over_rs_im<true>(X, S.r, S.cf, S.rs);
 }
 
 // per-side adjoint accumulators of the face state and of two derived quantities

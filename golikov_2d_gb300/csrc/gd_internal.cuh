@@ -406,22 +406,6 @@ __device__ __forceinline__ void sqrt_over_rs(double a, double r, double& c, doub
     c = fma(w, et, w);
     rs = fma(y, et, y);
 }
-// sqrt_over_rs with its products on the integer pipes: the same c as sqrt_over_im
-__device__ __forceinline__ void sqrt_over_rs_im(double a, double r, double& c, double& rs) {
-    if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
-        rs = rsqrt_times(a, r);
-        c = a * rs;
-        return;
-    }
-    float f;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
-    const double y = widen_f32(f);
-    const double w = swfp::mul_rn(a, y);
-    const double e = fma(-w, swfp::mul_rn(r, y), 1.0);
-    const double et = swfp::mul_rn(e, fma(0.375, e, 0.5));
-    c = fma(w, et, w);
-    rs = fma(y, et, y);
-}
 __device__ __forceinline__ double sqrt_over(double a, double r) {
     double c, rs;
     sqrt_over_rs(a, r, c, rs);
@@ -462,6 +446,40 @@ __device__ __forceinline__ double sqrt_over_im(double a, double r) {
     return fma(w, et, w);
 }
 
+// sqrt_and_rs with its products on the integer pipes: the same sx as sqrt_fast_im
+template <bool OUTLINE = false>
+__device__ __forceinline__ void sqrt_and_rs_im(double x, double& sx, double& ix) {
+    if (!rsqrt_ok(x)) {
+        sx = sqrt(x);
+        ix = 1.0 / sx;
+        return;
+    }
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double w = imul<OUTLINE>(x, y);
+    const double e = fma(-w, y, 1.0);
+    const double et = imul<OUTLINE>(e, fma(0.375, e, 0.5));
+    sx = fma(w, et, w);
+    ix = fma(y, et, y);
+}
+// sqrt_over_rs with its products on the integer pipes: the same c as sqrt_over_im
+template <bool OUTLINE = false>
+__device__ __forceinline__ void sqrt_over_rs_im(double a, double r, double& c, double& rs) {
+    if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
+        rs = rsqrt_times(a, r);
+        c = a * rs;
+        return;
+    }
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
+    const double y = widen_f32(f);
+    const double w = imul<OUTLINE>(a, y);
+    const double e = fma(-w, imul<OUTLINE>(r, y), 1.0);
+    const double et = imul<OUTLINE>(e, fma(0.375, e, 0.5));
+    c = fma(w, et, w);
+    rs = fma(y, et, y);
+}
 // isfinite(x) on the integer pipe: the exponent field is not all ones
 __device__ __forceinline__ bool finite_bits(double x) {
     return (mag(x) >> 53) != 0x7ffULL;
