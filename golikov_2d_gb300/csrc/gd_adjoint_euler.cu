@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(NT) eadj_update_kernel(Params P, CPlanes U, co
         double r2 = r - d[0];
         const bool rfl = le_zero(r2);
         if (rfl) r2 = 0.0001;
-        const double inv = rcp_fast(r2);
+        const double inv = rcp_2op(r2);
         const double mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
         const double u2 = imul(mx2, inv), v2 = imul(my2, inv);
         const double w = fma(u, u, imul(v, v));
@@ -113,8 +113,8 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     // ---- forward
     const double gpL = imul(g, pL), gpR = imul(g, pR);
     double cL, cR, rsL, rsR;  // sqrt_over(g p, rho) of the forward and 1/sqrt(g p rho)
-    sqrt_over_rs_im(gpL, rL, cL, rsL);
-    sqrt_over_rs_im(gpR, rR, cR, rsR);
+    cL = sqrt_over_2op(gpL, rL, &rsL);
+    cR = sqrt_over_2op(gpR, rR, &rsR);
     const double aL = unL - cL, aR = unR - cR;
     const double bL = unL + cL, bR = unR + cR;
     const bool slR = dlt(aR, aL);  // SL = dmin(aL, aR)
@@ -135,7 +135,7 @@ __device__ __forceinline__ void hllc_vjp(const double* a, const double* b, const
     double rb, pb, unb, utb, V2b, Sb = 0.0, sub = 0.0, mmb = 0.0, Nmb = 0.0, Db = 0.0;
     if (star) {
         const double X = fma(S, D, -Nm);
-        const double R = rcp_fast(imul(D, X));
+        const double R = rcp_2op(imul(D, X));
         const double NR = imul(Nm, R);
         const double SM = imul(NR, X);
         const double q = imul(NR, D);

@@ -78,6 +78,16 @@ __device__ __forceinline__ Dual sqrt_over(Dual a, Dual r) {
     if ((bits(a.v) << 1) == 0) return {v, 0.0};
     return {v, 0.5 * v * (a.d / a.v - r.d / r.v)};
 }
+// the values as the double versions compute them (the tangent takes the step's branches)
+__device__ __forceinline__ Dual rcp_2op(Dual x) {
+    const double r = rcp_2op(x.v);
+    return {r, -x.d * r * r};
+}
+__device__ __forceinline__ Dual sqrt_over_2op(Dual a, Dual r) {
+    const double v = sqrt_over_2op(a.v, r.v);
+    if ((bits(a.v) << 1) == 0) return {v, 0.0};
+    return {v, 0.5 * v * (a.d / a.v - r.d / r.v)};
+}
 __device__ __forceinline__ unsigned long long abs_bits(Dual x) { return abs_bits(x.v); }
 __device__ __forceinline__ unsigned long long mag(Dual x) { return mag(x.v); }
 __device__ __forceinline__ bool mag_lt(Dual a, Dual b) { return mag_lt(a.v, b.v); }

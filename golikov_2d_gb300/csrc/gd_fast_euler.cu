@@ -57,8 +57,8 @@ template <class T>
 __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
                                                T utR, const Params& P, T& UU) {
     const double g = P.gamma;
-    const T cL = sqrt_over_im(mulx(g, pL), rL);  // sqrt(g p / rho)
-    const T cR = sqrt_over_im(mulx(g, pR), rR);
+    const T cL = sqrt_over_2op(mulx(g, pL), rL);  // sqrt(g p / rho)
+    const T cR = sqrt_over_2op(mulx(g, pR), rR);
     const T aL = unL - cL, aR = unR - cR;
     const T bL = unL + cL, bR = unR + cR;
     const T SL = dmin(aL, aR);  // Davis estimates (kernel.cu:981-982)
@@ -93,7 +93,7 @@ __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T
         // S_M and q from one reciprocal: with X = S_K D - Nm = D (S_K - S_M),
         //   S_M = Nm X / (D X),  q = Nm D / (D X).
         const T X = fma(S, D, -Nm);
-        const T R = rcp_fast(mulx(D, X));
+        const T R = rcp_2op(mulx(D, X));
         const T NR = mulx(Nm, R);
         const T SM = mulx(NR, X);
         const T q = mulx(NR, D);
@@ -406,7 +406,7 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
         }
         T r2 = r - d[0];
         if (le_zero(r2)) { r2 = cst<T>(0.0001); ++nfl_r; }
-        const T inv = rcp_fast(r2);
+        const T inv = rcp_2op(r2);
         const T mx2 = fma(r, u, -d[2]), my2 = fma(r, v, -d[3]);
         const T u2 = mulx(mx2, inv);
         const T v2 = mulx(my2, inv);

@@ -480,6 +480,68 @@ __device__ __forceinline__ void sqrt_over_rs_im(double a, double r, double& c, d
     c = fma(w, et, w);
     rs = fma(y, et, y);
 }
+// ---------------------------------------------------------------------------------------
+// Root and reciprocal in two FP64 operations.  The Newton corrections above,
+//   sqrt(a / r) = w (1 + e/2 + 3 e^2 / 8),   1 / x = y (1 + e + e^2),
+// take three: the residual e, the polynomial in e, the final multiply-add.  The quadratic
+// term is 2^-40 or less of the result, so FP32 resolves it: w (3 e^2 / 8) (or y e^2) is formed
+// in FP32 as a count of w's last place (at most 2^22) and added to w's bit pattern (integer
+// pipe); the final multiply-add then takes w e/2 (or y e) on top.  An addition that carries
+// into w's exponent field counts the places beyond the binade boundary at the doubled size
+// (halved, rounded).  Relative error about 1 ulp, as the three-operation forms.
+// ---------------------------------------------------------------------------------------
+// e as an FP32 value from its high word (20 bits of mantissa); 0 for |e| < 2^-126
+__device__ __forceinline__ float small_f32(double e) {
+    uint32_t hi, lo;
+    swfp::halves(e, hi, lo);
+    return ((hi >> 20) & 0x7ffu) > 896u ? seed_f32(e) : 0.0f;
+}
+// w (1 + t / 2^52) for normal w and 0 <= t < 2^-31 2^52 (t given scaled by 2^52), on the
+// integer pipe; the magnitude grows by t / 2^52 of itself (either sign of w)
+__device__ __forceinline__ double grow_rel(double w, float t) {
+    uint32_t hi, lo;
+    swfp::halves(w, hi, lo);
+    const float mant = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3));  // [1, 2)
+    const uint32_t m = __float_as_uint(fmaf(mant, t, 12582912.0f)) - 0x4b400000u;  // round
+    uint32_t nlo = lo + m;
+    const uint32_t c = nlo < lo ? 1u : 0u;
+    if (c && (hi & 0xfffffu) == 0xfffffu) nlo = (nlo + 1u) >> 1;  // into the next binade
+    return swfp::from_halves(hi + c, nlo);
+}
+// exactly x / 2 for |x| >= 2^-1021 or x = +-0 (exponent field decremented)
+__device__ __forceinline__ double half_exact(double x) {
+    uint32_t hi, lo;
+    swfp::halves(x, hi, lo);
+    return swfp::from_halves((hi & 0x7ff00000u) != 0u ? hi - 0x100000u : hi, lo);
+}
+// sqrt(a / r) as sqrt_over_im, and (with rs) 1/sqrt(a r), the root in two FP64 operations
+__device__ __forceinline__ double sqrt_over_2op(double a, double r, double* rs = nullptr) {
+    if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
+        const double q = rsqrt_times(a, r);
+        if (rs) *rs = q;
+        return a * q;
+    }
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(seed23_f32(a) * seed23_f32(r)));
+    const double y = widen_f32(f);
+    const double w = imul(a, y);
+    const double e = fma(-w, imul(r, y), 1.0);
+    const float ef = small_f32(e);
+    const double wq = grow_rel(w, (ef * ef) * 1688849860263936.0f);  // 3/8 2^52
+    if (rs) *rs = fma(y, imul(e, fma(0.375, e, 0.5)), y);
+    return fma(half_exact(w), e, wq);
+}
+// 1/x as rcp_fast, in two FP64 operations
+__device__ __forceinline__ double rcp_2op(double x) {
+    if (!in_f32_range(x)) return 1.0 / x;
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(seed_f32(x)));
+    const double y = widen_f32(r);
+    const double e = fma(-x, y, 1.0);
+    const float ef = small_f32(e);
+    return fma(y, e, grow_rel(y, (ef * ef) * 4503599627370496.0f));  // 2^52
+}
+
 // isfinite(x) on the integer pipe: the exponent field is not all ones
 __device__ __forceinline__ bool finite_bits(double x) {
     return (mag(x) >> 53) != 0x7ffULL;
