@@ -117,6 +117,24 @@ def ncu_fp64_per_cell(workload):
     return None
 
 
+def int_products_per_cell(workload):
+    """Binary64 products per cell the step kernel forms on the integer pipes (gd_swfp.cuh),
+    from the `int_products=<n>` token of the workload's line in profiles/ncu_traffic.txt."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if parts and parts[0] == workload:
+            for tok in parts[3:]:
+                if tok.startswith("int_products="):
+                    try:
+                        return float(tok.split("=", 1)[1])
+                    except ValueError:
+                        return None
+    return None
+
+
 def ncu_l2_hit_pct(workload):
     """L2 sector hit rate of the step kernel (lts__t_sector_hit_rate) where the committed ncu
     summary records one, as an `l2hit=<percent>` token of the workload's line."""
@@ -241,6 +259,17 @@ def fp64_roofline(g, workload, cells_per_s, torch, sm_mhz=None):
         out.update({"ops_per_cell": per_cell, "achieved": ach, "frac": ach / pipe_peak_ops,
                     "frac_of_dfma_loop": ach / (probe / 2.0),
                     "ops_source": OPS_SOURCE})
+        ip = int_products_per_cell(workload)
+        if ip is not None:
+            # the binary64 arithmetic of a cell is the FP64-pipe operations plus the products
+            # formed on the integer pipes (bit-identical to FP64 multiplies)
+            b64 = (per_cell + ip) * cells_per_s
+            out.update({"int_pipe_products_per_cell": ip,
+                        "binary64_ops_per_cell": per_cell + ip,
+                        "binary64_achieved": b64,
+                        "binary64_vs_fp64_pipe_peak": b64 / pipe_peak_ops,
+                        "int_products_source": "count of integer-pipe products in the kernel "
+                                               "source per cell, profiles/ncu_traffic.txt"})
     return out
 
 
