@@ -288,7 +288,8 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
     __syncthreads();
 
     // ---- U: update (kernel.cu:2606-2660 in Heaviside-Lorentz field units) ----------------------
-    const double kx = T_do * P.inv_dx, ky = T_do * P.inv_dy;
+    const double kx = imul<true>(T_do, P.inv_dx), ky = imul<true>(T_do, P.inv_dy);
+    const double hkx = half_exact(kx), hky = half_exact(ky);  // 0.5 kx, 0.5 ky
     const bool axi = P.geometry == GD_AXISYM;
     bool any_active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
@@ -319,7 +320,7 @@ __device__ __forceinline__ void mhd_tile(const Params& P, const IN& in, const OU
         // Powell divergence from cell-centred field: dx dy div b (kernel.cu:2568-2604)
         const T bxE = c[4 * PS + 1], bxW = c[4 * PS - 1];
         const T byN = c[5 * PS + SX], byS = c[5 * PS - SX];
-        T divb = fma(0.5 * kx, bxE - bxW, 0.5 * ky * (byN - byS));  // T_do * div b
+        T divb = fma(hkx, bxE - bxW, mulx<true>(hky, byN - byS));  // T_do * div b
         const double iy = axi ? rcp_fast(P.y0 + gy * P.dy) : 0.0;
         if (axi) divb = fma(T_do * by, iy, divb);                 // kernel.cu:2615
         if constexpr (std::is_same<T, double>::value) {
