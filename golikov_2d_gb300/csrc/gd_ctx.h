@@ -17,7 +17,10 @@ namespace gd {
 // The banded step is captured once per (host buffers, current plane set) into a CUDA graph
 // and replayed: a graph launch puts all of a step's copies and launches on the GPU at once,
 // where enqueuing them one API call at a time (a dozen per band) paces a short step.
-constexpr int kMaxBands = 64;
+// At most 32 bands: every band's upload and download is a copy of its own, and at 64 bands
+// the per-copy cost outweighed the shorter fill and drain (KH 4096^2 host to host: 4.42 ms
+// per step at 64 bands, 4.26 at 32, 4.50 at 16).
+constexpr int kMaxBands = 32;
 constexpr int kCompStreams = 3;  // the caller's stream and two more
 constexpr int kStepGraphs = 4;   // cached step graphs (two per ping-pong pair of host buffers)
 struct StepGraph {

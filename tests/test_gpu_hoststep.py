@@ -23,7 +23,7 @@ CASES = {
     "hancock_parity": lambda: problems.hancock_wind(160, 96, mode=g.MODE_PARITY),
     "hancock_fast": lambda: problems.hancock_wind(160, 96),
     "hancock_fast_ragged": lambda: problems.hancock_wind(131, 77, scheme=g.SCHEME_HANCOCK),
-    # grids of many bands (16 to 53)
+    # grids of many bands (16 to 32, the most a step takes)
     "kh2048x1024_many_bands": lambda: problems.kelvin_helmholtz(2048, 1024),
     "ot1024_many_bands": lambda: problems.orszag_tang(1024, 1024),
     "hancock_fast_many_bands": lambda: problems.hancock_wind(1024, 640),
