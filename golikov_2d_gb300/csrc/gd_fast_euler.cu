@@ -9,7 +9,10 @@
 //   U  conservative update of each cell from its four face fluxes, positivity floors,
 //      primitive recovery; store; block dt minimum and the fused funk_time rotation.
 // The reference computes every face twice, once from each neighbour (kernel.cu:3560-3586);
-// here each face is computed once and used with opposite signs by its two cells.
+// here each face is computed once and used with opposite signs by its two cells.  The
+// standalone products run on the integer pipes (mulx: the FP64 multiply's bits), the sound
+// speeds and reciprocals take two FP64 operations each (sqrt_over_2op, rcp_2op), and the
+// HLLC star state takes S_M and q from one reciprocal.
 //
 // Each tile shape is a separate template instantiation; the compiler may fuse multiply-adds
 // differently in each, so shapes agree to rounding (~1e-14 relative per step), not bit for

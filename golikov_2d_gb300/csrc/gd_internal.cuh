@@ -1,9 +1,11 @@
 // gd_internal.cuh -- device-side types and helpers shared by the step kernels.
 //
 // FP64 on GB300 issues at a small fraction of the FP32 rate, so the step is bound by the
-// FP64 pipe, not by HBM.  Everything that does not need FP64 arithmetic is done on the
+// FP64 pipe, not by HBM.  Everything that does not need the FP64 unit is done on the
 // integer pipe here: sign tests, absolute values, minmod selection and max-reductions
-// work on the IEEE-754 bit patterns.
+// work on the IEEE-754 bit patterns, binary64 products can be formed there bit for bit
+// (imul, from gd_swfp.cuh), and the small second-order terms of the Newton corrections are
+// added into bit patterns (grow_rel).
 #pragma once
 
 #include <cstdint>
