@@ -372,7 +372,7 @@ __device__ __noinline__ void euler_tile(const Params& P, const IN& in, const OUT
     __syncthreads();
 
     // ---- U: update --------------------------------------------------------------------------
-    const double kx = imul(T_do, P.inv_dx), ky = imul(T_do, P.inv_dy);
+    const double kx = T_do * P.inv_dx, ky = T_do * P.inv_dy;
     bool any_active = false;
     unsigned int nfl_r = 0, nfl_p = 0, nbad = 0;
     for (int i = tid; i < TX * TY; i += NT) {

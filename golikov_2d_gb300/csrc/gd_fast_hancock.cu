@@ -46,44 +46,63 @@ constexpr size_t kSmemBytes = sizeof(double) * (kUnion + 3 * kPred + 2 * PY + TX
 
 constexpr int BNT = 128;  // band kernel
 
-// physical flux of state s = {r, p, u, v, bx, by, bz} (b units) through an x face and a
-// y face, components {mass, energy, mom x, mom y, bx, by, bz}
-__device__ __forceinline__ void flux_x(const double* s, double ig, double* F) {
-    const double r = s[0], p = s[1], u = s[2], v = s[3], bx = s[4], by = s[5], bz = s[6];
-    const double bb = fma(bz, bz, fma(by, by, bx * bx));
-    const double pT = fma(0.5, bb, p);
-    const double E = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
+// Half the jump F(m + h) - F(m - h) of the physical flux through a face, in its local frame
+// (normal velocity u, tangential v, no z velocity; field bn, bt, bz in b units), by the product
+// rule: the predictor's flux differences of kernel.cu:1611-1720 without forming the two
+// fluxes (no cancellation between them).  For a product, (a + x)(b + y) - (a - x)(b - y) =
+// 2 (a y + x b); the cubic and quartic terms expand the same way.  G = gamma / (gamma - 1).
+// Components: mass, energy, normal and tangential momentum, tangential and z field (the normal
+// field's flux is 0).
+struct FluxJump {
+    double m, e, mn, mt, bt, bz;
+};
+__device__ __forceinline__ FluxJump flux_jump(double r, double p, double u, double v, double bn,
+                                              double bt, double bz, double rh, double ph,
+                                              double uh, double vh, double bnh, double bth,
+                                              double bzh, double G) {
+    FluxJump J;
     const double ru = r * u;
-    F[0] = ru;
-    F[1] = fma(E + pT, u, -bx * fma(u, bx, v * by));
-    F[2] = fma(ru, u, pT - bx * bx);
-    F[3] = fma(ru, v, -bx * by);
-    F[4] = 0.0;
-    F[5] = fma(u, by, -v * bx);
-    F[6] = u * bz;
-}
-__device__ __forceinline__ void flux_y(const double* s, double ig, double* F) {
-    const double r = s[0], p = s[1], u = s[2], v = s[3], bx = s[4], by = s[5], bz = s[6];
-    const double bb = fma(bz, bz, fma(by, by, bx * bx));
-    const double pT = fma(0.5, bb, p);
-    const double E = fma(p, ig, 0.5 * fma(r, fma(u, u, v * v), bb));
-    const double rv = r * v;
-    F[0] = rv;
-    F[1] = fma(E + pT, v, -by * fma(u, bx, v * by));
-    F[2] = fma(rv, u, -bx * by);
-    F[3] = fma(rv, v, pT - by * by);
-    F[4] = fma(v, bx, -u * by);
-    F[5] = 0.0;
-    F[6] = v * bz;
+    const double A0 = fma(r, uh, rh * u);  // half the jump of r u
+    const double rhuh = rh * uh;
+    const double u2 = fma(u, u, uh * uh);
+    J.m = A0;
+    // r u^2 + p + (bt^2 + bz^2 - bn^2) / 2
+    J.mn = fma(bt, bth, fma(bz, bzh, fma(-bn, bnh, fma(rh, u2, fma(twice_exact(ru), uh, ph)))));
+    // r u v - bn bt
+    const double X = fma(bn, bth, bnh * bt);
+    J.mt = fma(ru, vh, fma(A0, v, fma(rhuh, vh, -X)));
+    // u bt - v bn; u bz
+    J.bt = fma(u, bth, fma(uh, bt, -fma(v, bnh, vh * bn)));
+    J.bz = fma(u, bzh, uh * bz);
+    // energy: G p u + r u (u^2 + v^2) / 2 + u (bt^2 + bz^2) - v bn bt
+    const double S = u2 + fma(v, v, vh * vh);
+    const double kin = fma(half_exact(A0), S, (ru + rhuh) * fma(u, uh, v * vh));
+    const double Tb = fma(bt, bth, bz * bzh);
+    const double Sb = fma(bt, bt, fma(bth, bth, fma(bz, bz, bzh * bzh)));
+    const double Y = fma(bn, bt, bnh * bth);
+    J.e = fma(G, fma(p, uh, ph * u),
+              fma(twice_exact(u), Tb, fma(uh, Sb, fma(-v, X, fma(-vh, Y, kin)))));
+    return J;
 }
 
-// Q + sgn D/2 with the reference's fallback of rho and p to Q when <= 0 (kernel.cu:1640-1680)
-__device__ __forceinline__ void half_state(const double* Q, const double* D, double sgn,
-                                           double* S) {
+// The predictor's face states Q +- D/2 as mean m and half-difference h: rho and p from the
+// two states with the reference's fallback to Q where <= 0 (kernel.cu:1640-1680); the other
+// fields m = Q, h = D/2 exactly.
+__device__ __forceinline__ void mean_half(const double* Q, const double* D, double* m,
+                                          double* h) {
 #pragma unroll
-    for (int f = 0; f < NF; ++f) S[f] = fma(0.5 * sgn, D[f], Q[f]);
-    S[0] = le_zero(S[0]) ? Q[0] : S[0];
-    S[1] = le_zero(S[1]) ? Q[1] : S[1];
+    for (int f = 0; f < 2; ++f) {
+        double a = fma(0.5, D[f], Q[f]), b = fma(-0.5, D[f], Q[f]);
+        a = le_zero(a) ? Q[f] : a;
+        b = le_zero(b) ? Q[f] : b;
+        m[f] = half_exact(a + b);
+        h[f] = half_exact(a - b);
+    }
+#pragma unroll
+    for (int f = 2; f < NF; ++f) {
+        m[f] = Q[f];
+        h[f] = half_exact(D[f]);
+    }
 }
 
 template <bool VYP>
@@ -150,6 +169,7 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
     const double T_do = *T_do_ptr;
     const double st = 0.5 * T_do;
     const double sx = st * P.inv_dx, sy = st * P.inv_dy;
+    const double sx2 = twice_exact(sx), sy2 = twice_exact(sy);
     for (int i = tid; i < PY * PX; i += NT) {
         const int py = i / PX, px = i - py * PX;
         if ((px == 0 || px == PX - 1) && (py == 0 || py == PY - 1)) continue;
@@ -167,22 +187,24 @@ __global__ void __launch_bounds__(NT) hancock_tile_kernel(Params P, CPlanes in, 
             DX[3] = DX[1];
             DY[3] = DY[1];
         }
-        // predictor (kernel.cu:1611-1720): flux differences of the four face states
+        // predictor (kernel.cu:1611-1720): the flux differences of the face states Q +- D/2,
+        // 2 sx J_x + 2 sy J_y with J the half jumps (x: normal u, field bx; y: normal v, by)
         double d[NF];
         {
-            double Sp[NF], Sm[NF], Fp[NF], Fm[NF];
-            half_state(Q, DX, 1.0, Sp);
-            half_state(Q, DX, -1.0, Sm);
-            flux_x(Sp, ig, Fp);
-            flux_x(Sm, ig, Fm);
-#pragma unroll
-            for (int f = 0; f < NF; ++f) d[f] = sx * (Fp[f] - Fm[f]);
-            half_state(Q, DY, 1.0, Sp);
-            half_state(Q, DY, -1.0, Sm);
-            flux_y(Sp, ig, Fp);
-            flux_y(Sm, ig, Fm);
-#pragma unroll
-            for (int f = 0; f < NF; ++f) d[f] = fma(sy, Fp[f] - Fm[f], d[f]);
+            double m[NF], h[NF];
+            mean_half(Q, DX, m, h);
+            const FluxJump Jx = flux_jump(m[0], m[1], m[2], m[3], m[4], m[5], m[6], h[0], h[1],
+                                          h[2], h[3], h[4], h[5], h[6], P.g_gm1);
+            mean_half(Q, DY, m, h);
+            const FluxJump Jy = flux_jump(m[0], m[1], m[3], m[2], m[5], m[4], m[6], h[0], h[1],
+                                          h[3], h[2], h[5], h[4], h[6], P.g_gm1);
+            d[0] = fma(sy2, Jy.m, sx2 * Jx.m);
+            d[1] = fma(sy2, Jy.e, sx2 * Jx.e);
+            d[2] = fma(sy2, Jy.mt, sx2 * Jx.mn);
+            d[3] = fma(sy2, Jy.mn, sx2 * Jx.mt);
+            d[4] = sy2 * Jy.bt;
+            d[5] = sx2 * Jx.bt;
+            d[6] = fma(sy2, Jy.bz, sx2 * Jx.bz);
         }
         const double sty = st * rowiy[py];
         const double r = Q[0], p = Q[1], u = Q[2], v = Q[3], bx = Q[4], by = Q[5], bz = Q[6];

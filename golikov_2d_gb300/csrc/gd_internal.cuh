@@ -516,6 +516,14 @@ __device__ __forceinline__ double half_exact(double x) {
     swfp::halves(x, hi, lo);
     return swfp::from_halves((hi & 0x7ff00000u) != 0u ? hi - 0x100000u : hi, lo);
 }
+// exactly 2 x for |x| < 2^1023 (exponent field incremented; +-0 and subnormals take the FP64
+// sum)
+__device__ __forceinline__ double twice_exact(double x) {
+    uint32_t hi, lo;
+    swfp::halves(x, hi, lo);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    return (e - 1u) < 2045u ? swfp::from_halves(hi + 0x100000u, lo) : x + x;
+}
 // sqrt(a / r) as sqrt_over_im, and (with rs) 1/sqrt(a r), the root in two FP64 operations
 __device__ __forceinline__ double sqrt_over_2op(double a, double r, double* rs = nullptr) {
     if (!(in_half_range_pos(a) && in_half_range_pos(r))) {
