@@ -41,16 +41,16 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
          k += (long long)gridDim.x * blockDim.x) {
         const double r = U.f[0][k], p = U.f[1][k], u = U.f[2][k], v = U.f[3][k];
         // rounded products, as the forward update has them (see ld_b)
-        const double bx = __dmul_rn(U.f[4][k], kInvSpi4), by = __dmul_rn(U.f[5][k], kInvSpi4);
-        const double bz = __dmul_rn(U.f[6][k], kInvSpi4);
+        const double bx = imul(U.f[4][k], kInvSpi4), by = imul(U.f[5][k], kInvSpi4);
+        const double bz = imul(U.f[6][k], kInvSpi4);
         double d[NF];
 #pragma unroll
         for (int f = 0; f < NF; ++f) d[f] = aux[(size_t)f * K + k];
         const double divb = aux[(size_t)7 * K + k];
         // forward (same operations as the tile update)
-        const double ub = fma(u, bx, v * by);
-        const double bb = fma(bz, bz, fma(by, by, bx * bx));
-        const double E = fma(p, P.inv_gm1, 0.5 * fma(r, fma(u, u, v * v), bb));
+        const double ub = fma(u, bx, imul(v, by));
+        const double bb = fma(bz, bz, fma(by, by, imul(bx, bx)));
+        const double E = fma(p, P.inv_gm1, half_exact(fma(r, fma(u, u, imul(v, v)), bb)));
         double r2 = r - d[0];
         const bool rfl = le_zero(r2);
         if (rfl) r2 = r;
@@ -61,15 +61,15 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
         const double bz2 = bz - d[6];
         const double E2 = E - fma(ub, divb, d[1]);
         const double inv = rcp_fast(r2);
-        const double u2 = mx2 * inv, v2 = my2 * inv;
-        const double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, v2 * v2),
-                                          fma(bz2, bz2, fma(by2, by2, bx2 * bx2)))) * P.gm1;
+        const double u2 = imul(mx2, inv), v2 = imul(my2, inv);
+        const double p2 = (E2 - 0.5 * fma(r2, fma(u2, u2, imul(v2, v2)),
+                                          fma(bz2, bz2, fma(by2, by2, imul(bx2, bx2))))) * P.gm1;
         const bool pfl = le_zero(p2);
         // reverse
         double r2b = lam_out.f[0][k], p2b = lam_out.f[1][k];
         double u2b = lam_out.f[2][k], v2b = lam_out.f[3][k];
-        double bx2b = lam_out.f[4][k] * kSpi4, by2b = lam_out.f[5][k] * kSpi4;
-        double bz2b = lam_out.f[6][k] * kSpi4;
+        double bx2b = imul(lam_out.f[4][k], kSpi4), by2b = imul(lam_out.f[5][k], kSpi4);
+        double bz2b = imul(lam_out.f[6][k], kSpi4);
         double E2b = 0.0;
         if (!pfl) {
             E2b = p2b * P.gm1;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(NT) adj_update_kernel(Params P, CPlanes U, con
             by2b += Xb * 2.0 * by2;
             bz2b += Xb * 2.0 * bz2;
         }
-        const double mx2b = u2b * inv, my2b = v2b * inv;
+        const double mx2b = imul(u2b, inv), my2b = imul(v2b, inv);
         const double invb = u2b * mx2 + v2b * my2;
         r2b += -invb * inv * inv;
         double rb = 0.0, pb = 0.0, ub_ = 0.0, vb = 0.0, bxb = 0.0, byb = 0.0, bzb = 0.0;

@@ -510,20 +510,9 @@ __device__ __forceinline__ double grow_rel(double w, float t) {
     if (c && (hi & 0xfffffu) == 0xfffffu) nlo = (nlo + 1u) >> 1;  // into the next binade
     return swfp::from_halves(hi + c, nlo);
 }
-// exactly x / 2 for |x| >= 2^-1021 or x = +-0 (exponent field decremented)
-__device__ __forceinline__ double half_exact(double x) {
-    uint32_t hi, lo;
-    swfp::halves(x, hi, lo);
-    return swfp::from_halves((hi & 0x7ff00000u) != 0u ? hi - 0x100000u : hi, lo);
-}
-// exactly 2 x for |x| < 2^1023 (exponent field incremented; +-0 and subnormals take the FP64
-// sum)
-__device__ __forceinline__ double twice_exact(double x) {
-    uint32_t hi, lo;
-    swfp::halves(x, hi, lo);
-    const uint32_t e = (hi >> 20) & 0x7ffu;
-    return (e - 1u) < 2045u ? swfp::from_halves(hi + 0x100000u, lo) : x + x;
-}
+// x / 2 and 2 x, exactly as the FP64 unit rounds them, on the integer pipe (swfp)
+__device__ __forceinline__ double half_exact(double x) { return swfp::half_rn(x); }
+__device__ __forceinline__ double twice_exact(double x) { return swfp::twice_rn(x); }
 // sqrt(a / r) as sqrt_over_im, and (with rs) 1/sqrt(a r), the root in two FP64 operations
 __device__ __forceinline__ double sqrt_over_2op(double a, double r, double* rs = nullptr) {
     if (!(in_half_range_pos(a) && in_half_range_pos(r))) {

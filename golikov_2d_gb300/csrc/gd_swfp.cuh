@@ -159,6 +159,34 @@ GD_HD uint64_t dmul_slow(uint64_t A, uint64_t B) {
     return S | bits;
 }
 
+// x / 2 and 2 x rounded to nearest even, every input, on the integer pipe: the exponent
+// field moves by one; at the bottom of the range the magnitude shifts (a subnormal half
+// rounds its dropped bit to even; a doubled subnormal may become normal, which the shifted
+// pattern encodes as it is); 2 x above the range is infinity; infinities and NaN pass through.
+GD_HD double half_rn(double x) {
+    uint32_t hi, lo;
+    halves(x, hi, lo);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (e == 0x7ffu) return x;
+    if (e >= 2u) return from_halves(hi - 0x100000u, lo);
+    const uint32_t sign = hi & 0x80000000u, mh = hi & 0x7fffffffu;
+    uint32_t nl = (lo >> 1) | (mh << 31), nh = mh >> 1;
+    const uint32_t rnd = lo & nl & 1u;  // dropped bit set and the result odd: to even
+    nl += rnd;
+    nh += (nl < rnd) ? 1u : 0u;
+    return from_halves(sign | nh, nl);
+}
+GD_HD double twice_rn(double x) {
+    uint32_t hi, lo;
+    halves(x, hi, lo);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    const uint32_t sign = hi & 0x80000000u;
+    if (e == 0x7ffu) return x;
+    if (e == 0x7feu) return from_halves(sign | 0x7ff00000u, 0u);
+    if (e != 0u) return from_halves(hi + 0x100000u, lo);
+    return from_halves(sign | ((hi << 1) & 0x7fffffffu) | (lo >> 31), lo << 1);
+}
+
 #if defined(__CUDA_ARCH__)
 static __device__ __noinline__ uint64_t dmul_slow_call(uint64_t A, uint64_t B) {
     return dmul_slow(A, B);

@@ -1,5 +1,5 @@
-// Host check of gd::swfp (the integer-pipe binary64 multiplication) against the host's
-// IEEE-754 multiplication.  Usage: swfp_check <cases per class> <seed>.  Prints one line per
+// Host check of gd::swfp (the integer-pipe binary64 multiplication, halving and doubling)
+// against the host's IEEE-754 arithmetic.  Usage: swfp_check <cases per class> <seed>.  Prints one line per
 // class; exits 1 if any result differs from a * b (two NaNs count as equal: the integer
 // path returns the canonical quiet NaN) or if the fast path accepts a case and is wrong.
 #include <cstdio>
@@ -101,6 +101,37 @@ int main(int argc, char** argv) {
         }
         printf("%-22s cases %lld fast path %lld mismatches %lld\n", names[cls], n, fast, bad);
         failed += bad != 0;
+    }
+    // x / 2 and 2 x (half_rn, twice_rn) against the host's x * 0.5 and x + x
+    {
+        const char* hn[] = {"half/twice any bits", "half/twice subnormal and edges"};
+        for (int cls = 0; cls < 2; ++cls) {
+            long long bad = 0;
+            for (long long i = 0; i < n; ++i) {
+                const uint64_t r1 = next64(), r3 = next64();
+                double x;
+                if (cls == 0) {
+                    x = from_bits(r1);
+                } else {
+                    const uint64_t e = (r3 & 3) == 0 ? 0 : (r3 & 3) == 1 ? 1 : (r3 & 3) == 2 ? 2046 : 2045;
+                    x = make((r3 >> 8) & 1, e, r1 >> ((r3 >> 16) % 53));
+                }
+                const double h = half_rn(x), t = twice_rn(x);
+                const double H = x * 0.5, T = x + x;
+                const bool okh = to_bits(h) == to_bits(H) || (std::isnan(h) && std::isnan(H));
+                const bool okt = to_bits(t) == to_bits(T) || (std::isnan(t) && std::isnan(T));
+                if (!okh || !okt) {
+                    if (bad < 5)
+                        printf("MISMATCH %s: x %016llx half %016llx (%016llx) twice %016llx (%016llx)\n",
+                               hn[cls], (unsigned long long)to_bits(x), (unsigned long long)to_bits(h),
+                               (unsigned long long)to_bits(H), (unsigned long long)to_bits(t),
+                               (unsigned long long)to_bits(T));
+                    ++bad;
+                }
+            }
+            printf("%-22s cases %lld mismatches %lld\n", hn[cls], n, bad);
+            failed += bad != 0;
+        }
     }
     return failed ? 1 : 0;
 }

@@ -1,10 +1,12 @@
 """The IEEE-754 binary64 multiplication on the integer pipes (golikov_2d_gb300/csrc/gd_swfp.cuh)
-that the fast Euler and MHD kernels use for part of their products.  On the CPU the header is
+that the fast Euler and MHD kernels use for part of their products, and its exact halving and
+doubling.  On the CPU the header is
 compiled for the host and checked against the host's multiplication bit for bit on random bit
 patterns, typical magnitudes, products near the overflow and underflow limits, short
 significands (exact products and halfway cases), zeros, all-ones significands, subnormal
 operands, infinities and NaNs (two NaNs count as equal: the integer path returns the
-canonical quiet NaN).  On the GPU, gd_check_int_mul compares the device code with the FP64
+canonical quiet NaN); halving and doubling against x * 0.5 and x + x on random bit patterns
+and on subnormals and the exponent range's edges.  On the GPU, gd_check_int_mul compares the device code with the FP64
 unit's multiply."""
 import os
 import shutil
@@ -26,7 +28,7 @@ def test_integer_multiply_matches_host_ieee(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout[-3000:]
     lines = [ln for ln in r.stdout.splitlines() if "cases" in ln]
-    assert len(lines) == 8
+    assert len(lines) == 10
     assert all(ln.split()[-1] == "0" for ln in lines)
 
 
