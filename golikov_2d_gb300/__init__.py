@@ -47,7 +47,7 @@ EXPORTS = (
     "gd_init_dt", "gd_advance", "gd_get_stats", "gd_field_ptr", "gd_launch_count",
     "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
     "gd_probe_fp64_peak", "gd_probe_faces", "gd_step_ref_static", "gd_alloc_counts",
-    "gd_check_int_mul",
+    "gd_check_int_mul", "gd_check_fast_roots",
     "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
     "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance", "gd_batch_autotune",
     "gd_batch_get_stats", "gd_batch_get_info", "gd_batch_launch_count",
@@ -146,6 +146,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.gd_step_ref_static.argtypes = [cfgp, vp, vp, vp, vp, vp, vp, vp, vp, i, vp]
     L.gd_alloc_counts.argtypes = [ctypes.POINTER(ll), ctypes.POINTER(ll)]
     L.gd_check_int_mul.argtypes = [ll, ctypes.c_ulonglong, ctypes.POINTER(ll)]
+    L.gd_check_fast_roots.argtypes = [ll, ctypes.c_ulonglong, ctypes.POINTER(ll)]
     L.gd_adj_forward.argtypes = [vp, i, i, vp]
     for name in ("gd_adj_backward", "gd_tangent", "gd_adj_replay"):
         getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
@@ -177,11 +178,13 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                  "gd_set_dt_policy", "gd_advance_to", "gd_step_host", "gd_set_floor_limit",
                  "gd_get_stats", "gd_field_ptr", "gd_probe_fp64_peak", "gd_probe_faces",
                  "gd_step_ref_static", "gd_alloc_counts", "gd_check_int_mul",
+                 "gd_check_fast_roots",
                  "gd_batch_create", "gd_batch_destroy", "gd_batch_import", "gd_batch_export",
                  "gd_batch_set_time", "gd_batch_init_dt", "gd_batch_advance",
                  "gd_batch_autotune", "gd_batch_get_stats", "gd_batch_get_info",
                  "gd_adj_forward", "gd_adj_backward", "gd_tangent", "gd_adj_replay",
-                 "gd_adj_switches", "gd_format_text", "gd_write_text", "gd_parse_text", "gd_read_text",
+                 "gd_adj_switches", "gd_format_text", "gd_write_text", "gd_parse_text",
+                 "gd_read_text",
                  "gd_write_binary", "gd_read_binary", "gd_format_tecplot", "gd_write_tecplot"):
         getattr(L, name).restype = i
     _lib = L
@@ -534,6 +537,16 @@ def check_int_mul(pairs: int = 1 << 24, seed: int = 1) -> dict:
     c = (ctypes.c_longlong * 4)()
     _check(L.gd_check_int_mul(int(pairs), int(seed), c), "gd_check_int_mul")
     return {"mismatches": c[0], "nan_payload": c[1], "slow_path": c[2], "checked": c[3]}
+
+
+def check_fast_roots(count: int = 1 << 24, seed: int = 1) -> dict:
+    """Largest errors, in units of the last place, of the step's two-operation reciprocal and
+    root against IEEE division and square root (gd_check_fast_roots)."""
+    L = load()
+    c = (ctypes.c_longlong * 4)()
+    _check(L.gd_check_fast_roots(int(count), int(seed), c), "gd_check_fast_roots")
+    return {"rcp_2op_ulp": c[0], "sqrt_over_2op_ulp": c[1], "sqrt_over_ulp": c[2],
+            "checked": c[3]}
 
 
 def alloc_counts() -> tuple[int, int]:

@@ -539,6 +539,12 @@ gd_status gd_check_int_mul(long long pairs, unsigned long long seed, long long* 
     return GD_OK;
 }
 
+gd_status gd_check_fast_roots(long long count, unsigned long long seed, long long* out) {
+    if (!out || count <= 0 || count > (1LL << 34)) return GD_ERR_INVALID_ARG;
+    GD_CUDA(gd::check_roots(count, seed, out));
+    return GD_OK;
+}
+
 gd_status gd_probe_faces(int physics, int method, double gamma, int axis, long long n,
                          const double* L, const double* R, double* flux, double* speed,
                          gd_stream stream) {

@@ -149,6 +149,7 @@ cudaError_t launch_dt_commit(Scalars* sc, cudaStream_t st);
 cudaError_t launch_reset_T(Scalars* sc, cudaStream_t st);
 cudaError_t probe_fp64_peak(double* flops);
 cudaError_t check_imul(long long pairs, unsigned long long seed, long long* out);
+cudaError_t check_roots(long long count, unsigned long long seed, long long* out);
 
 // Every device and pinned-host allocation and release the library makes goes through these
 // (gd_api.cu), which count them for gd_alloc_counts.

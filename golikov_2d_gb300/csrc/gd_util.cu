@@ -245,6 +245,65 @@ __global__ void check_imul_kernel(unsigned long long* counts, unsigned long long
 }
 }  // namespace
 
+// The two-operation reciprocal and root against IEEE division and square root on seeded
+// values (reciprocals of +-[2^-100, 2^100], roots sqrt(a / r) of a, r in [2^-50, 2^50]):
+// the largest distance in units of the last place of the IEEE result.  The IEEE sqrt(a / r)
+// rounds twice (the quotient, then the root), so it is itself within one unit of the exact
+// root.  out: max ulp of rcp_2op, of sqrt_over_2op, of the three-operation sqrt_over, count.
+__device__ __forceinline__ double ulp_dist(double x, double ref) {
+    const long long d = bits(x) - bits(ref);
+    return (double)(d < 0 ? -d : d);
+}
+__global__ void check_roots_kernel(unsigned long long* out, unsigned long long seed, int n) {
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    double m0 = 0, m1 = 0, m2 = 0;
+    for (int i = 0; i < n; ++i) {
+        const unsigned long long r1 = mix64(seed + 3 * (t * n + i)), r2 = mix64(r1 + 1),
+                                 r3 = mix64(r2 + 2);
+        const double x = from_bits((long long)((r1 & 0x800fffffffffffffULL) |
+                                               ((923ULL + (r3 >> 8) % 201) << 52)));
+        const double a = from_bits((long long)((r2 & 0x000fffffffffffffULL) |
+                                               ((973ULL + (r3 >> 20) % 101) << 52)));
+        const double r = from_bits((long long)((r3 & 0x000fffffffffffffULL) |
+                                               ((973ULL + (r1 >> 52) % 101) << 52)));
+        double q;
+        asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(q) : "d"(1.0), "d"(x));
+        m0 = fmax(m0, ulp_dist(rcp_2op(x), q));
+        double ar, sr;
+        asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(ar) : "d"(a), "d"(r));
+        asm volatile("sqrt.rn.f64 %0, %1;" : "=d"(sr) : "d"(ar));
+        m1 = fmax(m1, ulp_dist(sqrt_over_2op(a, r), sr));
+        m2 = fmax(m2, ulp_dist(sqrt_over(a, r), sr));
+    }
+    atomicMax(out + 0, (unsigned long long)m0);
+    atomicMax(out + 1, (unsigned long long)m1);
+    atomicMax(out + 2, (unsigned long long)m2);
+    atomicAdd(out + 3, (unsigned long long)n);
+}
+
+cudaError_t check_roots(long long count, unsigned long long seed, long long* out) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 4, threads = 256;
+    const long long per = (count + (long long)blocks * threads - 1) / ((long long)blocks * threads);
+    unsigned long long* c = nullptr;
+    e = gd::dev_alloc(&c, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        check_roots_kernel<<<blocks, threads>>>(c, seed, (int)(per < 1 ? 1 : per));
+        e = cudaGetLastError();
+    }
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, c, sizeof h, cudaMemcpyDeviceToHost);
+    gd::dev_free(c);
+    for (int i = 0; i < 4; ++i) out[i] = (long long)h[i];
+    return e;
+}
+
 cudaError_t check_imul(long long pairs, unsigned long long seed, long long* out) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);

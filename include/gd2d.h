@@ -396,6 +396,14 @@ gd_status gd_probe_fp64_peak(double* flops_out);
  * the integer fast path, [3]: pairs checked.  Blocking. */
 gd_status gd_check_int_mul(long long pairs, unsigned long long seed, long long* counts_out);
 
+/* Diagnostic (no reference counterpart): the Euler step's two-operation reciprocal and root
+ * against IEEE division and square root on about `count` seeded values (reciprocals of
+ * +-[2^-100, 2^100]; sqrt(a / r) for a, r in [2^-50, 2^50], whose IEEE form rounds twice).
+ * out[0]: largest distance of the reciprocal in units of the last place, out[1]: of the
+ * root, out[2]: of the three-operation root the MHD step uses, out[3]: values checked.
+ * Blocking. */
+gd_status gd_check_fast_roots(long long count, unsigned long long seed, long long* out);
+
 /* Diagnostic (no reference counterpart): how many device or pinned-host allocations
  * (cudaMalloc, cudaMallocHost) and releases (cudaFree, cudaFreeHost) this library has made
  * in this process, over all contexts and threads.  Every allocation of the library goes
