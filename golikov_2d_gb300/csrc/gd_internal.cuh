@@ -494,24 +494,9 @@ __device__ __forceinline__ void sqrt_over_rs_im(double a, double r, double& c, d
 // 67 M values): the reciprocal within 1 ulp of 1/x, the root within 2 ulp of the IEEE
 // sqrt(a / r) -- which itself rounds twice -- where the three-operation root stays within 1.
 // ---------------------------------------------------------------------------------------
-// e as an FP32 value from its high word (20 bits of mantissa); 0 for |e| < 2^-126
-__device__ __forceinline__ float small_f32(double e) {
-    uint32_t hi, lo;
-    swfp::halves(e, hi, lo);
-    return ((hi >> 20) & 0x7ffu) > 896u ? seed_f32(e) : 0.0f;
-}
-// w (1 + t / 2^52) for normal w and 0 <= t < 2^-31 2^52 (t given scaled by 2^52), on the
-// integer pipe; the magnitude grows by t / 2^52 of itself (either sign of w)
-__device__ __forceinline__ double grow_rel(double w, float t) {
-    uint32_t hi, lo;
-    swfp::halves(w, hi, lo);
-    const float mant = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3));  // [1, 2)
-    const uint32_t m = __float_as_uint(fmaf(mant, t, 12582912.0f)) - 0x4b400000u;  // round
-    uint32_t nlo = lo + m;
-    const uint32_t c = nlo < lo ? 1u : 0u;
-    if (c && (hi & 0xfffffu) == 0xfffffu) nlo = (nlo + 1u) >> 1;  // into the next binade
-    return swfp::from_halves(hi + c, nlo);
-}
+// e as an FP32 value (high word), and w grown by t 2^-52 of itself on the integer pipe (swfp)
+__device__ __forceinline__ float small_f32(double e) { return swfp::high_f32(e); }
+__device__ __forceinline__ double grow_rel(double w, float t) { return swfp::grow_rel(w, t); }
 // x / 2 and 2 x, exactly as the FP64 unit rounds them, on the integer pipe (swfp)
 __device__ __forceinline__ double half_exact(double x) { return swfp::half_rn(x); }
 __device__ __forceinline__ double twice_exact(double x) { return swfp::twice_rn(x); }

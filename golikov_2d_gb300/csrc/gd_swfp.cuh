@@ -23,6 +23,7 @@
 // checked against the host's IEEE multiplication on the CPU.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -185,6 +186,53 @@ GD_HD double twice_rn(double x) {
     if (e == 0x7feu) return from_halves(sign | 0x7ff00000u, 0u);
     if (e != 0u) return from_halves(hi + 0x100000u, lo);
     return from_halves(sign | ((hi << 1) & 0x7fffffffu) | (lo >> 31), lo << 1);
+}
+
+GD_HD float f32_from_bits(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float f;
+    std::memcpy(&f, &b, sizeof f);
+    return f;
+#endif
+}
+GD_HD uint32_t bits_of_f32(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t b;
+    std::memcpy(&b, &f, sizeof b);
+    return b;
+#endif
+}
+// e as an FP32 value from its high word (20 bits of mantissa, truncated); 0 for |e| < 2^-126
+GD_HD float high_f32(double e) {
+    uint32_t hi, lo;
+    halves(e, hi, lo);
+    if (((hi >> 20) & 0x7ffu) <= 896u) return 0.0f;
+    return f32_from_bits((hi & 0x80000000u) | (((hi & 0x7fffffffu) - (896u << 20)) << 3));
+}
+// w (1 + t 2^-52) for normal w and 0 <= t < 2^21 (the relative growth below 2^-31): the
+// increment, w t 2^-52 in units of w's last place (at most 2^22), formed in FP32 and added to
+// w's bit pattern; the magnitude grows (either sign of w).  An addition that carries into the
+// exponent field counts the places beyond the binade boundary at the doubled size (halved,
+// rounded half up).  Within one unit of the last place of the exact value.
+GD_HD double grow_rel(double w, float t) {
+    uint32_t hi, lo;
+    halves(w, hi, lo);
+    // w's significand in [1, 2) from its leading 23 bits
+    const float mant = f32_from_bits(0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29));
+#if defined(__CUDA_ARCH__)
+    const float q = fmaf(mant, t, 12582912.0f);
+#else
+    const float q = std::fmaf(mant, t, 12582912.0f);
+#endif
+    const uint32_t m = bits_of_f32(q) - 0x4b400000u;  // round(mant t)
+    uint32_t nlo = lo + m;
+    const uint32_t c = nlo < lo ? 1u : 0u;
+    if (c && (hi & 0xfffffu) == 0xfffffu) nlo = (nlo + 1u) >> 1;  // into the next binade
+    return from_halves(hi + c, nlo);
 }
 
 #if defined(__CUDA_ARCH__)

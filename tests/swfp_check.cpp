@@ -133,5 +133,34 @@ int main(int argc, char** argv) {
             failed += bad != 0;
         }
     }
+    // grow_rel: w (1 + t 2^-52) against the exact value in extended precision, within one unit
+    // of the result's last place; a quarter of the cases with w's mantissa near all ones, so
+    // that the increment carries into the exponent field
+    {
+        long long bad = 0, carried = 0;
+        for (long long i = 0; i < n; ++i) {
+            const uint64_t r1 = next64(), r3 = next64();
+            uint64_t frac = r1 & 0xfffffffffffffULL;
+            if ((r3 & 3) == 0) frac = 0xfffffffffffffULL - (r1 % 4194304);
+            const double w = make((r3 >> 2) & 1, 1000 + (r3 >> 8) % 60, frac);
+            const float t = (float)((r3 >> 32) % 2097152) + (float)((r3 >> 16) & 0xffff) / 65536.0f;
+            const double g = grow_rel(w, t);
+            const long double ex = (long double)w * (1.0L + (long double)t / 4503599627370496.0L);
+            const double er = (double)ex;
+            const uint64_t gb = to_bits(g), eb = to_bits(er);
+            const uint64_t d = gb > eb ? gb - eb : eb - gb;
+            carried += ((gb >> 52) & 0x7ff) != ((to_bits(w) >> 52) & 0x7ff);
+            if (d > 1) {
+                if (bad < 5)
+                    printf("MISMATCH grow_rel: w %016llx t %.9g -> %016llx, exact %016llx\n",
+                           (unsigned long long)to_bits(w), t, (unsigned long long)gb,
+                           (unsigned long long)eb);
+                ++bad;
+            }
+        }
+        printf("%-22s cases %lld mismatches %lld (binade carries %lld)\n", "grow_rel", n, bad,
+               carried);
+        failed += bad != 0;
+    }
     return failed ? 1 : 0;
 }

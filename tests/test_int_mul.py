@@ -28,8 +28,8 @@ def test_integer_multiply_matches_host_ieee(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout[-3000:]
     lines = [ln for ln in r.stdout.splitlines() if "cases" in ln]
-    assert len(lines) == 10
-    assert all(ln.split()[-1] == "0" for ln in lines)
+    assert len(lines) == 11
+    assert all(ln.split()[ln.split().index("mismatches") + 1] == "0" for ln in lines)
 
 
 @pytest.mark.gpu
