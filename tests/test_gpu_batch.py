@@ -98,3 +98,20 @@ def test_looped_sync_equals_looped(cuda):
         assert st1.t == st2.t and st1.dt == st2.dt
     with pytest.raises(g.GdError):
         run_batch(grids, 1, schedule=g.BATCH_LOOPED_SYNC, use_graph=True)
+
+
+def test_persistent_16x16_keeps_four_ctas_per_sm(cuda):
+    """The persistent kernel of the default 16x16 tile runs four CTAs per SM, as the
+    single-grid step does (registers and shared memory both allow four).  Its register count
+    is sensitive to the tile function's code: at 74 registers it fell to three CTAs per SM
+    and the batched step slowed by 13 %."""
+    import torch
+    grids = problems.batch_four_quadrant(64, lo=64, hi=512, seed=5)
+    b = g.Batch([c for c, *_ in grids])
+    for k, (c, s, u, _) in enumerate(grids):
+        b.import_grid(k, s, u)
+    info = b.info()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    b.close()
+    assert (info.tile_x, info.tile_y) == (16, 16)
+    assert info.ctas == min(4 * sms, info.tiles), (info.ctas, sms)
