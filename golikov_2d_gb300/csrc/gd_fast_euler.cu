@@ -120,6 +120,9 @@ __device__ __forceinline__ FluxE<T> hllc_local(T rL, T pL, T unL, T utL, T rR, T
 // hllc_local): sound speed 0 where rho <= 0, D_L = min(un) - max(c), D_R = max(un) + max(c),
 // the upwind physical flux when the fan lies on one side of the face (strict tests against
 // Omega = 0, kernel.cu:11), else (D_R F_L - D_L F_R + D_L D_R (U_R - U_L)) / (D_R - D_L).
+// Its products stay on the FP64 unit: the tile function holds both fluxes, and registers
+// are allocated for its heavier path -- integer-pipe products here took the tile to about
+// 110 registers a thread, two CTAs per SM for the HLLC step as well.
 template <class T>
 __device__ __forceinline__ FluxE<T> hll_local(T rL, T pL, T unL, T utL, T rR, T pR, T unR,
                                               T utR, const Params& P, T& UU) {
